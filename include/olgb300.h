@@ -1,0 +1,170 @@
+/*
+ * olgb300.h -- C-ABI of libolgb300.so, the GB300 (sm_103a) engine behind the
+ * OpenOL propagation / hologram calls.
+ *
+ * The reference (somamake/openol) is a header-only C++ template library; its
+ * callers instantiate ol::gAsmProp, ol::gFresnelProp, ol::ARSSFresnelProp,
+ * ol::Prop, ol::gCgh, ol::WRPMethod ... directly.  Each entry point below is
+ * what those templates reduce to once the template and RAII layers are peeled
+ * off: raw device pointers (thrust::complex<float> == float2 == 8 bytes
+ * interleaved re/im, row-major), sizes, physical parameters, a CUDA stream.
+ * The drop-in C++ headers in include/openol_gb300/ and the Python mirror in
+ * openol_gb300/ both call these functions; each comment names the reference
+ * function (file:line in the reference project) that the entry point replaces.
+ *
+ * Conventions
+ *  - Return value: OLG_OK (0) or a negative OLG_ERR_* code; never exits,
+ *    never throws.  olg_last_error() gives a message for the calling thread.
+ *  - Asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream).
+ *  - `work`/`work_bytes`: optional caller-provided device scratch of at least
+ *    the size reported by the matching *_workspace_bytes() query.  With
+ *    work == NULL the library takes stream-ordered scratch from the CUDA memory
+ *    pool (cudaMallocAsync / cudaFreeAsync on `stream`).
+ *  - In-place operation is allowed wherever an input and an output pointer
+ *    have the same shape (u_in == u_out).
+ *  - Sizes: the FFT engine handles ny, nx powers of two in [32, 4096]
+ *    (padded grid 64 .. 8192); other sizes return OLG_ERR_UNSUPPORTED_SIZE.
+ */
+#ifndef OLGB300_H
+#define OLGB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OLG_OK 0
+#define OLG_ERR_INVALID_ARG (-1)
+#define OLG_ERR_UNSUPPORTED_SIZE (-2)
+#define OLG_ERR_CUDA (-3)
+#define OLG_ERR_WORKSPACE (-4)
+#define OLG_ERR_NOMEM (-5)
+
+/* flags */
+#define OLG_CONJ 0x1         /* adjoint operator (conjugate transfer function / chirps) */
+#define OLG_NO_NORMALIZE 0x2 /* host-pointer overload convention: no 1/Np factors */
+#define OLG_ACCUMULATE 0x4   /* out += result (gCghReduction semantics) */
+#define OLG_VERBOSE 0x8      /* print the chosen method like the reference's printf */
+#define OLG_CHECK_F32 0x10   /* olg_prop_c64: evaluate the AUTO checks in float (PREC_T=float) */
+
+/* propagation modes, ol::PROPMODE (oldefine.h:7-9) */
+#define OLG_ASM 0
+#define OLG_FRESNEL 1
+#define OLG_AUTO 2
+
+/* complex2img modes, ol::MODE (olimg.h:268) */
+#define OLG_PHASE 0
+#define OLG_REAL 1
+#define OLG_IMAG 2
+#define OLG_AMP 3
+
+/* WRP windows */
+#define OLG_WINDOW_CIRCLE 0 /* WRPStep1   golcgh.h:291-378 */
+#define OLG_WINDOW_SQUARE 1 /* WRPStep1_D golcgh.h:392-491 */
+
+typedef void *olg_stream_t;
+
+/* ---------------------------------------------------------------- library */
+int olg_version(void);
+const char *olg_status_string(int status);
+/* Message of the last failing call on this host thread ("" if none). */
+const char *olg_last_error(void);
+/* Number of kernels this library has launched so far in this process. */
+unsigned long long olg_launch_count(void);
+
+/* ------------------------------------------------------------ propagation */
+/* Device scratch for one propagation of an ny x nx field (any method). */
+size_t olg_prop_workspace_bytes(int ny, int nx);
+
+/* Angular spectrum method.  Replaces ol::gAsmProp (device overload,
+ * golprop.h:507-534): u_out = crop(IFFT(H * FFT(pad(u_in)) / Np)).
+ * OLG_NO_NORMALIZE reproduces the host-pointer overload (golprop.h:458-504,
+ * no 1/Np); OLG_CONJ applies the adjoint (conj H). */
+int olg_asm_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                     double z, int flags, void *work, size_t work_bytes, olg_stream_t stream);
+
+/* Fresnel propagation (convolution with the sampled impulse response).
+ * Replaces ol::gFresnelProp (device overload golprop.h:167-198; host overload
+ * golprop.h:70-124 with OLG_NO_NORMALIZE) and, with bandlimit = 1,
+ * ol::gFresnelPropBandLimit (golprop.h:202-302). */
+int olg_fresnel_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx,
+                         double lambda, double z, int bandlimit, int flags, void *work, size_t work_bytes,
+                         olg_stream_t stream);
+
+/* ARSS scaled Fresnel propagation.  Replaces ol::ARSSFresnelProp
+ * (golprop.h:941-995): pre-chirp with window, pad, FFT/Np, x FFT(chirp_s)/Np,
+ * IFFT, crop, post-chirp inside its window.  s in {0, 1} is rejected
+ * (OLG_ERR_INVALID_ARG): the reference's window limits divide by s|s-1|. */
+int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx, double lambda,
+                      double z, double s, double oy, double ox, int flags, void *work, size_t work_bytes,
+                      olg_stream_t stream);
+
+/* AUTO method selection, ol::AsmPropCheck (olprop.h:209-225) and
+ * ol::FresnelPropCheck (olprop.h:109-123); single_precision != 0 evaluates
+ * them in float like the reference's PREC_T=float instantiation.  1 = pass. */
+int olg_asm_prop_check(int ny, int nx, double dy, double dx, double lambda, double z, int single_precision);
+int olg_fresnel_prop_check(int ny, int nx, double dy, double dx, double lambda, double z, int single_precision);
+
+/* Dispatcher.  Replaces ol::Prop (device overload, golprop.h:578-604):
+ * mode OLG_ASM / OLG_FRESNEL / OLG_AUTO; AUTO picks ASM, else Fresnel, else
+ * band-limited Fresnel.  *chosen (nullable) receives 0 ASM, 1 Fresnel,
+ * 2 band-limited Fresnel.  In place on u. */
+int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, double lambda, double z, int mode, int flags,
+                 int *chosen, void *work, size_t work_bytes, olg_stream_t stream);
+
+/* ------------------------------------------------------------------- CGH */
+/* Points are AoS float32 triples (x, y, z) in metres, ol::Vect3<float>
+ * (olclass.h:45-52) as held by ol::gObject (golclass.h:58-71).  Pixel (w, h)
+ * sits at (px*w, py*h) (corner origin, golcgh.h:75-76).  amp / phase0 are
+ * optional per-point float arrays (NULL = 1 and 0). */
+
+/* Fresnel-form CGH, U[h,w] = sum_j a_j exp(i(pi rho^2 / (lambda z_j) + phi_j)).
+ * Replaces ol::gCgh / gCghShared (golcgh.h:47-145) and, with OLG_ACCUMULATE,
+ * ol::gCghReduction (golcgh.h:147-195).  phase_out (nullable, float ny x nx)
+ * receives atan2(Im U, Re U) like the phase kernels golcgh.h:5-45; U may be
+ * NULL when only the phase is wanted. */
+int olg_cgh_fresnel_c64(const float *points, const float *amp, const float *phase0, int n_points, void *U,
+                        float *phase_out, int ny, int nx, double py, double px, double lambda, int flags,
+                        olg_stream_t stream);
+
+/* Exact spherical-wave CGH, U = sum_j a_j exp(i(k r_j + phi_j)) / r_j
+ * (the kernel commented out at golcgh.h:218,323).  FP32 terms with the phase
+ * range reduced per pixel tile in double-float arithmetic. */
+int olg_cgh_exact_c64(const float *points, const float *amp, const float *phase0, int n_points, void *U,
+                      int ny, int nx, double py, double px, double lambda, int flags, olg_stream_t stream);
+
+/* ------------------------------------------------------------------- WRP */
+/* plane_z of ol::WRPMethod (golcgh.h:561-581, window = circle) and
+ * ol::WRPMethod_D (golcgh.h:519-559, window = square), float arithmetic as
+ * there; plimit <= 0 means plimit = p. */
+float olg_wrp_plane_z(int window, int ny, int nx, float p, float plimit, float lambda, float zmin, float s);
+
+/* WRP step 1.  Replaces ol::WRPStep1 (golcgh.h:369-389, circle window) and
+ * ol::WRPStep1_D (golcgh.h:470-491, square window): U (ny x nx) is
+ * overwritten with sum_j [inside window_j] exp(i pi rho^2 / (lambda dz_j)) / |dz_j|,
+ * dz_j = z_j - plane_z.  Window radii and membership follow the reference's
+ * float32 expressions; plimit <= 0 means plimit = p. */
+int olg_wrp_step1_c64(const float *points, int n_points, void *U, int ny, int nx, float p, float lambda,
+                      float plane_z, float plimit, int window, olg_stream_t stream);
+
+/* Whole WRP method: step 1 onto the plane at olg_wrp_plane_z(), then
+ * ol::WRPStep2 (golcgh.h:494-517): propagate by plane_z with `propmode`
+ * (AUTO falls back to ASM, not band-limited Fresnel, as there).
+ * Replaces ol::WRPMethod / ol::WRPMethod_D.  *plane_z_out is nullable. */
+int olg_wrp_method_c64(const float *points, int n_points, void *U, int ny, int nx, float p, float lambda,
+                       float zmin, float s, float plimit, int window, int propmode, int flags,
+                       float *plane_z_out, olg_stream_t stream);
+
+/* ------------------------------------------------------------ quantisers */
+/* ol::complex2img(u, img, ny, nx, MODE) (olimg.h:348-391): per-pixel value
+ * (phase / real / imag / amplitude), min-max (phase: -pi..pi) normalised to
+ * round(255 (v - min) / (max - min)); a constant image maps to 0. */
+int olg_complex2img_u8(const void *u, uint8_t *img, int ny, int nx, int mode, olg_stream_t stream);
+/* Binarised 8-bit hologram (project rule): 255 where Re(U) >= 0, else 0. */
+int olg_binarize_u8(const void *u, uint8_t *img, int ny, int nx, olg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,16 @@
+"""openol_gb300 -- GB300-native (sm_103a) engine for OpenOL's propagation and
+hologram hot path, behind the reference's own API names.
+
+The compute lives in libolgb300.so (C-ABI: include/olgb300.h).  This package is
+the host-side mirror of the reference's golprop.h / golcgh.h / olimg.h calls,
+with PyTorch CUDA tensors standing in for the reference's device buffers.
+"""
+from ._lib import OlgError, launch_count, lib  # noqa: F401
+from .cgh import (Object2cuda, WRPMethod, WRPMethod_D, WRPStep1, WRPStep1_D, WRPStep2,  # noqa: F401
+                  cgh_exact, cgh_fresnel, gCgh, gCghReduction, gObject, wrp_plane_z)
+from .img import MODE, binarize, complex2img  # noqa: F401
+from .prop import (ASM, AUTO, FRESNEL, PROPMODE, ARSSFresnelProp, AsmPropCheck, FresnelPropCheck,  # noqa: F401
+                   Prop, arss_prop, asm_prop, fresnel_prop, gAsmProp, gFresnelProp, gFresnelPropBandLimit,
+                   workspace, workspace_bytes)
+
+__version__ = "0.1.0"

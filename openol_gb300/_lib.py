@@ -1,0 +1,85 @@
+"""ctypes binding of libolgb300.so (the C-ABI declared in include/olgb300.h).
+
+The library is the product: there is no CPU fallback.  Importing a routine
+whose library is missing raises immediately, and every non-zero status of the
+C-ABI is raised as ``OlgError`` (the analogue of the reference's
+``CHECK_CUDA_ERROR`` throwing ``std::runtime_error``, golclass.h:9-21).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libolgb300.so")
+
+OLG_OK = 0
+OLG_CONJ = 0x1
+OLG_NO_NORMALIZE = 0x2
+OLG_ACCUMULATE = 0x4
+OLG_VERBOSE = 0x8
+OLG_CHECK_F32 = 0x10
+
+_d, _f, _i, _p, _sz = C.c_double, C.c_float, C.c_int, C.c_void_p, C.c_size_t
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "olg_version": (_i, []),
+    "olg_status_string": (C.c_char_p, [_i]),
+    "olg_last_error": (C.c_char_p, []),
+    "olg_launch_count": (C.c_ulonglong, []),
+    "olg_prop_workspace_bytes": (_sz, [_i, _i]),
+    "olg_asm_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_fresnel_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _i, _p, _sz, _p]),
+    "olg_arss_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_asm_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),
+    "olg_fresnel_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),
+    "olg_prop_c64": (_i, [_p, _i, _i, _d, _d, _d, _d, _i, _i, C.POINTER(_i), _p, _sz, _p]),
+    "olg_cgh_fresnel_c64": (_i, [_p, _p, _p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p]),
+    "olg_cgh_exact_c64": (_i, [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d, _i, _p]),
+    "olg_wrp_plane_z": (_f, [_i, _i, _i, _f, _f, _f, _f, _f]),
+    "olg_wrp_step1_c64": (_i, [_p, _i, _p, _i, _i, _f, _f, _f, _f, _i, _p]),
+    "olg_wrp_method_c64": (_i, [_p, _i, _p, _i, _i, _f, _f, _f, _f, _f, _i, _i, _i, C.POINTER(_f), _p]),
+    "olg_complex2img_u8": (_i, [_p, _p, _i, _i, _i, _p]),
+    "olg_binarize_u8": (_i, [_p, _p, _i, _i, _p]),
+}
+
+
+class OlgError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        super().__init__(f"{where}: status {status}: {msg}")
+        self.status = status
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def check(status: int, where: str) -> None:
+    if status != OLG_OK:
+        L = lib()
+        raise OlgError(status, where, (L.olg_last_error() or b"").decode() or L.olg_status_string(status).decode())
+
+
+def call(name: str, *args):
+    fn = getattr(lib(), name)
+    rc = fn(*args)
+    check(rc, name)
+    return rc
+
+
+def launch_count() -> int:
+    return int(lib().olg_launch_count())

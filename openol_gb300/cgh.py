@@ -1,0 +1,155 @@
+"""Point-cloud CGH and the WRP method: the Python mirror of golcgh.h.
+
+Point clouds are ``gObject`` instances holding a CUDA float32 tensor of shape
+(N, 3) -- the reference's ``ol::gObject<float>`` (golclass.h:58-71), an AoS of
+``Vect3<float>``.  Holograms are CUDA complex64 tensors (ny, nx), or float32
+tensors for the phase-output kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from ._lib import OLG_ACCUMULATE, OLG_VERBOSE, call, lib
+from .prop import PROPMODE, _dev_field, _stream
+
+
+class gObject:
+    """Device point cloud, ol::gObject<float> (golclass.h:58-71)."""
+
+    def __init__(self, points, device="cuda"):
+        if isinstance(points, int):
+            self.points = torch.zeros((points, 3), dtype=torch.float32, device=device)
+        else:
+            t = torch.as_tensor(np.asarray(points, dtype=np.float32) if not isinstance(points, torch.Tensor)
+                                else points)
+            self.points = t.to(device=device, dtype=torch.float32).reshape(-1, 3).contiguous()
+
+    @property
+    def size(self) -> int:
+        return int(self.points.shape[0])
+
+    def __len__(self):
+        return self.size
+
+
+def Object2cuda(obj) -> gObject:
+    """ol::Object2cuda (golclass.h:73-78): host (N, 3) points -> gObject."""
+    if isinstance(obj, gObject):
+        return obj
+    return gObject(obj)
+
+
+def _opt(t):
+    if t is None:
+        return None
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
+        raise TypeError("per-point arrays must be contiguous CUDA float32 tensors")
+    return t.data_ptr()
+
+
+def cgh_fresnel(gobj, U=None, *, ny, nx, py, px, lam, amp=None, phase0=None, phase_out=None, accumulate=False,
+                stream=None):
+    """Fresnel-form CGH (olg_cgh_fresnel_c64): U[h,w] = sum_j a_j exp(i(pi rho^2/(lambda z_j) + phi_j))."""
+    if U is not None:
+        _dev_field(U, ny, nx, "U")
+    if phase_out is not None and (phase_out.dtype != torch.float32 or not phase_out.is_cuda):
+        raise TypeError("phase_out must be a CUDA float32 tensor")
+    call("olg_cgh_fresnel_c64", gobj.points.data_ptr(), _opt(amp), _opt(phase0), gobj.size,
+         U.data_ptr() if U is not None else None, phase_out.data_ptr() if phase_out is not None else None,
+         ny, nx, float(py), float(px), float(lam), OLG_ACCUMULATE if accumulate else 0, _stream(stream))
+    return U if U is not None else phase_out
+
+
+def cgh_exact(gobj, U, *, ny, nx, py, px, lam, amp=None, phase0=None, accumulate=False, stream=None):
+    """Exact spherical CGH (olg_cgh_exact_c64): U = sum_j a_j exp(i(k r_j + phi_j)) / r_j."""
+    _dev_field(U, ny, nx, "U")
+    call("olg_cgh_exact_c64", gobj.points.data_ptr(), _opt(amp), _opt(phase0), gobj.size, U.data_ptr(), ny, nx,
+         float(py), float(px), float(lam), OLG_ACCUMULATE if accumulate else 0, _stream(stream))
+    return U
+
+
+def gCgh(gobj, U, ny, nx, *params):
+    """ol::gCgh.  gCgh(gobj, U, ny, nx, p, lambda) -> complex hologram (gCghShared,
+    golcgh.h:137-145); gCgh(gobj, U, ny, nx, py, px, lambda) -> complex hologram
+    (golcgh.h:108-135) or, when U is a float32 tensor, its phase (golcgh.h:26-45)."""
+    if len(params) == 2:
+        p, lam = params
+        py = px = p
+    elif len(params) == 3:
+        py, px, lam = params
+    else:
+        raise TypeError("gCgh(gobj, U, ny, nx, p, lambda) or gCgh(gobj, U, ny, nx, py, px, lambda)")
+    if U.dtype == torch.float32:
+        return cgh_fresnel(gobj, None, ny=ny, nx=nx, py=py, px=px, lam=lam, phase_out=U)
+    return cgh_fresnel(gobj, U, ny=ny, nx=nx, py=py, px=px, lam=lam)
+
+
+def gCghReduction(gobj, U, ny, nx, p, lam):
+    """ol::gCghReduction (golcgh.h:147-195): U += the Fresnel-form hologram."""
+    return cgh_fresnel(gobj, U, ny=ny, nx=nx, py=p, px=p, lam=lam, accumulate=True)
+
+
+# ---------------------------------------------------------------------- WRP
+def wrp_plane_z(window, ny, nx, p, lam, zmin, s, p_limit=None) -> float:
+    return float(lib().olg_wrp_plane_z(int(window), ny, nx, p, 0.0 if p_limit is None else p_limit, lam, zmin, s))
+
+
+def _wrp_step1(obj, U, ny, nx, p, lam, d, plimit, window):
+    _dev_field(U, ny, nx, "U")
+    call("olg_wrp_step1_c64", obj.points.data_ptr(), obj.size, U.data_ptr(), ny, nx, float(p), float(lam),
+         float(d), 0.0 if plimit is None else float(plimit), int(window), _stream())
+    return U
+
+
+def WRPStep1(obj, U, ny, nx, p, lam, d, plimit=None):
+    """ol::WRPStep1 (golcgh.h:369-389): circular windows W_j = |z_j - d| / sqrt(4 (p/lambda)^2 - 1)."""
+    return _wrp_step1(obj, U, ny, nx, p, lam, d, plimit, 0)
+
+
+def WRPStep1_D(obj, U, ny, nx, p, lam, d, plimit=None):
+    """ol::WRPStep1_D (golcgh.h:470-491): square windows of side D_j = sqrt(2) W_j."""
+    return _wrp_step1(obj, U, ny, nx, p, lam, d, plimit, 1)
+
+
+def WRPStep2(U, ny, nx, p, lam, d, propmode=PROPMODE.AUTO, verbose=True):
+    """ol::WRPStep2 (golcgh.h:494-517)."""
+    from .prop import AsmPropCheck, FresnelPropCheck, asm_prop, fresnel_prop
+    _dev_field(U, ny, nx, "U")
+    V = U.view(ny, nx)
+    if propmode == PROPMODE.FRESNEL:
+        return fresnel_prop(V, dy=p, dx=p, lam=lam, z=d)
+    if propmode == PROPMODE.ASM:
+        return asm_prop(V, dy=p, dx=p, lam=lam, z=d)
+    if AsmPropCheck(ny, nx, p, p, lam, d):
+        if verbose:
+            print("WRP Step2 is AsmProp")
+        return asm_prop(V, dy=p, dx=p, lam=lam, z=d)
+    if not FresnelPropCheck(ny, nx, p, p, lam, d):
+        if verbose:
+            print("warning!!\neither AsmProp or FresnelProp does not meet the condition.")
+        return asm_prop(V, dy=p, dx=p, lam=lam, z=d)
+    if verbose:
+        print("WRP Step2 is FresnelProp")
+    return fresnel_prop(V, dy=p, dx=p, lam=lam, z=d)
+
+
+def _wrp_method(obj, U, ny, nx, p, lam, zmin, s, propmode, p_limit, window, verbose):
+    _dev_field(U, ny, nx, "U")
+    pz = C.c_float(0.0)
+    call("olg_wrp_method_c64", obj.points.data_ptr(), obj.size, U.data_ptr(), ny, nx, float(p), float(lam),
+         float(zmin), float(s), 0.0 if p_limit is None else float(p_limit), int(window), int(propmode),
+         OLG_VERBOSE if verbose else 0, C.byref(pz), _stream())
+    return U, pz.value
+
+
+def WRPMethod(obj, U, ny, nx, p, lam, zmin, s=0.9, propmode=PROPMODE.AUTO, verbose=True):
+    """ol::WRPMethod (golcgh.h:561-581).  Returns (U, plane_z)."""
+    return _wrp_method(obj, U, ny, nx, p, lam, zmin, s, propmode, None, 0, verbose)
+
+
+def WRPMethod_D(obj, U, ny, nx, p, lam, zmin, s=0.9, propmode=PROPMODE.AUTO, p_limit=None, verbose=True):
+    """ol::WRPMethod_D (golcgh.h:519-559, p_limit overload :540-559).  Returns (U, plane_z)."""
+    return _wrp_method(obj, U, ny, nx, p, lam, zmin, s, propmode, p_limit, 1, verbose)

@@ -1,0 +1,687 @@
+// prop.cu -- fused ASM / Fresnel / ARSS propagation on GB300 (sm_103a).
+//
+// The reference runs each propagation as ~8 full-size elementwise kernels
+// plus 2-3 cuFFT calls over a 2x zero-padded grid (golprop.h:507-534 for ASM,
+// 167-198 Fresnel, 941-995 ARSS), synchronising after every step.  Here one
+// propagation of an ny x nx field (padded NY = 2ny, NX = 2nx) is three passes
+// over HBM, with the padding, transfer function / chirp products and the
+// crop folded into the FFT passes:
+//
+//   pass 1 (k_rows_fwd): the ny non-zero rows: load (x pre-chirp), zero-pad to
+//          NX in shared memory, row FFT, store to scratch S (ny x NX).
+//   pass 2 (k_cols):     tiles of C adjacent columns of S: load the ny rows
+//          into the centre of an NY-long column (zeros around), column FFT,
+//          x T(ky, kx), inverse column FFT, keep the central ny rows, store
+//          back in place.
+//   pass 3 (k_rows_inv): rows of S: inverse row FFT, keep the central nx
+//          columns (x post-chirp), store the ny x nx result.
+//
+// Algorithmic HBM traffic per propagation: 8n + 16n + 16n + 16n + 16n + 8n =
+// 80 n bytes (n = ny * nx), against ~71 n complex64 reads/writes in the
+// reference's chain.  Transfer functions are evaluated in registers (ASM) or
+// from two 1-D spectra of the separable chirp (Fresnel, ARSS): the 2-D FFT of
+// the sampled chirp exp(i pi (x^2 + y^2) / (lambda z)) is the outer product of
+// two 1-D FFTs, which k_chirp computes per call (exactly the DFT of the sampled
+// response the reference builds, golprop.h:184-187, olprop.h:133-137).
+#include <mutex>
+#include <vector>
+#include <cmath>
+#include <cstdio>
+
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace olg {
+
+static __device__ float2 g_tw[FFT_MAX];
+
+enum : int { M_ASM = 0, M_CHIRP = 1 };
+// pre/post operation modes
+enum : int { OP_NONE = 0, OP_TABLE = 1, OP_TABLE_IN_WINDOW = 2 };
+
+struct PropParams {
+    int ny, nx, NY, NX;
+    int method;     // M_ASM: T computed in registers; M_CHIRP: T = Hx[kx] * Hy[ky]
+    int conj;       // conjugate T (adjoint)
+    float scale;    // folded into T
+    // ASM transfer function constants (cycles)
+    float c0;               // frac(z / lambda)
+    float ax_hi, ax_lo;     // z lambda du^2 / 2
+    float ay_hi, ay_lo;     // z lambda dv^2 / 2
+    float tx, ty;           // lambda^2 du^2, lambda^2 dv^2
+    float zl;               // z / lambda
+    // chirp spectra (M_CHIRP)
+    const float2 *Hx, *Hy;
+    // pass-1 and pass-3 elementwise operations
+    int pre_mode, post_mode;
+    const float2 *prex, *prey, *postx, *posty;
+    int pre_hlim, pre_wlim, post_hlim, post_wlim;
+    int accumulate;
+    const float2 *in;
+    float2 *out;
+    float2 *S;
+};
+
+// ---------------------------------------------------------------- launch shapes
+template <int N>
+struct RowCfg {
+    static constexpr int NT = N >= 2048 ? N / 16 : 128;
+    static constexpr int NSEQ = N >= 2048 ? 1 : 2048 / N;
+    static constexpr int SMEM = NSEQ * padded_len(N) * 8;
+};
+template <int N>
+struct ColCfg {
+    static constexpr int E = N >= 4096 ? 2 * N : 8192; // elements per CTA
+    static constexpr int C = E / N;                    // columns per CTA
+    static constexpr int NT = E / 16;                  // 1 radix-16 butterfly per thread per stage
+    static constexpr int SMEM = padded_len(N) * C * 8;
+};
+
+__device__ __forceinline__ float2 apply_op(float2 v, int mode, const float2 *tx, const float2 *ty, int h, int w,
+                                           int ny, int nx, int hlim, int wlim)
+{
+    if (mode == OP_NONE) return v;
+    if (mode == OP_TABLE_IN_WINDOW) {
+        if (!(abs(w - nx / 2) < wlim && abs(h - ny / 2) < hlim)) return v;
+    }
+    return cmul(v, cmul(__ldg(tx + w), __ldg(ty + h)));
+}
+
+// ------------------------------------------------------------------- pass 1
+template <int N>
+__global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_fwd(PropParams P)
+{
+    using Cfg = RowCfg<N>;
+    extern __shared__ float2 sm[];
+    constexpr int SS = padded_len(N);
+    const int tid = threadIdx.x;
+    const int r0 = blockIdx.x * Cfg::NSEQ;
+    const int nx = P.nx, off = N / 4;
+    // zero the pad regions [0, N/4) and [3N/4, N) of every row
+    for (int e = tid; e < Cfg::NSEQ * (N / 2); e += Cfg::NT) {
+        const int q = e / (N / 2), i = e % (N / 2);
+        const int idx = i < N / 4 ? i : i + N / 2;
+        sm[q * SS + pidx(idx)] = make_float2(0.f, 0.f);
+    }
+    // load the nx input samples of each row (two complex per float4)
+    const int hx = nx / 2;
+    for (int e = tid; e < Cfg::NSEQ * hx; e += Cfg::NT) {
+        const int q = e / hx, w2 = (e % hx) * 2;
+        const int h = r0 + q;
+        float2 a = make_float2(0.f, 0.f), b = a;
+        if (h < P.ny) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(P.in + (size_t)h * nx + w2));
+            a = make_float2(v.x, v.y);
+            b = make_float2(v.z, v.w);
+            a = apply_op(a, P.pre_mode, P.prex, P.prey, h, w2, P.ny, nx, P.pre_hlim, P.pre_wlim);
+            b = apply_op(b, P.pre_mode, P.prex, P.prey, h, w2 + 1, P.ny, nx, P.pre_hlim, P.pre_wlim);
+        }
+        sm[q * SS + pidx(off + w2)] = a;
+        sm[q * SS + pidx(off + w2 + 1)] = b;
+    }
+    __syncthreads();
+    smem_fft<N, -1, Cfg::NT, false, Cfg::NSEQ>(sm, SS, g_tw, tid);
+    // store full rows to S
+    for (int e = tid; e < Cfg::NSEQ * (N / 2); e += Cfg::NT) {
+        const int q = e / (N / 2), i2 = (e % (N / 2)) * 2;
+        const int h = r0 + q;
+        if (h >= P.ny) continue;
+        const float2 a = sm[q * SS + pidx(i2)], b = sm[q * SS + pidx(i2 + 1)];
+        *reinterpret_cast<float4 *>(P.S + (size_t)h * N + i2) = make_float4(a.x, a.y, b.x, b.y);
+    }
+}
+
+// ------------------------------------------------------------------- pass 3
+template <int N>
+__global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_inv(PropParams P)
+{
+    using Cfg = RowCfg<N>;
+    extern __shared__ float2 sm[];
+    constexpr int SS = padded_len(N);
+    const int tid = threadIdx.x;
+    const int r0 = blockIdx.x * Cfg::NSEQ;
+    for (int e = tid; e < Cfg::NSEQ * (N / 2); e += Cfg::NT) {
+        const int q = e / (N / 2), i2 = (e % (N / 2)) * 2;
+        const int h = r0 + q;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (h < P.ny) v = *reinterpret_cast<const float4 *>(P.S + (size_t)h * N + i2);
+        sm[q * SS + pidx(i2)] = make_float2(v.x, v.y);
+        sm[q * SS + pidx(i2 + 1)] = make_float2(v.z, v.w);
+    }
+    __syncthreads();
+    smem_fft<N, +1, Cfg::NT, false, Cfg::NSEQ>(sm, SS, g_tw, tid);
+    const int nx = P.nx, off = N / 4, hx = nx / 2;
+    for (int e = tid; e < Cfg::NSEQ * hx; e += Cfg::NT) {
+        const int q = e / hx, w2 = (e % hx) * 2;
+        const int h = r0 + q;
+        if (h >= P.ny) continue;
+        float2 a = sm[q * SS + pidx(off + w2)], b = sm[q * SS + pidx(off + w2 + 1)];
+        a = apply_op(a, P.post_mode, P.postx, P.posty, h, w2, P.ny, nx, P.post_hlim, P.post_wlim);
+        b = apply_op(b, P.post_mode, P.postx, P.posty, h, w2 + 1, P.ny, nx, P.post_hlim, P.post_wlim);
+        float4 *dst = reinterpret_cast<float4 *>(P.out + (size_t)h * nx + w2);
+        if (P.accumulate) {
+            const float4 o = *dst;
+            a.x += o.x; a.y += o.y; b.x += o.z; b.y += o.w;
+        }
+        *dst = make_float4(a.x, a.y, b.x, b.y);
+    }
+}
+
+// ASM transfer function exp(2 pi i z w) at (fx, fy), cycles evaluated as
+//   frac(z/lambda) - ax fx^2 - ay fy^2 - (z/lambda) t^2 / (2 (1 + sqrt(1-t))^2)
+// with t = lambda^2 (u^2 + v^2): the exact expansion of z sqrt(1/lambda^2 - u^2 - v^2).
+// The two quadratic terms are reduced exactly (frac_mul); the remainder is
+// a few cycles at most, so FP32 keeps ~1e-6 rad of phase.  t > 1 gives NaN,
+// as sqrt of a negative argument does in the reference (golprop.h:318).
+__device__ __forceinline__ float2 asm_tf(const PropParams &P, int fx, int fy)
+{
+    const float fx2 = (float)(fx * fx), fy2 = (float)(fy * fy);
+    const float t = P.tx * fx2 + P.ty * fy2;
+    const float s = sqrtf(1.0f - t);
+    const float q = t / (1.0f + s);
+    const float g = 0.5f * q * q;
+    float cyc = P.c0 - frac_mul(P.ax_hi, P.ax_lo, fx2) - frac_mul(P.ay_hi, P.ay_lo, fy2) - P.zl * g;
+    cyc = wrap_cycles(cyc);
+    if (P.conj) cyc = -cyc;
+    return cscale(cis_cycles(cyc), P.scale);
+}
+
+// ------------------------------------------------------------------- pass 2
+template <int N>
+__global__ void __launch_bounds__(ColCfg<N>::NT) k_cols(PropParams P)
+{
+    using Cfg = ColCfg<N>;
+    constexpr int C = Cfg::C, NT = Cfg::NT;
+    extern __shared__ float2 sm[];
+    const int tid = threadIdx.x;
+    const int c0 = blockIdx.x * C;
+    const int NX = P.NX, ny = P.ny, off = N / 4;
+    // zero rows [0, N/4) and [3N/4, N)
+    for (int e = tid; e < (N / 2) * C; e += NT) {
+        const int i = e / C, c = e % C;
+        const int idx = i < N / 4 ? i : i + N / 2;
+        sm[pidx(idx) * C + c] = make_float2(0.f, 0.f);
+    }
+    // load the ny stored rows into the centre
+    constexpr int C2 = C / 2;
+    for (int e = tid; e < ny * C2; e += NT) {
+        const int h = e / C2, c = (e % C2) * 2;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c0 + c < NX) v = *reinterpret_cast<const float4 *>(P.S + (size_t)h * NX + c0 + c);
+        sm[pidx(off + h) * C + c] = make_float2(v.x, v.y);
+        sm[pidx(off + h) * C + c + 1] = make_float2(v.z, v.w);
+    }
+    __syncthreads();
+    smem_fft<N, -1, NT, true, C>(sm, 0, g_tw, tid);
+    // multiply by the transfer function
+    for (int e = tid; e < N * C; e += NT) {
+        const int ky = e / C, c = e % C;
+        const int kx = c0 + c;
+        float2 T;
+        if (P.method == M_ASM) {
+            const int fx = kx < NX / 2 ? kx : kx - NX;
+            const int fy = ky < N / 2 ? ky : ky - N;
+            T = asm_tf(P, fx, fy);
+        } else {
+            T = cmul(__ldg(P.Hx + (kx < NX ? kx : 0)), __ldg(P.Hy + ky));
+            if (P.conj) T = cconj(T);
+        }
+        float2 &x = sm[pidx(ky) * C + c];
+        x = cmul(x, T);
+    }
+    __syncthreads();
+    smem_fft<N, +1, NT, true, C>(sm, 0, g_tw, tid);
+    for (int e = tid; e < ny * C2; e += NT) {
+        const int h = e / C2, c = (e % C2) * 2;
+        if (c0 + c >= NX) continue;
+        const float2 a = sm[pidx(off + h) * C + c], b = sm[pidx(off + h) * C + c + 1];
+        *reinterpret_cast<float4 *>(P.S + (size_t)h * NX + c0 + c) = make_float4(a.x, a.y, b.x, b.y);
+    }
+}
+
+// ------------------------------------------------------------- chirp tables
+// Per axis (blockIdx.x == 0): the 1-D spectrum H[k] = sum_j c(j') e^{-2 pi i j k / L},
+// j' = j for j < L/2 else j - L (the fftshift'ed centred response), with
+// c(m) = exp(2 pi i kap m^2) and c = 0 for |m| >= lim (lim < 0: no window).
+// blockIdx.x == 1: the pass-1 / pass-3 tables along this axis:
+//   a[m] = [|m'| < alim] exp(2 pi i (a2 m'^2 + a1 m' + a0))  (m' = m - n/2), and b[] likewise.
+struct ChirpAxis {
+    int L, n;                  // padded length, field length along this axis
+    float kap_hi, kap_lo;      // chirp cycles per index^2
+    int lim;                   // chirp window (< 0: none)
+    float scale;               // applied to the spectrum
+    int conj_spec;             // conjugate the spectrum
+    float2 *H;                 // out: L
+    // elementwise tables (nullable)
+    float2 *ta, *tb;           // out: n each
+    float a2_hi, a2_lo, a1_hi, a1_lo, a0; int alim; int aconj;
+    float b2_hi, b2_lo, b1_hi, b1_lo, b0; int blim; int bconj;
+};
+
+template <int N>
+struct ChirpCfg {
+    static constexpr int NT = N / 16 < 256 ? N / 16 : 256;
+    static constexpr int SMEM = padded_len(N) * 8;
+};
+
+template <int N>
+__global__ void __launch_bounds__(ChirpCfg<N>::NT) k_chirp(ChirpAxis A)
+{
+    constexpr int NT = ChirpCfg<N>::NT;
+    extern __shared__ float2 sm[];
+    const int tid = threadIdx.x;
+    if (blockIdx.x == 0) {
+        for (int j = tid; j < N; j += NT) {
+            const int m = j < N / 2 ? j : j - N;
+            float2 c = make_float2(0.f, 0.f);
+            if (A.lim < 0 || abs(m) < A.lim) c = cis_cycles(frac_mul(A.kap_hi, A.kap_lo, (float)(m * m)));
+            sm[pidx(j)] = c;
+        }
+        __syncthreads();
+        smem_fft<N, -1, NT, false, 1>(sm, padded_len(N), g_tw, tid);
+        for (int j = tid; j < N; j += NT) {
+            const float2 v = cscale(sm[pidx(j)], A.scale);
+            A.H[j] = A.conj_spec ? cconj(v) : v;
+        }
+    } else {
+        for (int m = tid; m < A.n; m += NT) {
+            const int mp = m - A.n / 2;
+            const float fm = (float)mp, fm2 = (float)(mp * mp);
+            if (A.ta) {
+                float2 v = make_float2(0.f, 0.f);
+                if (A.alim < 0 || abs(mp) < A.alim) {
+                    const float cyc = frac_mul(A.a2_hi, A.a2_lo, fm2) + frac_mul(A.a1_hi, A.a1_lo, fm) + A.a0;
+                    v = cis_cycles(wrap_cycles(cyc));
+                    if (A.aconj) v = cconj(v);
+                }
+                A.ta[m] = v;
+            }
+            if (A.tb) {
+                float2 v = make_float2(0.f, 0.f);
+                if (A.blim < 0 || abs(mp) < A.blim) {
+                    const float cyc = frac_mul(A.b2_hi, A.b2_lo, fm2) + frac_mul(A.b1_hi, A.b1_lo, fm) + A.b0;
+                    v = cis_cycles(wrap_cycles(cyc));
+                    if (A.bconj) v = cconj(v);
+                }
+                A.tb[m] = v;
+            }
+        }
+    }
+}
+
+// ===================================================================== host
+namespace {
+
+std::mutex g_tw_mu;
+bool g_tw_ready[64] = {};
+
+int ensure_twiddles()
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return fail(OLG_ERR_INVALID_ARG, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_tw_mu);
+    if (g_tw_ready[dev]) return OLG_OK;
+    std::vector<float2> t(FFT_MAX);
+    for (int m = 0; m < FFT_MAX; ++m) {
+        const double a = -2.0 * M_PI * (double)m / (double)FFT_MAX;
+        t[m] = make_float2((float)cos(a), (float)sin(a));
+    }
+    e = cudaMemcpyToSymbol(g_tw, t.data(), sizeof(float2) * FFT_MAX);
+    if (e != cudaSuccess) return cuda_fail(e, "twiddle table upload");
+    g_tw_ready[dev] = true;
+    return OLG_OK;
+}
+
+template <typename K>
+int prep_smem(K kern, int bytes)
+{
+    if (bytes <= 48 * 1024) return OLG_OK;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaFuncSetAttribute");
+}
+
+template <int N>
+int launch_rows(const PropParams &P, bool inverse, cudaStream_t st)
+{
+    using C = RowCfg<N>;
+    const int grid = (P.ny + C::NSEQ - 1) / C::NSEQ;
+    if (!inverse) {
+        if (int rc = prep_smem(k_rows_fwd<N>, C::SMEM)) return rc;
+        k_rows_fwd<N><<<grid, C::NT, C::SMEM, st>>>(P);
+    } else {
+        if (int rc = prep_smem(k_rows_inv<N>, C::SMEM)) return rc;
+        k_rows_inv<N><<<grid, C::NT, C::SMEM, st>>>(P);
+    }
+    count_launch();
+    return check_launch(inverse ? "k_rows_inv" : "k_rows_fwd");
+}
+
+template <int N>
+int launch_cols(const PropParams &P, cudaStream_t st)
+{
+    using C = ColCfg<N>;
+    const int grid = (P.NX + C::C - 1) / C::C;
+    if (int rc = prep_smem(k_cols<N>, C::SMEM)) return rc;
+    k_cols<N><<<grid, C::NT, C::SMEM, st>>>(P);
+    count_launch();
+    return check_launch("k_cols");
+}
+
+template <int N>
+int launch_chirp(const ChirpAxis &A, cudaStream_t st)
+{
+    using C = ChirpCfg<N>;
+    if (int rc = prep_smem(k_chirp<N>, C::SMEM)) return rc;
+    const int grid = (A.ta || A.tb) ? 2 : 1;
+    k_chirp<N><<<grid, C::NT, C::SMEM, st>>>(A);
+    count_launch();
+    return check_launch("k_chirp");
+}
+
+#define OLG_SIZE_SWITCH(n, FN, ...)                                                                              \
+    switch (n) {                                                                                                 \
+    case 64: return FN<64>(__VA_ARGS__);                                                                         \
+    case 128: return FN<128>(__VA_ARGS__);                                                                       \
+    case 256: return FN<256>(__VA_ARGS__);                                                                       \
+    case 512: return FN<512>(__VA_ARGS__);                                                                       \
+    case 1024: return FN<1024>(__VA_ARGS__);                                                                     \
+    case 2048: return FN<2048>(__VA_ARGS__);                                                                     \
+    case 4096: return FN<4096>(__VA_ARGS__);                                                                     \
+    case 8192: return FN<8192>(__VA_ARGS__);                                                                     \
+    default: return fail(OLG_ERR_UNSUPPORTED_SIZE, "FFT length not supported");                                \
+    }
+
+int rows_pass(const PropParams &P, bool inverse, cudaStream_t st) { OLG_SIZE_SWITCH(P.NX, launch_rows, P, inverse, st) }
+int cols_pass(const PropParams &P, cudaStream_t st) { OLG_SIZE_SWITCH(P.NY, launch_cols, P, st) }
+int chirp_axis(const ChirpAxis &A, cudaStream_t st) { OLG_SIZE_SWITCH(A.L, launch_chirp, A, st) }
+
+struct Layout {
+    float2 *S, *Hx, *Hy, *tax, *tay, *tbx, *tby;
+};
+
+size_t layout_bytes(int ny, int nx, Layout *L, char *base)
+{
+    size_t off = 0;
+    auto take = [&](size_t elems) {
+        char *p = base ? base + off : nullptr;
+        off += align_up(elems * sizeof(float2), 256);
+        return (float2 *)p;
+    };
+    Layout l;
+    l.S = take((size_t)ny * 2 * nx);
+    l.Hx = take(2 * (size_t)nx);
+    l.Hy = take(2 * (size_t)ny);
+    l.tax = take(nx);
+    l.tay = take(ny);
+    l.tbx = take(nx);
+    l.tby = take(ny);
+    if (L) *L = l;
+    return off;
+}
+
+int validate(const void *a, const void *b, int ny, int nx)
+{
+    if (!a || !b) return fail(OLG_ERR_INVALID_ARG, "null field pointer");
+    if (((uintptr_t)a & 15) || ((uintptr_t)b & 15)) return fail(OLG_ERR_INVALID_ARG, "field pointers must be 16-byte aligned");
+    if (!is_pow2(nx) || !is_pow2(ny) || nx < 32 || ny < 32 || 2 * nx > FFT_MAX || 2 * ny > FFT_MAX)
+        return fail(OLG_ERR_UNSUPPORTED_SIZE, "ny, nx must be powers of two in [32, 4096]");
+    return OLG_OK;
+}
+
+PropParams base_params(const void *in, void *out, int ny, int nx, const Layout &L)
+{
+    PropParams P{};
+    P.ny = ny; P.nx = nx; P.NY = 2 * ny; P.NX = 2 * nx;
+    P.in = (const float2 *)in;
+    P.out = (float2 *)out;
+    P.S = L.S;
+    P.Hx = L.Hx; P.Hy = L.Hy;
+    P.pre_mode = OP_NONE; P.post_mode = OP_NONE;
+    return P;
+}
+
+int run_passes(const PropParams &P, cudaStream_t st)
+{
+    if (int rc = rows_pass(P, false, st)) return rc;
+    if (int rc = cols_pass(P, st)) return rc;
+    return rows_pass(P, true, st);
+}
+
+long floor_lim(double v)
+{
+    double f = std::floor(v);
+    if (!(f < 1073741824.0)) f = 1073741824.0;
+    if (f < -1073741824.0) f = -1073741824.0;
+    return (long)f;
+}
+
+void set_quad(float &hi, float &lo, double v)
+{
+    DF d = split_df(v);
+    hi = d.hi;
+    lo = d.lo;
+}
+
+// frac(v) in [-0.5, 0.5]
+float frac_host(double v) { return (float)(v - std::nearbyint(v)); }
+
+ChirpAxis chirp_axis_params(int L, int n, double d, double lambda, double z, double s_factor, int lim, double scale,
+                            float2 *H)
+{
+    ChirpAxis A{};
+    A.L = L;
+    A.n = n;
+    set_quad(A.kap_hi, A.kap_lo, s_factor * d * d / (2.0 * lambda * z));
+    A.lim = lim;
+    A.scale = (float)scale;
+    A.conj_spec = 0;
+    A.H = H;
+    A.alim = A.blim = -1;
+    return A;
+}
+
+} // namespace
+} // namespace olg
+
+using namespace olg;
+
+extern "C" size_t olg_prop_workspace_bytes(int ny, int nx)
+{
+    if (ny <= 0 || nx <= 0) return 0;
+    return layout_bytes(ny, nx, nullptr, nullptr);
+}
+
+extern "C" int olg_asm_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                                double z, int flags, void *work, size_t work_bytes, olg_stream_t stream)
+{
+    if (int rc = validate(u_in, u_out, ny, nx)) return rc;
+    if (!(dy > 0) || !(dx > 0) || !(lambda > 0) || !std::isfinite(z)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
+    Layout L;
+    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    PropParams P = base_params(u_in, u_out, ny, nx, L);
+    const double NX = 2.0 * nx, NY = 2.0 * ny;
+    const double du = 1.0 / (dx * NX), dv = 1.0 / (dy * NY);
+    const double zl = z / lambda;
+    P.method = M_ASM;
+    P.conj = (flags & OLG_CONJ) ? 1 : 0;
+    P.scale = (flags & OLG_NO_NORMALIZE) ? 1.0f : (float)(1.0 / (NX * NY));
+    P.c0 = frac_host(zl);
+    set_quad(P.ax_hi, P.ax_lo, z * lambda * du * du / 2.0);
+    set_quad(P.ay_hi, P.ay_lo, z * lambda * dv * dv / 2.0);
+    P.tx = (float)(lambda * lambda * du * du);
+    P.ty = (float)(lambda * lambda * dv * dv);
+    P.zl = (float)zl;
+    return run_passes(P, st);
+}
+
+extern "C" int olg_fresnel_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                                    double z, int bandlimit, int flags, void *work, size_t work_bytes,
+                                    olg_stream_t stream)
+{
+    if (int rc = validate(u_in, u_out, ny, nx)) return rc;
+    if (!(dy > 0) || !(dx > 0) || !(lambda > 0) || !std::isfinite(z) || z == 0.0)
+        return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (bandlimit < 0 || bandlimit > 2) return fail(OLG_ERR_INVALID_ARG, "bandlimit must be 0, 1 or 2");
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
+    Layout L;
+    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    PropParams P = base_params(u_in, u_out, ny, nx, L);
+    const int NX = 2 * nx, NY = 2 * ny;
+    const double np = (double)NX * (double)NY;
+    const double sc1 = (flags & OLG_NO_NORMALIZE) ? 1.0 : 1.0 / np;
+    int limx = -1, limy = -1;
+    if (bandlimit == 1) { // golprop.h:227-233: one limit, from x, on both axes
+        limx = limy = (int)floor_lim(std::fabs(lambda * z * 0.5 / dx) / dx);
+    } else if (bandlimit == 2) { // olprop.h:34-39
+        limx = (int)floor_lim(std::fabs(lambda * z * 0.5 / dx) / dx);
+        limy = (int)floor_lim(std::fabs(lambda * z * 0.5 / dy) / dy);
+    }
+    ChirpAxis ax = chirp_axis_params(NX, nx, dx, lambda, z, 1.0, limx, sc1, L.Hx);
+    ChirpAxis ay = chirp_axis_params(NY, ny, dy, lambda, z, 1.0, limy, sc1, L.Hy);
+    if (int rc = chirp_axis(ax, st)) return rc;
+    if (int rc = chirp_axis(ay, st)) return rc;
+    P.method = M_CHIRP;
+    P.conj = (flags & OLG_CONJ) ? 1 : 0;
+    P.scale = 1.0f;
+    return run_passes(P, st);
+}
+
+extern "C" int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx, double lambda,
+                                 double z, double s, double oy, double ox, int flags, void *work, size_t work_bytes,
+                                 olg_stream_t stream)
+{
+    if (int rc = validate(u_src, u_dst, ny, nx)) return rc;
+    if (!(dy > 0) || !(dx > 0) || !(lambda > 0) || !std::isfinite(z) || z == 0.0 || !std::isfinite(s))
+        return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (s == 0.0 || s == 1.0) return fail(OLG_ERR_INVALID_ARG, "ARSS is undefined for s = 0 or s = 1 (window limits divide by s|s-1|)");
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
+    Layout L;
+    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    PropParams P = base_params(u_src, u_dst, ny, nx, L);
+    const int NX = 2 * nx, NY = 2 * ny;
+    const double np = (double)NX * (double)NY;
+    // windows, golprop.h:849-852, 891-892, 928-931
+    const int hlim_u = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dy)) / dy);
+    const int wlim_u = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dx)) / dx);
+    const int lim_h = (int)floor_lim(std::fabs(lambda * z * 0.5 / (dx * s)) / dx);
+    const int hlim_c = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dy)) / dy);
+    const int wlim_c = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dx)) / dx);
+    const bool adj = (flags & OLG_CONJ) != 0;
+    const double lz2 = 2.0 * lambda * z;
+    ChirpAxis ax = chirp_axis_params(NX, nx, dx, lambda, z, s, lim_h, 1.0 / np, L.Hx);
+    ChirpAxis ay = chirp_axis_params(NY, ny, dy, lambda, z, s, lim_h, 1.0 / np, L.Hy);
+    // pre-chirp (golprop.h:830-841) and post-chirp (golprop.h:910-920) coefficients, cycles
+    struct Q { double a2, a1, a0; };
+    const Q prex{(s * s - s) * dx * dx / lz2, -2.0 * s * ox * dx / lz2, 0.0};
+    const Q prey{(s * s - s) * dy * dy / lz2, -2.0 * s * oy * dy / lz2, 0.0};
+    const Q postx{(1 - s) * dx * dx / lz2, 2.0 * ox * dx / lz2, (ox * ox + oy * oy) / lz2};
+    const Q posty{(1 - s) * dy * dy / lz2, 2.0 * oy * dy / lz2, 0.0};
+    auto fill = [&](ChirpAxis &A, float2 *ta, float2 *tb, const Q &qa, int alim, int aconj, const Q &qb, int blim,
+                    int bconj) {
+        A.ta = ta; A.tb = tb;
+        set_quad(A.a2_hi, A.a2_lo, qa.a2); set_quad(A.a1_hi, A.a1_lo, qa.a1); A.a0 = frac_host(qa.a0);
+        A.alim = alim; A.aconj = aconj;
+        set_quad(A.b2_hi, A.b2_lo, qb.a2); set_quad(A.b1_hi, A.b1_lo, qb.a1); A.b0 = frac_host(qb.a0);
+        A.blim = blim; A.bconj = bconj;
+    };
+    if (!adj) {
+        // pass 1: pre-chirp, zero outside its window; pass 3: post-chirp inside its window
+        fill(ax, L.tax, L.tbx, prex, wlim_u, 0, postx, -1, 0);
+        fill(ay, L.tay, L.tby, prey, hlim_u, 0, posty, -1, 0);
+        P.pre_mode = OP_TABLE;
+        P.post_mode = OP_TABLE_IN_WINDOW;
+        P.post_hlim = hlim_c; P.post_wlim = wlim_c;
+    } else {
+        // adjoint: conj(post-chirp) inside the Cz window first, conj(pre-chirp) with its window last
+        fill(ax, L.tax, L.tbx, postx, -1, 1, prex, wlim_u, 1);
+        fill(ay, L.tay, L.tby, posty, -1, 1, prey, hlim_u, 1);
+        P.pre_mode = OP_TABLE_IN_WINDOW;
+        P.pre_hlim = hlim_c; P.pre_wlim = wlim_c;
+        P.post_mode = OP_TABLE;
+    }
+    P.prex = L.tax; P.prey = L.tay; P.postx = L.tbx; P.posty = L.tby;
+    if (int rc = chirp_axis(ax, st)) return rc;
+    if (int rc = chirp_axis(ay, st)) return rc;
+    P.method = M_CHIRP;
+    P.conj = adj ? 1 : 0;
+    P.scale = 1.0f;
+    return run_passes(P, st);
+}
+
+// ---------------------------------------------------------------- AUTO checks
+// AsmPropCheck olprop.h:209-225 and FresnelPropCheck olprop.h:109-123 in the
+// caller's precision.  This file is compiled with -ffp-contract=off so the
+// float versions round each operation like the reference's float build.
+template <typename T>
+static int asm_check_t(int ny, int nx, T dy, T dx, T lambda, T z)
+{
+    const int64_t nx2 = 2 * (int64_t)nx, ny2 = 2 * (int64_t)ny;
+    const T du = 1 / (dx * nx2);
+    const T dv = 1 / (dy * ny2);
+    const T umax = du * nx2 / 2;
+    const T vmax = dv * ny2 / 2;
+    const T tmpsqrt = std::sqrt(1 / (lambda * lambda) - umax * umax - vmax * vmax);
+    const T zmax_u = tmpsqrt / (2 * umax * du);
+    const T zmax_v = tmpsqrt / (2 * vmax * dv);
+    return (zmax_u < std::abs(z) || zmax_v < std::abs(z)) ? 0 : 1;
+}
+template <typename T>
+static int fresnel_check_t(int ny, int nx, T dy, T dx, T lambda, T z)
+{
+    const size_t nx2 = 2 * (size_t)nx, ny2 = 2 * (size_t)ny;
+    const T xmax = dx * nx2 / 2;
+    const T ymax = dy * ny2 / 2;
+    const T zmin_x = 2 * xmax * dx / lambda;
+    const T zmin_y = 2 * ymax * dy / lambda;
+    return (zmin_x > std::abs(z) || zmin_y > std::abs(z)) ? 0 : 1;
+}
+
+extern "C" int olg_asm_prop_check(int ny, int nx, double dy, double dx, double lambda, double z, int single_precision)
+{
+    if (single_precision) return asm_check_t<float>(ny, nx, (float)dy, (float)dx, (float)lambda, (float)z);
+    return asm_check_t<double>(ny, nx, dy, dx, lambda, z);
+}
+
+extern "C" int olg_fresnel_prop_check(int ny, int nx, double dy, double dx, double lambda, double z, int single_precision)
+{
+    if (single_precision) return fresnel_check_t<float>(ny, nx, (float)dy, (float)dx, (float)lambda, (float)z);
+    return fresnel_check_t<double>(ny, nx, dy, dx, lambda, z);
+}
+
+extern "C" int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, double lambda, double z, int mode, int flags,
+                            int *chosen, void *work, size_t work_bytes, olg_stream_t stream)
+{
+    const bool verbose = (flags & OLG_VERBOSE) != 0;
+    const int f = flags & (OLG_CONJ | OLG_NO_NORMALIZE);
+    const int sp = (flags & OLG_CHECK_F32) ? 1 : 0;
+    int pick;
+    if (mode == OLG_FRESNEL) pick = 1;
+    else if (mode == OLG_ASM) pick = 0;
+    else if (mode == OLG_AUTO) {
+        if (olg_asm_prop_check(ny, nx, dy, dx, lambda, z, sp)) pick = 0;
+        else if (!olg_fresnel_prop_check(ny, nx, dy, dx, lambda, z, sp)) pick = 2;
+        else pick = 1;
+    } else {
+        return fail(OLG_ERR_INVALID_ARG, "invalid PROPMODE");
+    }
+    if (chosen) *chosen = pick;
+    if (verbose) {
+        if (pick == 0) printf("AsmProp\n");
+        else if (pick == 1) printf("FresnelProp\n");
+        else printf("warning!!\neither AsmProp or FresnelProp does not meet the condition.\n");
+    }
+    if (pick == 0) return olg_asm_prop_c64(u, u, ny, nx, dy, dx, lambda, z, f, work, work_bytes, stream);
+    return olg_fresnel_prop_c64(u, u, ny, nx, dy, dx, lambda, z, pick == 2 ? 1 : 0, f, work, work_bytes, stream);
+}

@@ -1,0 +1,169 @@
+"""Propagation: the Python mirror of the reference's golprop.h API.
+
+Names, argument order and meaning follow the reference (``ol::gAsmProp``,
+``ol::gFresnelProp``, ``ol::gFresnelPropBandLimit``, ``ol::ARSSFresnelProp``,
+``ol::Prop``, ``ol::AsmPropCheck``, ``ol::FresnelPropCheck``).  A device field is
+a CUDA ``torch.complex64`` tensor of shape (ny, nx) (the reference's
+``cuda::unique_ptr<thrust::complex<float>[]>``); like the reference, the result
+is written back into it.  A host field (numpy array or CPU tensor, the
+reference's ``std::unique_ptr<std::complex<float>[]>`` overloads) is copied to
+the GPU, propagated with the host overload's conventions, and copied back.
+
+Everything runs through libolgb300.so; failures raise ``OlgError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from enum import IntEnum
+
+import numpy as np
+import torch
+
+from ._lib import (OLG_CHECK_F32, OLG_CONJ, OLG_NO_NORMALIZE, OLG_VERBOSE, call, lib)
+
+
+class PROPMODE(IntEnum):
+    """ol::PROPMODE (oldefine.h:7-9)."""
+
+    ASM = 0
+    FRESNEL = 1
+    AUTO = 2
+
+
+ASM, FRESNEL, AUTO = PROPMODE.ASM, PROPMODE.FRESNEL, PROPMODE.AUTO
+
+
+def _stream(stream=None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def _dev_field(u, ny, nx, name="u"):
+    if not isinstance(u, torch.Tensor) or not u.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if u.dtype != torch.complex64 or not u.is_contiguous() or u.numel() != ny * nx:
+        raise ValueError(f"{name} must be a contiguous complex64 tensor with ny*nx = {ny * nx} elements")
+    return u
+
+
+def _is_host(u) -> bool:
+    return isinstance(u, np.ndarray) or (isinstance(u, torch.Tensor) and not u.is_cuda)
+
+
+def _host_roundtrip(u, ny, nx, fn):
+    """Copy a host field to the GPU, run fn(device_tensor), copy back in place."""
+    if isinstance(u, np.ndarray):
+        d = torch.from_numpy(np.ascontiguousarray(u, np.complex64).reshape(ny, nx)).cuda()
+        fn(d)
+        u[...] = d.cpu().numpy().reshape(u.shape).astype(u.dtype, copy=False)
+        return u
+    d = u.reshape(ny, nx).to(device="cuda", dtype=torch.complex64).contiguous()
+    fn(d)
+    u.copy_(d.cpu().reshape(u.shape).to(u.dtype))
+    return u
+
+
+# ------------------------------------------------------------------ general
+def asm_prop(u_in, u_out=None, *, dy, dx, lam, z, adjoint=False, normalize=True, stream=None, work=None):
+    """Angular spectrum method on device tensors (olg_asm_prop_c64).
+
+    ``adjoint`` applies the conjugate transfer function (the adjoint operator);
+    ``normalize=False`` omits 1/Np like the host-pointer overload.
+    """
+    ny, nx = u_in.shape
+    _dev_field(u_in, ny, nx, "u_in")
+    u_out = u_in if u_out is None else _dev_field(u_out, ny, nx, "u_out")
+    flags = (OLG_CONJ if adjoint else 0) | (0 if normalize else OLG_NO_NORMALIZE)
+    wp, wb = (work.data_ptr(), work.numel() * work.element_size()) if work is not None else (None, 0)
+    call("olg_asm_prop_c64", u_in.data_ptr(), u_out.data_ptr(), ny, nx, float(dy), float(dx), float(lam), float(z),
+         flags, wp, wb, _stream(stream))
+    return u_out
+
+
+def fresnel_prop(u_in, u_out=None, *, dy, dx, lam, z, bandlimit=0, adjoint=False, normalize=True, stream=None,
+                 work=None):
+    """Fresnel convolution propagation (olg_fresnel_prop_c64).  bandlimit: 0 none,
+    1 the GPU band limit (golprop.h:225-233), 2 the CPU band limit (olprop.h:26-50)."""
+    ny, nx = u_in.shape
+    _dev_field(u_in, ny, nx, "u_in")
+    u_out = u_in if u_out is None else _dev_field(u_out, ny, nx, "u_out")
+    flags = (OLG_CONJ if adjoint else 0) | (0 if normalize else OLG_NO_NORMALIZE)
+    wp, wb = (work.data_ptr(), work.numel() * work.element_size()) if work is not None else (None, 0)
+    call("olg_fresnel_prop_c64", u_in.data_ptr(), u_out.data_ptr(), ny, nx, float(dy), float(dx), float(lam),
+         float(z), int(bandlimit), flags, wp, wb, _stream(stream))
+    return u_out
+
+
+def arss_prop(u_src, u_dst=None, *, dy, dx, lam, z, s, oy=0.0, ox=0.0, adjoint=False, stream=None, work=None):
+    """ARSS scaled Fresnel propagation (olg_arss_prop_c64)."""
+    ny, nx = u_src.shape
+    _dev_field(u_src, ny, nx, "u_src")
+    u_dst = u_src if u_dst is None else _dev_field(u_dst, ny, nx, "u_dst")
+    wp, wb = (work.data_ptr(), work.numel() * work.element_size()) if work is not None else (None, 0)
+    call("olg_arss_prop_c64", u_src.data_ptr(), u_dst.data_ptr(), ny, nx, float(dy), float(dx), float(lam),
+         float(z), float(s), float(oy), float(ox), OLG_CONJ if adjoint else 0, wp, wb, _stream(stream))
+    return u_dst
+
+
+def workspace_bytes(ny, nx) -> int:
+    return int(lib().olg_prop_workspace_bytes(ny, nx))
+
+
+def workspace(ny, nx, device="cuda"):
+    """A reusable scratch buffer for one propagation of an ny x nx field."""
+    return torch.empty(workspace_bytes(ny, nx), dtype=torch.uint8, device=device)
+
+
+# ------------------------------------------------------- reference mirror
+def gAsmProp(u, ny, nx, dy, dx, lam, d):
+    """ol::gAsmProp: device overload golprop.h:507-534 (1/Np applied) or, for a
+    host field, the host overload golprop.h:458-504 (no 1/Np)."""
+    if _is_host(u):
+        return _host_roundtrip(u, ny, nx, lambda t: asm_prop(t, dy=dy, dx=dx, lam=lam, z=d, normalize=False))
+    return asm_prop(_dev_field(u, ny, nx).view(ny, nx), dy=dy, dx=dx, lam=lam, z=d)
+
+
+def gFresnelProp(u, ny, nx, dy, dx, lam, d):
+    """ol::gFresnelProp: device overload golprop.h:167-198, host overload golprop.h:70-124."""
+    if _is_host(u):
+        return _host_roundtrip(u, ny, nx, lambda t: fresnel_prop(t, dy=dy, dx=dx, lam=lam, z=d, normalize=False))
+    return fresnel_prop(_dev_field(u, ny, nx).view(ny, nx), dy=dy, dx=dx, lam=lam, z=d)
+
+
+def gFresnelPropBandLimit(u, ny, nx, dy, dx, lam, d):
+    """ol::gFresnelPropBandLimit, golprop.h:278-302."""
+    return fresnel_prop(_dev_field(u, ny, nx).view(ny, nx), dy=dy, dx=dx, lam=lam, z=d, bandlimit=1)
+
+
+def ARSSFresnelProp(usrc, udst, ny, nx, dy, dx, lam, z, s, oy=0.0, ox=0.0):
+    """ol::ARSSFresnelProp, golprop.h:941-995 (and the 9-argument form :990-995)."""
+    return arss_prop(_dev_field(usrc, ny, nx, "usrc").view(ny, nx), _dev_field(udst, ny, nx, "udst").view(ny, nx),
+                     dy=dy, dx=dx, lam=lam, z=z, s=s, oy=oy, ox=ox)
+
+
+def AsmPropCheck(ny, nx, dy, dx, lam, z, single_precision=True) -> bool:
+    """ol::AsmPropCheck, olprop.h:209-225 (float evaluation by default, as the GPU path uses it)."""
+    return bool(lib().olg_asm_prop_check(ny, nx, float(dy), float(dx), float(lam), float(z), int(single_precision)))
+
+
+def FresnelPropCheck(ny, nx, dy, dx, lam, z, single_precision=True) -> bool:
+    """ol::FresnelPropCheck, olprop.h:109-123."""
+    return bool(lib().olg_fresnel_prop_check(ny, nx, float(dy), float(dx), float(lam), float(z),
+                                             int(single_precision)))
+
+
+def Prop(u, ny, nx, dy, dx, lam, d, propmode=PROPMODE.AUTO, verbose=True, single_precision=True):
+    """ol::Prop, golprop.h:578-604: ASM / FRESNEL / AUTO (ASM if its check passes,
+    else Fresnel if its check passes, else band-limited Fresnel).  Prints the
+    chosen method like the reference when ``verbose``.  Returns the field;
+    the chosen branch (0 ASM, 1 Fresnel, 2 band-limited) is in ``Prop.last_choice``."""
+    t = _dev_field(u, ny, nx)
+    chosen = C.c_int(-1)
+    flags = (OLG_VERBOSE if verbose else 0) | (OLG_CHECK_F32 if single_precision else 0)
+    call("olg_prop_c64", t.data_ptr(), ny, nx, float(dy), float(dx), float(lam), float(d), int(propmode), flags,
+         C.byref(chosen), None, 0, _stream())
+    Prop.last_choice = chosen.value
+    return u
+
+
+Prop.last_choice = -1

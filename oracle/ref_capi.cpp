@@ -1,0 +1,115 @@
+/*
+ * ref_capi.cpp -- extern "C" entry points over the reference's OWN CPU
+ * templates, compiled from the unmodified reference headers (include/olprop.h,
+ * include/olcgh.h, include/olutils.h, include/olimg.h) with the shims in
+ * refshim/.  TEST INFRASTRUCTURE ONLY: used here to pin the oracle restatement
+ * (olcpu.c) and to generate the golden fixtures under tests/golden/.  Output
+ * goes to oracle/_ref/ (git-ignored).
+ */
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+
+#include "olprop.h"
+#include "olcgh.h"
+
+using cd = std::complex<double>;
+
+static std::unique_ptr<cd[]> load(const double *p, long n)
+{
+    auto u = std::make_unique<cd[]>(n);
+    std::memcpy((void *)u.get(), p, sizeof(cd) * n);
+    return u;
+}
+static void store(const std::unique_ptr<cd[]> &u, double *p, long n) { std::memcpy(p, (const void *)u.get(), sizeof(cd) * n); }
+
+static ol::Object<double> mkobj(const double *pts, int n)
+{
+    ol::Object<double> obj(n);
+    for (int j = 0; j < n; ++j) obj[j] = ol::Vect3<double>(pts[3 * j], pts[3 * j + 1], pts[3 * j + 2]);
+    return obj;
+}
+
+extern "C" {
+
+/* ol::AsmProp<double>, olprop.h:227-248 */
+void ref_asm_prop(double *u, int ny, int nx, double dy, double dx, double lam, double z)
+{
+    auto U = load(u, (long)ny * nx);
+    ol::AsmProp(U, (int64_t)ny, (int64_t)nx, dy, dx, lam, z);
+    store(U, u, (long)ny * nx);
+}
+
+/* ol::FresnelProp<double>, olprop.h:125-148 */
+void ref_fresnel_prop(double *u, int ny, int nx, double dy, double dx, double lam, double z)
+{
+    auto U = load(u, (long)ny * nx);
+    ol::FresnelProp(U, (size_t)ny, (size_t)nx, dy, dx, lam, z);
+    store(U, u, (long)ny * nx);
+}
+
+/* ol::FresnelPropBandLimit<double>, olprop.h:150-170 */
+void ref_fresnel_prop_bandlimit(double *u, int ny, int nx, double dy, double dx, double lam, double z)
+{
+    auto U = load(u, (long)ny * nx);
+    ol::FresnelPropBandLimit(U, (size_t)ny, (size_t)nx, dy, dx, lam, z);
+    store(U, u, (long)ny * nx);
+}
+
+/* ol::Prop (CPU dispatcher), olprop.h:656-682; mode = ol::PROPMODE */
+void ref_prop(double *u, int ny, int nx, double dy, double dx, double lam, double z, int mode)
+{
+    auto U = load(u, (long)ny * nx);
+    ol::Prop(U, ny, nx, dy, dx, lam, z, (ol::PROPMODE)mode);
+    store(U, u, (long)ny * nx);
+}
+
+int ref_asm_prop_check(int ny, int nx, double dy, double dx, double lam, double z)
+{
+    return ol::AsmPropCheck((int64_t)ny, (int64_t)nx, dy, dx, lam, z) ? 1 : 0;
+}
+int ref_asm_prop_check_f(int ny, int nx, float dy, float dx, float lam, float z)
+{
+    return ol::AsmPropCheck((int64_t)ny, (int64_t)nx, dy, dx, lam, z) ? 1 : 0;
+}
+int ref_fresnel_prop_check(int ny, int nx, double dy, double dx, double lam, double z)
+{
+    return ol::FresnelPropCheck((size_t)ny, (size_t)nx, dy, dx, lam, z) ? 1 : 0;
+}
+int ref_fresnel_prop_check_f(int ny, int nx, float dy, float dx, float lam, float z)
+{
+    return ol::FresnelPropCheck((size_t)ny, (size_t)nx, dy, dx, lam, z) ? 1 : 0;
+}
+
+/* ol::Cgh complex output, olcgh.h:368-379 -> _CghFresnel olcgh.h:297-313 */
+void ref_cgh(const double *pts, int n, double *u, int ny, int nx, double py, double px, double lam)
+{
+    auto obj = mkobj(pts, n);
+    auto U = std::make_unique<cd[]>((long)ny * nx);
+    ol::Cgh(obj, U, ny, nx, py, px, lam);
+    store(U, u, (long)ny * nx);
+}
+
+/* ol::Cgh phase output, olcgh.h:351-365 -> _CghFresnel olcgh.h:276-295 */
+void ref_cgh_phase(const double *pts, int n, double *phase, int ny, int nx, double p, double lam)
+{
+    auto obj = mkobj(pts, n);
+    auto ph = std::make_unique<double[]>((long)ny * nx);
+    ol::Cgh(obj, ph, ny, nx, p, lam);
+    std::memcpy(phase, ph.get(), sizeof(double) * (long)ny * nx);
+}
+
+/* ol::complex2img(MODE), olimg.h:348-391 */
+void ref_complex2img(const double *u, uint8_t *img, int ny, int nx, int mode)
+{
+    auto U = load(u, (long)ny * nx);
+    auto I = std::make_unique<uint8_t[]>((long)ny * nx);
+    ol::complex2img(U, I, ny, nx, (ol::MODE)mode);
+    std::memcpy(img, I.get(), (long)ny * nx);
+}
+
+/* ol::quant8bit, olimg.h:178-198 */
+void ref_quant8bit(double *real, uint8_t *img, int ny, int nx) { ol::quant8bit(real, img, ny, nx); }
+
+} /* extern "C" */

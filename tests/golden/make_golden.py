@@ -1,0 +1,118 @@
+"""Generate tests/golden/ref_golden.npz from the reference's OWN CPU code.
+
+The reference (somamake/openol) ships no golden vectors and no assertions, so
+the fixtures are made by running its CPU templates -- ``ol::AsmProp``,
+``ol::FresnelProp``, ``ol::FresnelPropBandLimit``, ``ol::Prop``,
+``ol::AsmPropCheck`` / ``ol::FresnelPropCheck``, ``ol::Cgh`` (complex and phase
+outputs), ``ol::complex2img`` and ``ol::quant8bit`` -- compiled unmodified by
+``oracle/Makefile`` (``make -C oracle ref``; needs the reference sources) on
+seeded inputs.  Run from the repository root:
+
+    make -C oracle ref && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+import oracle as O  # noqa: E402
+
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ref_golden.npz")
+
+
+def field(rng, shape):
+    """Binary amplitude (p = 0.5) x uniform phase, the propagation workload's distribution."""
+    amp = (rng.random(shape) < 0.5).astype(np.float64)
+    return amp * np.exp(2j * np.pi * rng.random(shape))
+
+
+def refcall(fn, u, *args):
+    u = np.ascontiguousarray(u, np.complex128).copy()
+    fn(O._ptr(u), u.shape[0], u.shape[1], *args)
+    return u
+
+
+def main():
+    R = O.ref()
+    rng = np.random.default_rng(20261203)
+    g = {}
+    prop_cases = [
+        # (ny, nx, dy, dx, lambda, z)
+        (16, 16, 8e-6, 8e-6, 532e-9, 0.05),
+        (32, 64, 8e-6, 8e-6, 532e-9, 0.05),
+        (64, 32, 4e-6, 6e-6, 633e-9, -0.02),
+        (64, 64, 20e-6, 20e-6, 532e-9, 0.01),   # band limit active
+        (128, 128, 3.74e-6, 3.74e-6, 532e-9, 0.1),
+        (24, 40, 8e-6, 8e-6, 450e-9, 0.03),     # not a power of two: oracle-only case
+    ]
+    for i, (ny, nx, dy, dx, lam, z) in enumerate(prop_cases):
+        u = field(rng, (ny, nx))
+        g[f"prop{i}_params"] = np.array([ny, nx, dy, dx, lam, z])
+        g[f"prop{i}_in"] = u
+        g[f"prop{i}_asm"] = refcall(R.ref_asm_prop, u, dy, dx, lam, z)
+        g[f"prop{i}_fresnel"] = refcall(R.ref_fresnel_prop, u, dy, dx, lam, z)
+        g[f"prop{i}_fresnel_bl"] = refcall(R.ref_fresnel_prop_bandlimit, u, dy, dx, lam, z)
+    g["n_prop"] = np.array(len(prop_cases))
+
+    # AUTO dispatcher: one case per branch (ASM / Fresnel / band-limited Fresnel)
+    n2, p2, l2 = 64, 2e-6, 633e-9
+    u2 = 1.0 / (2 * p2)
+    zmax = np.sqrt(1 / l2**2 - 2 * u2**2) / (2 * u2 * (1 / (p2 * n2)))
+    zmin = n2 * p2 * p2 / l2
+    auto_cases = [(32, 32, 8e-6, 8e-6, 532e-9, 0.005), (32, 32, 8e-6, 8e-6, 532e-9, 2.0),
+                  (32, 32, p2, p2, l2, 0.5 * (zmax + zmin))]
+    for i, (ny, nx, dy, dx, lam, z) in enumerate(auto_cases):
+        u = field(rng, (ny, nx))
+        g[f"auto{i}_params"] = np.array([ny, nx, dy, dx, lam, z])
+        g[f"auto{i}_in"] = u
+        g[f"auto{i}_out"] = refcall(R.ref_prop, u, dy, dx, lam, z, 2)
+        g[f"auto{i}_branch"] = np.array([R.ref_asm_prop_check(ny, nx, dy, dx, lam, z),
+                                         R.ref_fresnel_prop_check(ny, nx, dy, dx, lam, z)])
+    g["n_auto"] = np.array(len(auto_cases))
+
+    # AUTO checks in float and double over a sweep of distances
+    chk = []
+    for (ny, nx, p, lam) in [(1024, 1024, 8e-6, 532e-9), (4096, 4096, 4e-6, 532e-9), (2160, 3840, 3.74e-6, 532e-9)]:
+        for z in np.geomspace(1e-3, 3.0, 25):
+            chk.append([ny, nx, p, lam, z,
+                        R.ref_asm_prop_check(ny, nx, p, p, lam, z), R.ref_asm_prop_check_f(ny, nx, p, p, lam, z),
+                        R.ref_fresnel_prop_check(ny, nx, p, p, lam, z), R.ref_fresnel_prop_check_f(ny, nx, p, p, lam, z)])
+    g["checks"] = np.array(chk)
+
+    # Fresnel-form point-cloud CGH
+    for i, (ny, nx, py, px, lam, n) in enumerate([(24, 40, 8e-6, 8e-6, 532e-9, 7), (32, 48, 6e-6, 8e-6, 633e-9, 13)]):
+        pts = np.stack([rng.random(n) * nx * px, rng.random(n) * ny * py, 0.02 + rng.random(n) * 0.02], 1)
+        pts = pts.astype(np.float32).astype(np.float64)  # representable as the float32 points the GPU takes
+        U = np.zeros((ny, nx), np.complex128)
+        R.ref_cgh(O._ptr(np.ascontiguousarray(pts)), n, O._ptr(U), ny, nx, py, px, lam)
+        g[f"cgh{i}_params"] = np.array([ny, nx, py, px, lam])
+        g[f"cgh{i}_pts"] = pts
+        g[f"cgh{i}_U"] = U
+        if py == px:
+            ph = np.zeros((ny, nx), np.float64)
+            R.ref_cgh_phase(O._ptr(np.ascontiguousarray(pts)), n, O._ptr(ph), ny, nx, py, lam)
+            g[f"cgh{i}_phase"] = ph
+    g["n_cgh"] = np.array(2)
+
+    # 8-bit quantisers
+    u = field(rng, (16, 24)) * (0.2 + rng.random((16, 24)))
+    g["q_in"] = u
+    for mode in range(4):
+        img = np.zeros((16, 24), np.uint8)
+        R.ref_complex2img(O._ptr(np.ascontiguousarray(u)), O._ptr(img), 16, 24, mode)
+        g[f"q_mode{mode}"] = img
+    real = np.ascontiguousarray(u.real)
+    img = np.zeros((16, 24), np.uint8)
+    R.ref_quant8bit(O._ptr(real.copy()), O._ptr(img), 16, 24)
+    g["q_quant8bit"] = img
+
+    np.savez_compressed(OUT, **g)
+    print("wrote", OUT, os.path.getsize(OUT), "bytes")
+
+
+if __name__ == "__main__":
+    main()

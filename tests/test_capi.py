@@ -1,0 +1,102 @@
+"""CPU: the C-ABI library loads, exports every declared entry point, and its
+host-side logic (AUTO checks, WRP plane, argument validation) matches the
+reference.  No kernel is launched here."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+
+from conftest import ROOT
+from openol_gb300 import _lib
+from openol_gb300 import build as B
+
+HEADER = os.path.join(ROOT, "include", "olgb300.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(olg_\w+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    syms = declared_symbols()
+    assert len(syms) >= 18
+    out = subprocess.run(["nm", "-D", "--defined-only", B.LIB], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r" T (olg_\w+)", out))
+    missing = [s for s in syms if s not in exported]
+    assert not missing, missing
+    L = C.CDLL(B.LIB)
+    for s in syms:
+        assert hasattr(L, s)
+
+
+def test_python_binding_covers_header():
+    assert set(declared_symbols()) <= set(_lib.SIGNATURES)
+
+
+def test_status_strings():
+    L = _lib.lib()
+    assert L.olg_version() >= 100
+    assert L.olg_status_string(0) == b"ok"
+    assert b"argument" in L.olg_status_string(-1)
+
+
+def test_auto_checks_match_reference_float_and_double(golden):
+    L = _lib.lib()
+    for ny, nx, p, lam, z, a64, a32, f64, f32 in golden["checks"]:
+        ny, nx = int(ny), int(nx)
+        assert L.olg_asm_prop_check(ny, nx, p, p, lam, z, 0) == int(a64)
+        assert L.olg_asm_prop_check(ny, nx, p, p, lam, z, 1) == int(a32)
+        assert L.olg_fresnel_prop_check(ny, nx, p, p, lam, z, 0) == int(f64)
+        assert L.olg_fresnel_prop_check(ny, nx, p, p, lam, z, 1) == int(f32)
+
+
+def _plane_z_ref(window, ny, nx, p, plimit, lam, zmin, s):
+    """golcgh.h:561-581 / 519-559 evaluated with the reference's float/double mix."""
+    f = np.float32
+    p, plimit, lam, zmin, s = f(p), f(plimit), f(lam), f(zmin), f(s)
+    if s >= 0:
+        return f(zmin * s)
+    if window == 0:
+        Wpow2 = f(np.float64(f(f(f(nx * ny) * p) * p)) / np.pi * 1 / 1024.0)
+        q = np.float64(f(p / lam))
+        d = f(np.sqrt((4 * q ** 2 - 1) * np.float64(Wpow2)))
+        return f(zmin - d)
+    D = f(np.float64(f(f(nx) * p)) * 0.05)
+    q = np.float64(f(plimit / lam))
+    d = f(np.sqrt(4 * q ** 2 - 1) / np.sqrt(2.0) * np.float64(D))
+    return f(zmin - d)
+
+
+def test_wrp_plane_z():
+    L = _lib.lib()
+    for window in (0, 1):
+        for (ny, nx, p, lam, zmin, s) in [(4096, 4096, 4e-6, 532e-9, 0.151, -1.0), (2160, 3840, 3.74e-6, 532e-9, -0.1, -1.0),
+                                          (1080, 1920, 8e-6, 633e-9, 0.2, 0.9)]:
+            got = L.olg_wrp_plane_z(window, ny, nx, p, 0.0, lam, zmin, s)
+            assert np.float32(got) == _plane_z_ref(window, ny, nx, p, p, lam, zmin, s)
+
+
+def test_argument_validation_without_gpu():
+    L = _lib.lib()
+    # rejected before any device work
+    assert L.olg_asm_prop_c64(None, None, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, None, 0, None) == -1
+    buf = (C.c_char * 64)()
+    base = (C.addressof(buf) + 15) // 16 * 16
+    assert L.olg_asm_prop_c64(base, base, 48, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, None, 0, None) == -2
+    assert L.olg_asm_prop_c64(base, base, 64, 8192, 8e-6, 8e-6, 532e-9, 0.05, 0, None, 0, None) == -2
+    assert L.olg_asm_prop_c64(base + 8, base, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, None, 0, None) == -1
+    assert L.olg_arss_prop_c64(base, base, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 1.0, 0, 0, 0, None, 0, None) == -1
+    assert b"s = 1" in L.olg_last_error() or b"s|s-1|" in L.olg_last_error()
+    assert L.olg_cgh_fresnel_c64(None, None, None, 5, None, None, 8, 8, 8e-6, 8e-6, 532e-9, 0, None) == -1
+    assert L.olg_prop_c64(base, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 7, 0, None, None, 0, None) == -1
+
+
+def test_workspace_size():
+    L = _lib.lib()
+    ws = L.olg_prop_workspace_bytes(1024, 1024)
+    assert ws >= 1024 * 2048 * 8
+    assert ws < 1024 * 2048 * 8 * 1.1

@@ -1,0 +1,106 @@
+"""GPU parity: point-cloud CGH (Fresnel form and exact spherical) through the
+C-ABI against the reference's golden vectors and the FP64 oracle.
+Gate: relative L2 <= 1e-5."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+import openol_gb300 as og
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy().astype(np.complex128)
+
+
+@pytest.mark.parametrize("i", [0, 1])
+def test_cgh_golden(golden, i):
+    ny, nx, py, px, lam = golden[f"cgh{i}_params"]
+    ny, nx = int(ny), int(nx)
+    obj = og.Object2cuda(golden[f"cgh{i}_pts"])
+    U = torch.zeros((ny, nx), dtype=torch.complex64, device="cuda")
+    og.gCgh(obj, U, ny, nx, py, px, lam)
+    assert rel_l2(host(U), golden[f"cgh{i}_U"]) < TOL
+    if f"cgh{i}_phase" in golden:
+        ph = torch.zeros((ny, nx), dtype=torch.float32, device="cuda")
+        og.gCgh(obj, ph, ny, nx, py, px, lam)
+        d = np.angle(np.exp(1j * (ph.cpu().numpy() - golden[f"cgh{i}_phase"])))
+        assert np.abs(d).max() < 1e-4
+
+
+def config2_points(n, W=1920, H=1080, p=8e-6, seed=20261205):
+    rng = np.random.default_rng(seed)
+    c = np.array([W / 2 * p, H / 2 * p, 0.1])
+    pts = c + (rng.random((n, 3)) - 0.5) * 5e-3
+    amp = 0.5 + 0.5 * rng.random(n)
+    ph = 2 * np.pi * rng.random(n)
+    return pts.astype(np.float32), amp.astype(np.float32), ph.astype(np.float32)
+
+
+@pytest.mark.parametrize("form", ["fresnel", "exact"])
+def test_cgh_workload_rows(form):
+    """The CGH benchmark workload (10,000 points, 1920 x 1080, p = 8 um,
+    532 nm); the FP64 oracle evaluates a seeded subset of 6 rows."""
+    pts, amp, ph = config2_points(10000)
+    ny, nx, p, lam = 1080, 1920, 8e-6, 532e-9
+    obj = og.gObject(pts)
+    a = torch.from_numpy(amp).cuda()
+    f = torch.from_numpy(ph).cuda()
+    U = torch.zeros((ny, nx), dtype=torch.complex64, device="cuda")
+    fn = og.cgh_fresnel if form == "fresnel" else og.cgh_exact
+    fn(obj, U, ny=ny, nx=nx, py=p, px=p, lam=lam, amp=a, phase0=f)
+    G = host(U)
+    rows = np.array([0, 1, 333, 540, 1000, 1079])
+    ofn = O.cgh_fresnel if form == "fresnel" else O.cgh_exact
+    for r in rows:
+        # oracle on one row: shift the points so that row r is row 0
+        sp = pts.astype(np.float64).copy()
+        sp[:, 1] -= p * r
+        ref = ofn(sp, 1, nx, p, p, lam, amp=amp.astype(np.float64), phase0=ph.astype(np.float64))
+        assert rel_l2(G[r:r + 1], ref) < TOL, (form, r)
+
+
+@pytest.mark.parametrize("form", ["fresnel", "exact"])
+@pytest.mark.parametrize("shape,n", [((37, 53), 1), ((64, 48), 300), ((33, 17), 257), ((16, 16), 0)])
+def test_cgh_edges(form, shape, n):
+    ny, nx = shape
+    rng = np.random.default_rng(n + ny)
+    pts = np.stack([rng.random(n) * nx * 6e-6, rng.random(n) * ny * 6e-6, 0.005 + rng.random(n) * 0.02], 1)
+    pts = pts.astype(np.float32).reshape(-1, 3)
+    U = torch.full((ny, nx), 1 + 1j, dtype=torch.complex64, device="cuda")
+    fn = og.cgh_fresnel if form == "fresnel" else og.cgh_exact
+    fn(og.gObject(pts), U, ny=ny, nx=nx, py=6e-6, px=6e-6, lam=633e-9)
+    ofn = O.cgh_fresnel if form == "fresnel" else O.cgh_exact
+    ref = ofn(pts.astype(np.float64), ny, nx, 6e-6, 6e-6, 633e-9)
+    if n == 0:
+        assert np.abs(host(U)).max() == 0
+    else:
+        assert rel_l2(host(U), ref) < TOL
+
+
+def test_cgh_reduction_accumulates():
+    rng = np.random.default_rng(4)
+    pts = np.stack([rng.random(40) * 32 * 8e-6, rng.random(40) * 32 * 8e-6, 0.02 + rng.random(40) * 0.01], 1)
+    obj = og.gObject(pts)
+    U = torch.zeros((32, 32), dtype=torch.complex64, device="cuda")
+    og.gCghReduction(obj, U, 32, 32, 8e-6, 532e-9)
+    og.gCghReduction(obj, U, 32, 32, 8e-6, 532e-9)
+    ref = 2 * O.cgh_fresnel(pts.astype(np.float32).astype(np.float64), 32, 32, 8e-6, 8e-6, 532e-9)
+    assert rel_l2(host(U), ref) < TOL
+
+
+def test_single_point_is_analytic_chirp():
+    """One point on the optical axis of pixel (16, 16): U = exp(i pi rho^2 / (lambda z))."""
+    p, lam, z = 8e-6, 532e-9, 0.05
+    pts = np.array([[16 * p, 16 * p, z]], np.float32)
+    U = torch.zeros((32, 32), dtype=torch.complex64, device="cuda")
+    og.cgh_fresnel(og.gObject(pts), U, ny=32, nx=32, py=p, px=p, lam=lam)
+    w = np.arange(32)
+    X, Y = np.meshgrid(w * p - np.float64(np.float32(16 * p)), w * p - np.float64(np.float32(16 * p)))
+    ref = np.exp(1j * np.pi * (X ** 2 + Y ** 2) / (lam * np.float64(np.float32(z))))
+    assert rel_l2(host(U), ref) < TOL
