@@ -249,8 +249,19 @@ def run_ours(args):
         def step_exact():
             og.cgh_exact(obj, U, ny=c["ny"], nx=c["nx"], py=c["p"], px=c["p"], lam=c["lam"], amp=a, phase0=f)
 
-        forms = {"fresnel_direct": step_fresnel, "exact": step_exact}
-        chosen = "fresnel_direct"
+        gws = og.cgh_gemm_workspace(c["n"], c["ny"], c["nx"])
+
+        def step_gemm():
+            og.cgh_fresnel_gemm(obj, U, ny=c["ny"], nx=c["nx"], py=c["p"], px=c["p"], lam=c["lam"], amp=a,
+                                phase0=f, work=gws)
+
+        def step_gemm_only():
+            og.cgh_fresnel_gemm(obj, U, ny=c["ny"], nx=c["nx"], py=c["p"], px=c["p"], lam=c["lam"], amp=a,
+                                phase0=f, work=gws, reuse_operands=True)
+
+        forms = {"fresnel_gemm": step_gemm, "fresnel_gemm_kernel_only": step_gemm_only,
+                 "fresnel_direct": step_fresnel, "exact": step_exact}
+        chosen = "fresnel_gemm"
         res = {}
         with ClockSampler(local) as clk:
             for name, fn in forms.items():
@@ -259,6 +270,7 @@ def run_ours(args):
                 launches = (og.launch_count() - l0) // (K + W) * K
                 res[name] = (ms, launches)
         clocks = clk.summary()
+        og.device_fault_check()
         ms_c, launches = res[chosen]
         t_step = max_over_ranks(statistics.mean(ms_c))
         value = ws * units / (t_step * 1e-3)
@@ -272,29 +284,38 @@ def run_ours(args):
             obj.points.copy_(hp, non_blocking=True)
             a.copy_(ha, non_blocking=True)
             f.copy_(hf, non_blocking=True)
-            step_fresnel()
+            step_gemm()
             hU.copy_(U, non_blocking=True)
 
         ms_e = timed(torch, step_e2e, K, W, flush, stream, barrier)
         t_e2e = max_over_ranks(statistics.mean(ms_e))
-        # SFU roofline of the chosen kernel: 2 MUFU (sin, cos) per point.pixel, 16 MUFU/clk/SM
+        # tensor roofline of the dominant kernel (k_cgh_gemm, timed alone with the
+        # operands already built): issued f16 MMA work 24 M N K flop per hologram
+        ms_g = statistics.mean(res["fresnel_gemm_kernel_only"][0])
+        kpad = ((2 * c["n"] + 63) // 64) * 64 // 2
+        issued = 24.0 * c["ny"] * c["nx"] * kpad
+        ach_tf = issued / (ms_g * 1e-3) / 1e12
         nsm = torch.cuda.get_device_properties(0).multi_processor_count
         mhz = clocks.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
         peak_gops = nsm * 16 * mhz * 1e6 / 1e9
-        ach_gops = 2 * units / (statistics.mean(ms_c) * 1e-3) / 1e9
+        sfu_gops = 2 * units / (statistics.mean(res["exact"][0]) * 1e-3) / 1e9
         out = {
             "metric": "CGH point.pixel/s", "value": value, "unit": "point.pixel/s",
             "ms_per_step": t_step,
-            "dtype": "f32 (double-float phase reduction)",
+            "dtype": "f16x3 split products, f32 accumulate",
             "config": {"workload": "cgh 1920x1080, 10000 points, p=8um, lambda=532nm, 5mm box at z=100mm",
                        "form": chosen, "l2": "flushed between steps (256 MiB write)"},
             "e2e": {"value": ws * units / (t_e2e * 1e-3), "unit": "point.pixel/s",
                     "h2d_bytes_per_step": pts.nbytes + amp.nbytes + ph.nbytes,
                     "d2h_bytes_per_step": c["ny"] * c["nx"] * 8},
             "gpu_launches": int(launches),
-            "roofline": {"bound": "sfu", "achieved": ach_gops, "peak": peak_gops, "unit": "Gop/s (MUFU)",
-                         "frac": ach_gops / peak_gops, "traffic": None,
-                         "note": f"2 MUFU per term; peak = {nsm} SM x 16 MUFU/clk x median SM clock {mhz} MHz"},
+            "roofline": {"bound": "tensor", "achieved": ach_tf, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                         "frac": ach_tf / pk["bf16_tflops"], "traffic": None,
+                         "note": f"k_cgh_gemm alone ({ms_g:.3f} ms): 24 M N K issued f16 flop (3 split products x "
+                                 f"4 real GEMMs), useful 8 M N K; peak = {pk_kind} dense bf16 (f16 same rate)"},
+            "exact_kernel_sfu": {"achieved": sfu_gops, "peak": peak_gops, "unit": "Gop/s (MUFU)",
+                                 "frac": sfu_gops / peak_gops,
+                                 "note": f"2 MUFU per term; peak {nsm} SM x 16 MUFU/clk x {mhz} MHz"},
             "forms": {k: {"point.pixel/s": units / (statistics.mean(v[0]) * 1e-3), "ms": statistics.mean(v[0])}
                       for k, v in res.items()},
             "clocks": clocks,

@@ -22,8 +22,8 @@
  *    pool (cudaMallocAsync / cudaFreeAsync on `stream`).
  *  - In-place operation is allowed wherever an input and an output pointer
  *    have the same shape (u_in == u_out).
- *  - Sizes: the FFT engine handles ny, nx powers of two in [32, 4096]
- *    (padded grid 64 .. 8192); other sizes return OLG_ERR_UNSUPPORTED_SIZE.
+ *  - Sizes: the FFT engine handles ny, nx powers of two in [16, 4096]
+ *    (padded grid 32 .. 8192); other sizes return OLG_ERR_UNSUPPORTED_SIZE.
  */
 #ifndef OLGB300_H
 #define OLGB300_H
@@ -47,6 +47,7 @@ extern "C" {
 #define OLG_ACCUMULATE 0x4   /* out += result (gCghReduction semantics) */
 #define OLG_VERBOSE 0x8      /* print the chosen method like the reference's printf */
 #define OLG_CHECK_F32 0x10   /* olg_prop_c64: evaluate the AUTO checks in float (PREC_T=float) */
+#define OLG_REUSE_OPERANDS 0x20 /* olg_cgh_fresnel_gemm_c64: operands already in `work` from a call with the same points */
 
 /* propagation modes, ol::PROPMODE (oldefine.h:7-9) */
 #define OLG_ASM 0
@@ -133,6 +134,21 @@ int olg_cgh_fresnel_c64(const float *points, const float *amp, const float *phas
  * range reduced per pixel tile in double-float arithmetic. */
 int olg_cgh_exact_c64(const float *points, const float *amp, const float *phase0, int n_points, void *U,
                       int ny, int nx, double py, double px, double lambda, int flags, olg_stream_t stream);
+
+/* Fresnel-form CGH (same sum as olg_cgh_fresnel_c64, amplitudes/phases
+ * included) as a split-FP16 complex GEMM on the tcgen05 tensor cores:
+ * U = Y' X^T with X[w,j], Y'[h,j] the separable per-point chirps, each f16
+ * hi + lo, three f16 products accumulated in f32.  nx, ny <= 4096.
+ * Scratch: olg_cgh_gemm_workspace_bytes() (work == NULL: stream-ordered pool).
+ * A bounded wait that expires inside the kernel is reported by
+ * olg_device_fault_check(). */
+size_t olg_cgh_gemm_workspace_bytes(int n_points, int ny, int nx);
+int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, const float *phase0, int n_points, void *U,
+                             int ny, int nx, double py, double px, double lambda, int flags, void *work,
+                             size_t work_bytes, olg_stream_t stream);
+/* Synchronises the device and reports (OLG_ERR_CUDA) whether any tensor-core
+ * kernel of this library gave up on a bounded wait; clear != 0 resets the flag. */
+int olg_device_fault_check(int clear);
 
 /* ------------------------------------------------------------------- WRP */
 /* plane_z of ol::WRPMethod (golcgh.h:561-581, window = circle) and

@@ -19,6 +19,7 @@ OLG_NO_NORMALIZE = 0x2
 OLG_ACCUMULATE = 0x4
 OLG_VERBOSE = 0x8
 OLG_CHECK_F32 = 0x10
+OLG_REUSE_OPERANDS = 0x20
 
 _d, _f, _i, _p, _sz = C.c_double, C.c_float, C.c_int, C.c_void_p, C.c_size_t
 
@@ -37,6 +38,9 @@ SIGNATURES = {
     "olg_prop_c64": (_i, [_p, _i, _i, _d, _d, _d, _d, _i, _i, C.POINTER(_i), _p, _sz, _p]),
     "olg_cgh_fresnel_c64": (_i, [_p, _p, _p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p]),
     "olg_cgh_exact_c64": (_i, [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d, _i, _p]),
+    "olg_cgh_gemm_workspace_bytes": (_sz, [_i, _i, _i]),
+    "olg_cgh_fresnel_gemm_c64": (_i, [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_device_fault_check": (_i, [_i]),
     "olg_wrp_plane_z": (_f, [_i, _i, _i, _f, _f, _f, _f, _f]),
     "olg_wrp_step1_c64": (_i, [_p, _i, _p, _i, _i, _f, _f, _f, _f, _i, _p]),
     "olg_wrp_method_c64": (_i, [_p, _i, _p, _i, _i, _f, _f, _f, _f, _f, _i, _i, _i, C.POINTER(_f), _p]),

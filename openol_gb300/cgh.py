@@ -12,7 +12,7 @@ import ctypes as C
 import numpy as np
 import torch
 
-from ._lib import OLG_ACCUMULATE, OLG_VERBOSE, call, lib
+from ._lib import OLG_ACCUMULATE, OLG_REUSE_OPERANDS, OLG_VERBOSE, call, lib
 from .prop import PROPMODE, _dev_field, _stream
 
 
@@ -69,6 +69,28 @@ def cgh_exact(gobj, U, *, ny, nx, py, px, lam, amp=None, phase0=None, accumulate
     call("olg_cgh_exact_c64", gobj.points.data_ptr(), _opt(amp), _opt(phase0), gobj.size, U.data_ptr(), ny, nx,
          float(py), float(px), float(lam), OLG_ACCUMULATE if accumulate else 0, _stream(stream))
     return U
+
+
+def cgh_fresnel_gemm(gobj, U, *, ny, nx, py, px, lam, amp=None, phase0=None, accumulate=False, stream=None,
+                     work=None, reuse_operands=False):
+    """Fresnel-form CGH as a split-FP16 tensor-core GEMM (olg_cgh_fresnel_gemm_c64).
+    ``reuse_operands``: the f16 operands are already in ``work`` from a previous
+    call with the same points, pitch and wavelength; only the GEMM runs."""
+    _dev_field(U, ny, nx, "U")
+    wp, wb = (work.data_ptr(), work.numel() * work.element_size()) if work is not None else (None, 0)
+    flags = (OLG_ACCUMULATE if accumulate else 0) | (OLG_REUSE_OPERANDS if reuse_operands else 0)
+    call("olg_cgh_fresnel_gemm_c64", gobj.points.data_ptr(), _opt(amp), _opt(phase0), gobj.size, U.data_ptr(),
+         ny, nx, float(py), float(px), float(lam), flags, wp, wb, _stream(stream))
+    return U
+
+
+def cgh_gemm_workspace(n_points, ny, nx, device="cuda"):
+    return torch.empty(int(lib().olg_cgh_gemm_workspace_bytes(n_points, ny, nx)), dtype=torch.uint8, device=device)
+
+
+def device_fault_check(clear=True):
+    """Raise OlgError if a tensor-core kernel gave up on a bounded wait (synchronises)."""
+    call("olg_device_fault_check", int(clear))
 
 
 def gCgh(gobj, U, ny, nx, *params):

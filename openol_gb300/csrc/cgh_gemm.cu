@@ -1,0 +1,415 @@
+// cgh_gemm.cu -- Fresnel-form point-cloud CGH as a split-FP16 complex GEMM on
+// the 5th-generation tensor cores (tcgen05 + TMA + TMEM, sm_103a).
+//
+// The Fresnel kernel of the reference (golcgh.h:47-145) is separable per
+// point:  exp(i pi ((px w - x_j)^2 + (py h - y_j)^2) / (lambda z_j))
+//       = X[w, j] * Y[h, j],   so   U = Y' X^T  with Y'[h, j] = a_j e^{i phi_j} Y[h, j],
+// a complex GEMM with M = ny, N = nx, K = n points.  As one real GEMM with the
+// real / imaginary parts interleaved on the M side:
+//   A (2M x 2K): row 2h = [Re Y', -Im Y'] per point, row 2h+1 = [Im Y', Re Y']
+//   B (N  x 2K): row w  = [Re X,  Im X ]
+//   D = A B^T (2M x N): D[2h, w] = Re U[h, w], D[2h+1, w] = Im U[h, w].
+// Precision: each operand is split into f16 hi + lo (22 significant bits);
+// D = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T accumulated in f32 in TMEM
+// (three K segments of one accumulation).  Issued tensor work 3 x 2 x 2M N 2K
+// = 24 M N K flop for 8 M N K useful.
+//
+// k_cgh_gemm_prep  per point, FP64: expansion coefficients of the x / y phases
+// k_cgh_gemm_ops   builds A_hi/A_lo/B_hi/B_lo (f16, K-contiguous, zero padded),
+//                  phases range-reduced exactly (frac_mul), sincospif
+// k_cgh_gemm       warp-specialised tcgen05 GEMM: warp 0 issues TMA loads into a
+//                  4-stage ring (128 x 64 A and 256 x 64 B f16 tiles, 128-byte
+//                  swizzle), warp 1 owns TMEM (256 f32 columns) and issues the
+//                  128 x 256 x 16 MMAs, warps 2-5 drain TMEM and write complex64.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <mutex>
+
+#include "common.cuh"
+#include "tc.cuh"
+
+namespace olg {
+
+constexpr int GB_M = 128, GB_N = 256, GB_K = 64, GB_STAGES = 4;
+constexpr int GB_A_BYTES = GB_M * GB_K * 2;
+constexpr int GB_B_BYTES = GB_N * GB_K * 2;
+constexpr int GB_SMEM = GB_STAGES * (GB_A_BYTES + GB_B_BYTES) + 1024 + 256;
+constexpr long long GB_WAIT = 4000000000LL; // ~2 s of SM clock per wait
+
+struct PointCoef {
+    float ax_hi, ax_lo, bx_hi, bx_lo, gx; // cycles(w) = ax w^2 - bx w + gx
+    float ay_hi, ay_lo, by_hi, by_lo, gy;
+    float cr, ci;                         // a_j e^{i phi_j}
+};
+
+struct GemmOps {
+    const float *pts, *amp, *ph0;
+    int n, ny, nx, kp; // kp: K row stride (elements), >= 2n, multiple of 64
+    double px, py, lambda;
+    PointCoef *coef;
+    __half *a_hi, *a_lo, *b_hi, *b_lo;
+};
+
+__global__ void k_cgh_gemm_prep(GemmOps G)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= G.n) return;
+    const double x = G.pts[3 * j], y = G.pts[3 * j + 1], z = G.pts[3 * j + 2];
+    const double k2 = 1.0 / (2.0 * G.lambda * z); // cycles per m^2
+    PointCoef c;
+    auto put = [](double v, float &hi, float &lo) {
+        hi = (float)v;
+        lo = (float)(v - (double)hi);
+    };
+    put(k2 * G.px * G.px, c.ax_hi, c.ax_lo);
+    put(2.0 * k2 * G.px * x, c.bx_hi, c.bx_lo);
+    double g = k2 * x * x;
+    c.gx = (float)(g - rint(g));
+    put(k2 * G.py * G.py, c.ay_hi, c.ay_lo);
+    put(2.0 * k2 * G.py * y, c.by_hi, c.by_lo);
+    g = k2 * y * y;
+    c.gy = (float)(g - rint(g));
+    const double a = G.amp ? (double)G.amp[j] : 1.0;
+    const double ph = G.ph0 ? (double)G.ph0[j] : 0.0;
+    c.cr = (float)(a * cos(ph));
+    c.ci = (float)(a * sin(ph));
+    G.coef[j] = c;
+}
+
+__device__ __forceinline__ void split2(float v, __half &hi, __half &lo)
+{
+    hi = __float2half_rn(v);
+    lo = __float2half_rn(v - __half2float(hi));
+}
+
+// grid.y = row block of (N rows of B, then M rows of A); x = point index
+__global__ void k_cgh_gemm_ops(GemmOps G)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x; // point index (pairs of K columns)
+    const int r = blockIdx.y;                            // 0..nx-1: B row w; nx..nx+ny-1: A rows 2h, 2h+1
+    if (2 * j >= G.kp) return;
+    __half2 hi0, lo0, hi1, lo1;
+    const bool isB = r < G.nx;
+    if (j >= G.n) {
+        hi0 = lo0 = hi1 = lo1 = __floats2half2_rn(0.f, 0.f);
+    } else {
+        const PointCoef c = G.coef[j];
+        float re, im;
+        if (isB) {
+            const float w = (float)r;
+            const float cyc = frac_mul(c.ax_hi, c.ax_lo, w * w) - frac_mul(c.bx_hi, c.bx_lo, w) + c.gx;
+            sincospif(2.0f * wrap_cycles(cyc), &im, &re);
+        } else {
+            const float h = (float)(r - G.nx);
+            const float cyc = frac_mul(c.ay_hi, c.ay_lo, h * h) - frac_mul(c.by_hi, c.by_lo, h) + c.gy;
+            float s, co;
+            sincospif(2.0f * wrap_cycles(cyc), &s, &co);
+            re = c.cr * co - c.ci * s;
+            im = c.cr * s + c.ci * co;
+        }
+        __half h0, l0, h1, l1;
+        if (isB) {
+            split2(re, h0, l0);
+            split2(im, h1, l1);
+            hi0 = __halves2half2(h0, h1);
+            lo0 = __halves2half2(l0, l1);
+        } else {
+            // row 2h: [re, -im], row 2h+1: [im, re]
+            __half hr, lr, hm, lm, hmn, lmn;
+            split2(re, hr, lr);
+            split2(im, hm, lm);
+            hmn = __hneg(hm);
+            lmn = __hneg(lm);
+            hi0 = __halves2half2(hr, hmn);
+            lo0 = __halves2half2(lr, lmn);
+            hi1 = __halves2half2(hm, hr);
+            lo1 = __halves2half2(lm, lr);
+        }
+    }
+    if (isB) {
+        const size_t o = (size_t)r * G.kp + 2 * j;
+        *reinterpret_cast<__half2 *>(G.b_hi + o) = hi0;
+        *reinterpret_cast<__half2 *>(G.b_lo + o) = lo0;
+    } else {
+        const int h = r - G.nx;
+        const size_t o0 = (size_t)(2 * h) * G.kp + 2 * j, o1 = o0 + G.kp;
+        *reinterpret_cast<__half2 *>(G.a_hi + o0) = hi0;
+        *reinterpret_cast<__half2 *>(G.a_lo + o0) = lo0;
+        *reinterpret_cast<__half2 *>(G.a_hi + o1) = hi1;
+        *reinterpret_cast<__half2 *>(G.a_lo + o1) = lo1;
+    }
+}
+
+struct GemmParams {
+    int m2, n, kblocks; // rows of D (2 ny), columns (nx), K blocks of 64 per segment
+    float2 *U;
+    int accumulate;
+    int *err;
+};
+
+__global__ void __launch_bounds__(192, 1)
+    k_cgh_gemm(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
+               const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, GemmParams P)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + GB_STAGES * GB_A_BYTES;
+    uint64_t *full = (uint64_t *)(sB + GB_STAGES * GB_B_BYTES);
+    uint64_t *empty = full + GB_STAGES;
+    uint64_t *done = empty + GB_STAGES;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    volatile int *fault = (volatile int *)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
+    const int total = 3 * P.kblocks;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < GB_STAGES; ++s) {
+            mbar_init(smem_u32(full + s), 1);
+            mbar_init(smem_u32(empty + s), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        *fault = 0;
+        fence_mbar_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(smem_u32(tmem_slot), GB_N);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int kb = 0; kb < total && !*fault; ++kb) {
+                const int s = kb % GB_STAGES;
+                const uint32_t ph = (uint32_t)(kb / GB_STAGES) & 1u;
+                if (!mbar_wait(smem_u32(empty + s), ph ^ 1u, GB_WAIT)) {
+                    *fault = 1;
+                    break;
+                }
+                const int seg = kb / P.kblocks, kk = (kb % P.kblocks) * GB_K;
+                const CUtensorMap *ma = seg < 2 ? &tAh : &tAl;
+                const CUtensorMap *mb = seg == 1 ? &tBl : &tBh;
+                mbar_expect_tx(smem_u32(full + s), GB_A_BYTES + GB_B_BYTES);
+                tma_load_2d(smem_u32(sA + s * GB_A_BYTES), ma, smem_u32(full + s), kk, m0);
+                tma_load_2d(smem_u32(sB + s * GB_B_BYTES), mb, smem_u32(full + s), kk, n0);
+                issued = kb + 1;
+            }
+            // never leave with copies in flight: wait (bounded) for the last
+            // stages issued to land before the CTA may exit
+            for (int kb = issued > GB_STAGES ? issued - GB_STAGES : 0; kb < issued; ++kb)
+                mbar_wait(smem_u32(full + kb % GB_STAGES), (uint32_t)(kb / GB_STAGES) & 1u, GB_WAIT);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_f16_f32(GB_M, GB_N);
+            for (int kb = 0; kb < total && !*fault; ++kb) {
+                const int s = kb % GB_STAGES;
+                if (!mbar_wait(smem_u32(full + s), (uint32_t)(kb / GB_STAGES) & 1u, GB_WAIT)) {
+                    *fault = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * GB_B_BYTES);
+#pragma unroll
+                for (int k = 0; k < GB_K / 16; ++k)
+                    umma_f16(tmem, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), idesc, (kb | k) ? 1u : 0u);
+                umma_commit(smem_u32(empty + s));
+            }
+            umma_commit(smem_u32(done));
+        }
+    } else {
+        // epilogue: warp w drains TMEM lanes [32 (w % 4), +32)
+        const int q = warp & 3;
+        const bool ok = mbar_wait(smem_u32(done), 0u, GB_WAIT);
+        if (!ok) *fault = 1;
+        tc_fence_after();
+        const int row = m0 + 32 * q + lane; // row of D
+        const int h = row >> 1;
+        const bool odd = row & 1;
+        for (int c = 0; c < GB_N; c += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c, v);
+            float o[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) o[i] = __shfl_xor_sync(0xffffffffu, v[i], 1);
+            if (!ok || *fault || row >= P.m2) continue;
+            // even lane holds Re of row h, odd lane Im: even writes columns c..c+7, odd c+8..c+15
+            const int cb = n0 + c + (odd ? 8 : 0);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int col = cb + i;
+                if (col >= P.n) break;
+                const float re = odd ? o[8 + i] : v[i];
+                const float im = odd ? v[8 + i] : o[i];
+                float2 *dst = P.U + (size_t)h * P.n + col;
+                if (P.accumulate) {
+                    const float2 prev = *dst;
+                    *dst = make_float2(prev.x + re, prev.y + im);
+                } else {
+                    *dst = make_float2(re, im);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) tmem_dealloc(tmem, GB_N);
+    if (threadIdx.x == 0 && *fault) atomicExch(P.err, 1);
+}
+
+// ------------------------------------------------------------------ host
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::mutex g_encode_mu;
+int *g_err_flag[64] = {};
+
+int get_encode()
+{
+    std::lock_guard<std::mutex> lk(g_encode_mu);
+    if (g_encode) return OLG_OK;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess) return fail(OLG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    return OLG_OK;
+}
+
+int err_flag(int **out)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_encode_mu);
+    if (!g_err_flag[dev]) {
+        cudaError_t e = cudaMalloc(&g_err_flag[dev], sizeof(int));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (error flag)");
+        e = cudaMemset(g_err_flag[dev], 0, sizeof(int));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemset (error flag)");
+    }
+    *out = g_err_flag[dev];
+    return OLG_OK;
+}
+
+int make_map(CUtensorMap *m, void *base, uint64_t rows, uint64_t kp, uint32_t box_rows)
+{
+    cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
+    cuuint32_t box[2] = {(cuuint32_t)GB_K, box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? OLG_OK : fail(OLG_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+}
+
+size_t gemm_layout(int n, int ny, int nx, int *kp_out, size_t off[5])
+{
+    const int kp = (int)align_up((size_t)2 * (size_t)(n > 0 ? n : 1), GB_K);
+    size_t o = 0;
+    off[0] = o; o += align_up((size_t)n * sizeof(PointCoef) + 16, 1024);
+    off[1] = o; o += align_up((size_t)2 * ny * kp * 2, 1024); // a_hi
+    off[2] = o; o += align_up((size_t)2 * ny * kp * 2, 1024); // a_lo
+    off[3] = o; o += align_up((size_t)nx * kp * 2, 1024);     // b_hi
+    off[4] = o; o += align_up((size_t)nx * kp * 2, 1024);     // b_lo
+    if (kp_out) *kp_out = kp;
+    return o;
+}
+
+} // namespace
+} // namespace olg
+
+using namespace olg;
+
+extern "C" size_t olg_cgh_gemm_workspace_bytes(int n_points, int ny, int nx)
+{
+    size_t off[5];
+    return gemm_layout(n_points, ny, nx, nullptr, off);
+}
+
+extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, const float *phase0, int n_points,
+                                        void *U, int ny, int nx, double py, double px, double lambda, int flags,
+                                        void *work, size_t work_bytes, olg_stream_t stream)
+{
+    if ((!points && n_points > 0) || !U) return fail(OLG_ERR_INVALID_ARG, "null pointer");
+    if (n_points < 0 || ny <= 0 || nx <= 0 || nx > (1 << 20) || ny > (1 << 20)) return fail(OLG_ERR_INVALID_ARG, "bad sizes");
+    if (nx > 4096 || ny > 4096) return fail(OLG_ERR_UNSUPPORTED_SIZE, "hologram side must be <= 4096 (exact w^2 in float)");
+    if (!(px > 0) || !(py > 0) || !(lambda > 0)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (int rc = get_encode()) return rc;
+    int *err = nullptr;
+    if (int rc = err_flag(&err)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    int kp = 0;
+    size_t off[5];
+    const size_t need = gemm_layout(n_points, ny, nx, &kp, off);
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, need, st)) return rc;
+    char *base = (char *)sc.ptr;
+    GemmOps G{};
+    G.pts = points; G.amp = amp; G.ph0 = phase0; G.n = n_points; G.ny = ny; G.nx = nx; G.kp = kp;
+    G.px = px; G.py = py; G.lambda = lambda;
+    G.coef = (PointCoef *)(base + off[0]);
+    G.a_hi = (__half *)(base + off[1]);
+    G.a_lo = (__half *)(base + off[2]);
+    G.b_hi = (__half *)(base + off[3]);
+    G.b_lo = (__half *)(base + off[4]);
+    const bool reuse = (flags & OLG_REUSE_OPERANDS) != 0;
+    if (reuse && !work) return fail(OLG_ERR_INVALID_ARG, "OLG_REUSE_OPERANDS needs the caller's workspace");
+    if (n_points > 0 && !reuse) {
+        k_cgh_gemm_prep<<<(n_points + 255) / 256, 256, 0, st>>>(G);
+        count_launch();
+        if (int rc = check_launch("k_cgh_gemm_prep")) return rc;
+    }
+    if (!reuse) {
+        dim3 og((kp / 2 + 127) / 128, nx + ny);
+        k_cgh_gemm_ops<<<og, 128, 0, st>>>(G);
+        count_launch();
+        if (int rc = check_launch("k_cgh_gemm_ops")) return rc;
+    }
+    CUtensorMap mAh, mAl, mBh, mBl;
+    if (int rc = make_map(&mAh, G.a_hi, 2 * (uint64_t)ny, kp, GB_M)) return rc;
+    if (int rc = make_map(&mAl, G.a_lo, 2 * (uint64_t)ny, kp, GB_M)) return rc;
+    if (int rc = make_map(&mBh, G.b_hi, nx, kp, GB_N)) return rc;
+    if (int rc = make_map(&mBl, G.b_lo, nx, kp, GB_N)) return rc;
+    GemmParams P{};
+    P.m2 = 2 * ny;
+    P.n = nx;
+    P.kblocks = kp / GB_K;
+    P.U = (float2 *)U;
+    P.accumulate = (flags & OLG_ACCUMULATE) ? 1 : 0;
+    P.err = err;
+    static bool attr_done[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!attr_done[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(k_cgh_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm)");
+        attr_done[dev] = true;
+    }
+    dim3 grid((nx + GB_N - 1) / GB_N, (2 * ny + GB_M - 1) / GB_M);
+    k_cgh_gemm<<<grid, 192, GB_SMEM, st>>>(mAh, mAl, mBh, mBl, P);
+    count_launch();
+    return check_launch("k_cgh_gemm");
+}
+
+extern "C" int olg_device_fault_check(int clear)
+{
+    int *err = nullptr;
+    if (int rc = err_flag(&err)) return rc;
+    int h = 0;
+    cudaError_t e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "reading the device fault flag");
+    if (clear && h) cudaMemset(err, 0, sizeof(int));
+    if (h) return fail(OLG_ERR_CUDA, "a tensor-core kernel gave up on a bounded wait");
+    return OLG_OK;
+}

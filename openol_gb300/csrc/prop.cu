@@ -382,6 +382,7 @@ int launch_chirp(const ChirpAxis &A, cudaStream_t st)
 
 #define OLG_SIZE_SWITCH(n, FN, ...)                                                                              \
     switch (n) {                                                                                                 \
+    case 32: return FN<32>(__VA_ARGS__);                                                                         \
     case 64: return FN<64>(__VA_ARGS__);                                                                         \
     case 128: return FN<128>(__VA_ARGS__);                                                                       \
     case 256: return FN<256>(__VA_ARGS__);                                                                       \
@@ -425,8 +426,8 @@ int validate(const void *a, const void *b, int ny, int nx)
 {
     if (!a || !b) return fail(OLG_ERR_INVALID_ARG, "null field pointer");
     if (((uintptr_t)a & 15) || ((uintptr_t)b & 15)) return fail(OLG_ERR_INVALID_ARG, "field pointers must be 16-byte aligned");
-    if (!is_pow2(nx) || !is_pow2(ny) || nx < 32 || ny < 32 || 2 * nx > FFT_MAX || 2 * ny > FFT_MAX)
-        return fail(OLG_ERR_UNSUPPORTED_SIZE, "ny, nx must be powers of two in [32, 4096]");
+    if (!is_pow2(nx) || !is_pow2(ny) || nx < 16 || ny < 16 || 2 * nx > FFT_MAX || 2 * ny > FFT_MAX)
+        return fail(OLG_ERR_UNSUPPORTED_SIZE, "ny, nx must be powers of two in [16, 4096]");
     return OLG_OK;
 }
 
