@@ -1,0 +1,137 @@
+/*
+ * golprop.h (drop-in) -- the reference's GPU propagation templates
+ * (include/golprop.h) with the same names and signatures, forwarding to
+ * libolgb300.so (include/olgb300.h).  Like the reference wrappers, each call
+ * returns with the device synchronised; errors throw std::runtime_error (the
+ * reference's CHECK_CUDA_ERROR behaviour) instead of passing silently.
+ * Fields are complex64 (thrust::complex<float>).  AsmPropCheck /
+ * FresnelPropCheck stay in the reference's CPU olprop.h; Prop evaluates them
+ * through olg_asm_prop_check / olg_fresnel_prop_check in PREC_T precision.
+ */
+#ifndef OLGB300_GOLPROP_H
+#define OLGB300_GOLPROP_H
+#include <thrust/complex.h>
+
+#include <complex>
+#include <cstdio>
+#include <string>
+#include <type_traits>
+
+#include "../olgb300.h"
+#include "golclass.h"
+#include "oldefine.h"
+
+namespace ol {
+namespace olgb {
+inline void check(int rc, const char *where)
+{
+    if (rc != OLG_OK) throw std::runtime_error(std::string(where) + ": " + olg_last_error());
+}
+inline void sync(const char *where) { CHECK_CUDA_ERROR(cudaDeviceSynchronize()); (void)where; }
+template <typename C>
+constexpr void complex64_only()
+{
+    static_assert(std::is_same<C, float>::value, "libolgb300 propagates complex64 (thrust::complex<float>) fields");
+}
+template <typename COMPLEX_T, typename F>
+void host_roundtrip(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int ny, int nx, F &&fn)
+{
+    complex64_only<COMPLEX_T>();
+    const size_t bytes = sizeof(std::complex<float>) * (size_t)ny * nx;
+    void *d = nullptr;
+    CHECK_CUDA_ERROR(cudaMalloc(&d, bytes));
+    CHECK_CUDA_ERROR(cudaMemcpy(d, u.get(), bytes, cudaMemcpyHostToDevice));
+    fn(d);
+    CHECK_CUDA_ERROR(cudaMemcpy(u.get(), d, bytes, cudaMemcpyDeviceToHost));
+    CHECK_CUDA_ERROR(cudaFree(d));
+}
+} // namespace olgb
+
+// device overload, golprop.h:507-534
+template <typename COMPLEX_T, typename PREC_T>
+void gAsmProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx, PREC_T lambda,
+              PREC_T d)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    olgb::check(olg_asm_prop_c64(u.get(), u.get(), ny, nx, dy, dx, lambda, d, 0, nullptr, 0, nullptr), "gAsmProp");
+    olgb::sync("gAsmProp");
+}
+
+// host overload (no 1/Np), golprop.h:458-504
+template <typename COMPLEX_T, typename PREC_T>
+void gAsmProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx, PREC_T lambda,
+              PREC_T d)
+{
+    olgb::host_roundtrip(u, ny, nx, [&](void *p) {
+        olgb::check(olg_asm_prop_c64(p, p, ny, nx, dy, dx, lambda, d, OLG_NO_NORMALIZE, nullptr, 0, nullptr), "gAsmProp");
+    });
+}
+
+// device overload, golprop.h:167-198
+template <typename COMPLEX_T, typename PREC_T>
+void gFresnelProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx,
+                  PREC_T lambda, PREC_T d)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    olgb::check(olg_fresnel_prop_c64(u.get(), u.get(), ny, nx, dy, dx, lambda, d, 0, 0, nullptr, 0, nullptr),
+                "gFresnelProp");
+    olgb::sync("gFresnelProp");
+}
+
+// host overload, golprop.h:70-124
+template <typename COMPLEX_T, typename PREC_T>
+void gFresnelProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx, PREC_T lambda,
+                  PREC_T d)
+{
+    olgb::host_roundtrip(u, ny, nx, [&](void *p) {
+        olgb::check(olg_fresnel_prop_c64(p, p, ny, nx, dy, dx, lambda, d, 0, OLG_NO_NORMALIZE, nullptr, 0, nullptr),
+                    "gFresnelProp");
+    });
+}
+
+// golprop.h:278-302
+template <typename COMPLEX_T, typename PREC_T>
+void gFresnelPropBandLimit(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx,
+                           PREC_T lambda, PREC_T d)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    olgb::check(olg_fresnel_prop_c64(u.get(), u.get(), ny, nx, dy, dx, lambda, d, 1, 0, nullptr, 0, nullptr),
+                "gFresnelPropBandLimit");
+    olgb::sync("gFresnelPropBandLimit");
+}
+
+// golprop.h:941-988
+template <typename PREC_T = float, typename COMPLEX_T>
+void ARSSFresnelProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &usrc,
+                     cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &udst, int ny, int nx, PREC_T dy, PREC_T dx,
+                     PREC_T lambda, PREC_T z, PREC_T s, PREC_T oy, PREC_T ox)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    if (!udst) udst = cuda::make_unique<thrust::complex<COMPLEX_T>[]>((size_t)ny * nx);
+    olgb::check(olg_arss_prop_c64(usrc.get(), udst.get(), ny, nx, dy, dx, lambda, z, s, oy, ox, 0, nullptr, 0, nullptr),
+                "ARSSFresnelProp");
+    olgb::sync("ARSSFresnelProp");
+}
+
+// golprop.h:990-995
+template <typename PREC_T = float, typename COMPLEX_T>
+void ARSSFresnelProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &usrc,
+                     cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &udst, int ny, int nx, PREC_T dy, PREC_T dx,
+                     PREC_T lambda, PREC_T z, PREC_T s)
+{
+    ARSSFresnelProp(usrc, udst, ny, nx, dy, dx, lambda, z, s, (PREC_T)0, (PREC_T)0);
+}
+
+// golprop.h:578-604 (prints the chosen method, as the reference does)
+template <typename COMPLEX_T, typename PREC_T>
+void Prop(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx, PREC_T lambda,
+          PREC_T d, PROPMODE propmode = PROPMODE::AUTO)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    const int mode = propmode == PROPMODE::ASM ? OLG_ASM : propmode == PROPMODE::FRESNEL ? OLG_FRESNEL : OLG_AUTO;
+    const int flags = OLG_VERBOSE | (std::is_same<PREC_T, float>::value ? OLG_CHECK_F32 : 0);
+    olgb::check(olg_prop_c64(u.get(), ny, nx, dy, dx, lambda, d, mode, flags, nullptr, nullptr, 0, nullptr), "Prop");
+    olgb::sync("Prop");
+}
+} // namespace ol
+#endif
