@@ -101,6 +101,22 @@ int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy,
                       double z, double s, double oy, double ox, int flags, void *work, size_t work_bytes,
                       olg_stream_t stream);
 
+/* Angular spectrum method that allocates nothing -- no counterpart in the
+ * reference.  Same computation and flags as olg_asm_prop_c64, but its scratch
+ * is a 17 MiB array compiled into the library, so it never calls cudaMalloc,
+ * cudaMallocAsync or any other allocator.  It is meant for callers that must
+ * not allocate device memory while they run: a holographic display loop with
+ * a fixed per-frame budget (an allocation can synchronise the device and miss
+ * a frame), or a plugin inside a host application that owns all GPU memory.
+ * Limit: ny * nx <= 1048576 (e.g. 1024 x 1024); larger fields return
+ * OLG_ERR_WORKSPACE.  The first call on each device looks up the array's
+ * device address and uploads the FFT twiddle table; make that first call
+ * before any stream capture.  All calls on a device share the one array:
+ * calls that overlap on the GPU (e.g. on two streams) race and corrupt each
+ * other's results, so serialise them. */
+int olg_asm_prop_noalloc_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                             double z, int flags, olg_stream_t stream);
+
 /* AUTO method selection, ol::AsmPropCheck (olprop.h:209-225) and
  * ol::FresnelPropCheck (olprop.h:109-123); single_precision != 0 evaluates
  * them in float like the reference's PREC_T=float instantiation.  1 = pass. */

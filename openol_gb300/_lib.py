@@ -31,6 +31,7 @@ SIGNATURES = {
     "olg_launch_count": (C.c_ulonglong, []),
     "olg_prop_workspace_bytes": (_sz, [_i, _i]),
     "olg_asm_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_asm_prop_noalloc_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _p]),
     "olg_fresnel_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _i, _p, _sz, _p]),
     "olg_arss_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _d, _i, _p, _sz, _p]),
     "olg_asm_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),

@@ -686,3 +686,53 @@ extern "C" int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, doubl
     if (pick == 0) return olg_asm_prop_c64(u, u, ny, nx, dy, dx, lambda, z, f, work, work_bytes, stream);
     return olg_fresnel_prop_c64(u, u, ny, nx, dy, dx, lambda, z, pick == 2 ? 1 : 0, f, work, work_bytes, stream);
 }
+
+// ------------------------------------------------------- no-allocation entry
+// Scratch for olg_asm_prop_noalloc_c64, owned by the library module itself:
+// 17 MiB per device, enough for any field with ny * nx <= 1,048,576
+// (1024 x 1024, 512 x 2048, ...).  Every device that loads the library keeps
+// this array until the process exits.
+namespace {
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)17 << 20;
+constexpr long NOALLOC_MAX_PIXELS = 1L << 20;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {};
+} // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch on the current device.  The name
+// g_noalloc_scratch in host code is only a host-side handle for the symbol,
+// so the address is looked up once per device (with that device current) and
+// cached; kernels receive this pointer like any caller-provided workspace.
+static int noalloc_scratch(void **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return fail(OLG_ERR_INVALID_ARG, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return OLG_OK;
+}
+
+extern "C" int olg_asm_prop_noalloc_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx,
+                                        double lambda, double z, int flags, olg_stream_t stream)
+{
+    if ((long)ny * (long)nx > NOALLOC_MAX_PIXELS || layout_bytes(ny, nx, nullptr, nullptr) > NOALLOC_SCRATCH_BYTES)
+        return fail(OLG_ERR_WORKSPACE, "olg_asm_prop_noalloc_c64: ny * nx must be <= 1048576 (its static scratch is "
+                                       "17 MiB); use olg_asm_prop_c64 with a workspace for larger fields");
+    if (int rc = validate(u_in, u_out, ny, nx)) return rc;
+    void *scratch = nullptr;
+    if (int rc = noalloc_scratch(&scratch)) return rc;
+    // Pass 1 writes every element of the scratch spectrum before passes 2 and 3
+    // read it, so the previous call's contents never leak into this one and
+    // nothing needs clearing.
+    return olg_asm_prop_c64(u_in, u_out, ny, nx, dy, dx, lambda, z, flags, scratch, NOALLOC_SCRATCH_BYTES, stream);
+}
