@@ -130,6 +130,23 @@ int olg_fresnel_prop_check(int ny, int nx, double dy, double dx, double lambda, 
 int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, double lambda, double z, int mode, int flags,
                  int *chosen, void *work, size_t work_bytes, olg_stream_t stream);
 
+/* -------------------------------------------------- phase optimisation */
+/* Multi-plane phase-only hologram optimisation (the reference has none; it
+ * builds on its ASM, golprop.h:507-534).  phi: ny x nx float (radians);
+ * targets: n_planes x ny x nx float intensities; z: n_planes host doubles.
+ * Loss L = sum_p mean((|ASM_{z_p}(e^{i phi})|^2 - t_p)^2).  The gradient is
+ * formed with the hand-written adjoint (conjugate transfer function), each
+ * plane's field recomputed rather than stored: 2 propagations per plane.
+ * loss (nullable) is a device double receiving L. */
+size_t olg_phase_opt_workspace_bytes(int ny, int nx);
+int olg_phase_loss_grad(const float *phi, const float *targets, const double *z, int n_planes, int ny, int nx,
+                        double dy, double dx, double lambda, float *grad, double *loss, void *work,
+                        size_t work_bytes, olg_stream_t stream);
+/* One Adam step (bias-corrected, step >= 1) on phi with state m, v. */
+int olg_phase_adam_step(float *phi, float *m, float *v, const float *targets, const double *z, int n_planes, int ny,
+                        int nx, double dy, double dx, double lambda, double lr, double beta1, double beta2, double eps,
+                        int step, double *loss, void *work, size_t work_bytes, olg_stream_t stream);
+
 /* ------------------------------------------------------------------- CGH */
 /* Points are AoS float32 triples (x, y, z) in metres, ol::Vect3<float>
  * (olclass.h:45-52) as held by ol::gObject (golclass.h:58-71).  Pixel (w, h)

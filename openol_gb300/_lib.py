@@ -37,6 +37,10 @@ SIGNATURES = {
     "olg_asm_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),
     "olg_fresnel_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),
     "olg_prop_c64": (_i, [_p, _i, _i, _d, _d, _d, _d, _i, _i, C.POINTER(_i), _p, _sz, _p]),
+    "olg_phase_opt_workspace_bytes": (_sz, [_i, _i]),
+    "olg_phase_loss_grad": (_i, [_p, _p, C.POINTER(_d), _i, _i, _i, _d, _d, _d, _p, _p, _p, _sz, _p]),
+    "olg_phase_adam_step": (_i, [_p, _p, _p, _p, C.POINTER(_d), _i, _i, _i, _d, _d, _d, _d, _d, _d, _d, _i, _p, _p,
+                                 _sz, _p]),
     "olg_cgh_fresnel_c64": (_i, [_p, _p, _p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p]),
     "olg_cgh_exact_c64": (_i, [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d, _i, _p]),
     "olg_cgh_gemm_workspace_bytes": (_sz, [_i, _i, _i]),

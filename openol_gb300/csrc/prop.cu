@@ -30,6 +30,7 @@
 
 #include "common.cuh"
 #include "fft.cuh"
+#include "fft2.cuh"
 
 namespace olg {
 
@@ -37,7 +38,7 @@ static __device__ float2 g_tw[FFT_MAX];
 
 enum : int { M_ASM = 0, M_CHIRP = 1 };
 // pre/post operation modes
-enum : int { OP_NONE = 0, OP_TABLE = 1, OP_TABLE_IN_WINDOW = 2 };
+enum : int { OP_NONE = 0, OP_TABLE = 1, OP_TABLE_IN_WINDOW = 2, OP_SEED = 3 };
 
 struct PropParams {
     int ny, nx, NY, NX;
@@ -60,6 +61,12 @@ struct PropParams {
     const float2 *in;
     float2 *out;
     float2 *S;
+    // phase-only input (pass 1 reads phi and forms exp(i phi)) when non-null
+    const float *in_phase;
+    // OP_SEED (pass 3): out = seed_scale (|v|^2 - target) v, loss += sum (|v|^2 - target)^2
+    const float *target;
+    float seed_scale;
+    double *loss;
 };
 
 // ---------------------------------------------------------------- launch shapes
@@ -110,9 +117,15 @@ __global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_fwd(PropParams P)
         const int h = r0 + q;
         float2 a = make_float2(0.f, 0.f), b = a;
         if (h < P.ny) {
-            const float4 v = __ldg(reinterpret_cast<const float4 *>(P.in + (size_t)h * nx + w2));
-            a = make_float2(v.x, v.y);
-            b = make_float2(v.z, v.w);
+            if (P.in_phase) {
+                const float2 ph = __ldg(reinterpret_cast<const float2 *>(P.in_phase + (size_t)h * nx + w2));
+                sincosf(ph.x, &a.y, &a.x);
+                sincosf(ph.y, &b.y, &b.x);
+            } else {
+                const float4 v = __ldg(reinterpret_cast<const float4 *>(P.in + (size_t)h * nx + w2));
+                a = make_float2(v.x, v.y);
+                b = make_float2(v.z, v.w);
+            }
             a = apply_op(a, P.pre_mode, P.prex, P.prey, h, w2, P.ny, nx, P.pre_hlim, P.pre_wlim);
             b = apply_op(b, P.pre_mode, P.prex, P.prey, h, w2 + 1, P.ny, nx, P.pre_hlim, P.pre_wlim);
         }
@@ -151,19 +164,39 @@ __global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_inv(PropParams P)
     __syncthreads();
     smem_fft<N, +1, Cfg::NT, false, Cfg::NSEQ>(sm, SS, g_tw, tid);
     const int nx = P.nx, off = N / 4, hx = nx / 2;
+    float lsum = 0.f;
     for (int e = tid; e < Cfg::NSEQ * hx; e += Cfg::NT) {
         const int q = e / hx, w2 = (e % hx) * 2;
         const int h = r0 + q;
         if (h >= P.ny) continue;
         float2 a = sm[q * SS + pidx(off + w2)], b = sm[q * SS + pidx(off + w2 + 1)];
-        a = apply_op(a, P.post_mode, P.postx, P.posty, h, w2, P.ny, nx, P.post_hlim, P.post_wlim);
-        b = apply_op(b, P.post_mode, P.postx, P.posty, h, w2 + 1, P.ny, nx, P.post_hlim, P.post_wlim);
+        if (P.post_mode == OP_SEED) {
+            const float2 t = __ldg(reinterpret_cast<const float2 *>(P.target + (size_t)h * nx + w2));
+            const float ra = a.x * a.x + a.y * a.y - t.x, rb = b.x * b.x + b.y * b.y - t.y;
+            lsum = fmaf(ra, ra, fmaf(rb, rb, lsum));
+            a = cscale(a, P.seed_scale * ra);
+            b = cscale(b, P.seed_scale * rb);
+        } else {
+            a = apply_op(a, P.post_mode, P.postx, P.posty, h, w2, P.ny, nx, P.post_hlim, P.post_wlim);
+            b = apply_op(b, P.post_mode, P.postx, P.posty, h, w2 + 1, P.ny, nx, P.post_hlim, P.post_wlim);
+        }
         float4 *dst = reinterpret_cast<float4 *>(P.out + (size_t)h * nx + w2);
         if (P.accumulate) {
             const float4 o = *dst;
             a.x += o.x; a.y += o.y; b.x += o.z; b.y += o.w;
         }
         *dst = make_float4(a.x, a.y, b.x, b.y);
+    }
+    if (P.post_mode == OP_SEED) {
+        __shared__ float red[32];
+        for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+        if ((tid & 31) == 0) red[tid >> 5] = lsum;
+        __syncthreads();
+        if (tid < 32) {
+            float v = tid < Cfg::NT / 32 ? red[tid] : 0.f;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (tid == 0) atomicAdd(P.loss, (double)v);
+        }
     }
 }
 
@@ -237,6 +270,223 @@ __global__ void __launch_bounds__(ColCfg<N>::NT) k_cols(PropParams P)
         const float2 a = sm[pidx(off + h) * C + c], b = sm[pidx(off + h) * C + c + 1];
         *reinterpret_cast<float4 *>(P.S + (size_t)h * NX + c0 + c) = make_float4(a.x, a.y, b.x, b.y);
     }
+}
+
+// =========================================================== v2 passes
+// N >= 256: register-resident first / last radix-16 stages (fft2.cuh).
+template <int N>
+struct Row2Cfg {
+    static constexpr int NT = N >= 8192 ? 512 : 256;
+    static constexpr int NSEQ = N >= 4096 ? 1 : 4096 / N;
+    static constexpr int SMEM = NSEQ * padded_len(N) * 8;
+};
+template <int N>
+struct Col2Cfg {
+    static constexpr int E = N >= 8192 ? 2 * N : 8192;
+    static constexpr int C = E / N;
+    static constexpr int NT = 512;
+    static constexpr int SMEM = padded_len(N) * C * 8;
+};
+
+__device__ __forceinline__ float2 load_in(const PropParams &P, int h, int w)
+{
+    float2 x;
+    if (P.in_phase) {
+        const float ph = __ldg(P.in_phase + (size_t)h * P.nx + w);
+        sincosf(ph, &x.y, &x.x);
+    } else {
+        x = __ldg(P.in + (size_t)h * P.nx + w);
+    }
+    return apply_op(x, P.pre_mode, P.prex, P.prey, h, w, P.ny, P.nx, P.pre_hlim, P.pre_wlim);
+}
+
+template <int N, int NT, int NSEQ>
+__device__ __forceinline__ void rows_fwd_body(const PropParams &P, int r0, float2 *sm, int tid)
+{
+    constexpr int SS = padded_len(N), B = N / 16;
+    static_assert((NSEQ * B) % NT == 0, "threads must divide the butterflies");
+    constexpr int BPT = NSEQ * B / NT;
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
+        float2 v[16];
+#pragma unroll
+        for (int r = 4; r < 12; ++r) v[r] = h < P.ny ? load_in(P, h, j + (r - 4) * B) : make_float2(0.f, 0.f);
+        dft16_in_mid<-1>(v);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+    }
+    __syncthreads();
+    mid_stages<N, -1, NT, false, NSEQ>(sm, SS, g_tw, tid);
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
+        float2 v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+        last_twiddle<N, -1>(v, j, g_tw);
+        dft<16, -1>(v);
+        if (h < P.ny) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) P.S[(size_t)h * N + j + k * B] = v[outpos<16>(k)];
+        }
+    }
+}
+
+template <int N, int NT, int NSEQ>
+__device__ __forceinline__ void rows_inv_body(const PropParams &P, int r0, float2 *sm, int tid, float &lsum)
+{
+    constexpr int SS = padded_len(N), B = N / 16;
+    constexpr int BPT = NSEQ * B / NT;
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
+        float2 v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r)
+            v[r] = h < P.ny ? P.S[(size_t)h * N + j + r * B] : make_float2(0.f, 0.f);
+        dft<16, +1>(v);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+    }
+    __syncthreads();
+    mid_stages<N, +1, NT, false, NSEQ>(sm, SS, g_tw, tid);
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
+        float2 v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+        last_twiddle<N, +1>(v, j, g_tw);
+        dft16_out_mid<+1>(v);
+        if (h >= P.ny) continue;
+#pragma unroll
+        for (int k = 4; k < 12; ++k) {
+            const int w = j + (k - 4) * B;
+            float2 a = v[outpos<16>(k)];
+            const size_t i = (size_t)h * P.nx + w;
+            if (P.post_mode == OP_SEED) {
+                const float r2 = a.x * a.x + a.y * a.y - __ldg(P.target + i);
+                lsum = fmaf(r2, r2, lsum);
+                a = cscale(a, P.seed_scale * r2);
+            } else {
+                a = apply_op(a, P.post_mode, P.postx, P.posty, h, w, P.ny, P.nx, P.post_hlim, P.post_wlim);
+            }
+            if (P.accumulate) {
+                const float2 o = P.out[i];
+                a.x += o.x;
+                a.y += o.y;
+            }
+            P.out[i] = a;
+        }
+    }
+}
+
+__device__ __forceinline__ float2 tf_at(const PropParams &P, int ky, int kx, int NY)
+{
+    if (P.method == M_ASM) {
+        const int fx = kx < P.NX / 2 ? kx : kx - P.NX;
+        const int fy = ky < NY / 2 ? ky : ky - NY;
+        return asm_tf(P, fx, fy);
+    }
+    float2 T = cmul(__ldg(P.Hx + kx), __ldg(P.Hy + ky));
+    return P.conj ? cconj(T) : T;
+}
+
+template <int N, int NT, int C>
+__device__ __forceinline__ void cols_body(const PropParams &P, int c0, float2 *sm, int tid)
+{
+    constexpr int B = N / 16;
+    static_assert((C * B) % NT == 0, "threads must divide the butterflies");
+    constexpr int BPT = C * B / NT;
+    const int NX = P.NX;
+    // forward first stage, straight from the ny stored rows (the rest is zero padding)
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, c = b % C, j = b / C, kx = c0 + c;
+        float2 v[16];
+#pragma unroll
+        for (int r = 4; r < 12; ++r)
+            v[r] = kx < NX ? P.S[(size_t)(j + (r - 4) * B) * NX + kx] : make_float2(0.f, 0.f);
+        dft16_in_mid<-1>(v);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = v[outpos<16>(k)];
+    }
+    __syncthreads();
+    mid_stages<N, -1, NT, true, C>(sm, 0, g_tw, tid);
+    // forward last stage -> x T(ky, kx) -> inverse first stage, in registers
+    float2 vv[BPT][16];
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, c = b % C, j = b / C;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) vv[t][r] = sm[pidx(j + r * B) * C + c];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, c = b % C, j = b / C, kx = c0 + c;
+        last_twiddle<N, -1>(vv[t], j, g_tw);
+        dft<16, -1>(vv[t]);
+        float2 w[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) w[k] = kx < NX ? cmul(vv[t][outpos<16>(k)], tf_at(P, j + k * B, kx, N)) : vv[t][outpos<16>(k)];
+        dft<16, +1>(w);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = w[outpos<16>(k)];
+    }
+    __syncthreads();
+    mid_stages<N, +1, NT, true, C>(sm, 0, g_tw, tid);
+    // inverse last stage: only the central ny rows, back in place
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, c = b % C, j = b / C, kx = c0 + c;
+        float2 v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j + r * B) * C + c];
+        last_twiddle<N, +1>(v, j, g_tw);
+        dft16_out_mid<+1>(v);
+        if (kx < NX) {
+#pragma unroll
+            for (int k = 4; k < 12; ++k) P.S[(size_t)(j + (k - 4) * B) * NX + kx] = v[outpos<16>(k)];
+        }
+    }
+}
+
+__device__ __forceinline__ void loss_reduce(float lsum, double *loss, int tid, int nt)
+{
+    __shared__ float red[32];
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((tid & 31) == 0) red[tid >> 5] = lsum;
+    __syncthreads();
+    if (tid < 32) {
+        float v = tid < nt / 32 ? red[tid] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (tid == 0) atomicAdd(loss, (double)v);
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(Row2Cfg<N>::NT) k_rows_fwd2(PropParams P)
+{
+    extern __shared__ float2 sm[];
+    rows_fwd_body<N, Row2Cfg<N>::NT, Row2Cfg<N>::NSEQ>(P, blockIdx.x * Row2Cfg<N>::NSEQ, sm, threadIdx.x);
+}
+
+template <int N>
+__global__ void __launch_bounds__(Row2Cfg<N>::NT) k_rows_inv2(PropParams P)
+{
+    extern __shared__ float2 sm[];
+    float lsum = 0.f;
+    rows_inv_body<N, Row2Cfg<N>::NT, Row2Cfg<N>::NSEQ>(P, blockIdx.x * Row2Cfg<N>::NSEQ, sm, threadIdx.x, lsum);
+    if (P.post_mode == OP_SEED) loss_reduce(lsum, P.loss, threadIdx.x, Row2Cfg<N>::NT);
+}
+
+template <int N>
+__global__ void __launch_bounds__(Col2Cfg<N>::NT) k_cols2(PropParams P)
+{
+    extern __shared__ float2 sm[];
+    cols_body<N, Col2Cfg<N>::NT, Col2Cfg<N>::C>(P, blockIdx.x * Col2Cfg<N>::C, sm, threadIdx.x);
 }
 
 // ------------------------------------------------------------- chirp tables
@@ -345,6 +595,19 @@ int prep_smem(K kern, int bytes)
 template <int N>
 int launch_rows(const PropParams &P, bool inverse, cudaStream_t st)
 {
+    if constexpr (N >= 256) {
+        using C2 = Row2Cfg<N>;
+        const int grid = (P.ny + C2::NSEQ - 1) / C2::NSEQ;
+        if (!inverse) {
+            if (int rc = prep_smem(k_rows_fwd2<N>, C2::SMEM)) return rc;
+            k_rows_fwd2<N><<<grid, C2::NT, C2::SMEM, st>>>(P);
+        } else {
+            if (int rc = prep_smem(k_rows_inv2<N>, C2::SMEM)) return rc;
+            k_rows_inv2<N><<<grid, C2::NT, C2::SMEM, st>>>(P);
+        }
+        count_launch();
+        return check_launch(inverse ? "k_rows_inv2" : "k_rows_fwd2");
+    }
     using C = RowCfg<N>;
     const int grid = (P.ny + C::NSEQ - 1) / C::NSEQ;
     if (!inverse) {
@@ -361,6 +624,14 @@ int launch_rows(const PropParams &P, bool inverse, cudaStream_t st)
 template <int N>
 int launch_cols(const PropParams &P, cudaStream_t st)
 {
+    if constexpr (N >= 256) {
+        using C2 = Col2Cfg<N>;
+        const int grid = (P.NX + C2::C - 1) / C2::C;
+        if (int rc = prep_smem(k_cols2<N>, C2::SMEM)) return rc;
+        k_cols2<N><<<grid, C2::NT, C2::SMEM, st>>>(P);
+        count_launch();
+        return check_launch("k_cols2");
+    }
     using C = ColCfg<N>;
     const int grid = (P.NX + C::C - 1) / C::C;
     if (int rc = prep_smem(k_cols<N>, C::SMEM)) return rc;
@@ -685,6 +956,172 @@ extern "C" int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, doubl
     }
     if (pick == 0) return olg_asm_prop_c64(u, u, ny, nx, dy, dx, lambda, z, f, work, work_bytes, stream);
     return olg_fresnel_prop_c64(u, u, ny, nx, dy, dx, lambda, z, pick == 2 ? 1 : 0, f, work, work_bytes, stream);
+}
+
+// ------------------------------------------- multi-plane phase optimisation
+// Phase-only hologram phi (ny x nx) propagated by ASM to P depth planes;
+// loss L = sum_p mean((|A_p e^{i phi}|^2 - t_p)^2).  Per plane: one forward
+// propagation whose pass 1 forms e^{i phi} from phi and whose pass 3 writes
+// the seed dL/dv* = (2/n)(|v|^2 - t) v (and sums the loss), then one adjoint
+// propagation (conjugate transfer function) of the seed accumulated into
+// g = dL/du*.  No plane's field is stored.  dL/dphi = -2 Im(u conj(g)).
+namespace olg {
+
+__global__ void k_phase_grad(const float *phi, const float2 *g, float *grad, long n)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        float s, c;
+        sincosf(phi[i], &s, &c);
+        const float2 G = g[i];
+        grad[i] = 2.0f * (c * G.y - s * G.x);
+    }
+}
+
+__global__ void k_adam(float *phi, float *m, float *v, const float2 *g, long n, float lr, float b1, float b2, float eps,
+                       float bc1, float bc2)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const float ph = phi[i];
+        float s, c;
+        sincosf(ph, &s, &c);
+        const float2 G = g[i];
+        const float gr = 2.0f * (c * G.y - s * G.x);
+        const float mm = b1 * m[i] + (1.0f - b1) * gr;
+        const float vv = b2 * v[i] + (1.0f - b2) * gr * gr;
+        m[i] = mm;
+        v[i] = vv;
+        phi[i] = ph - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+    }
+}
+
+__global__ void k_loss_scale(double *loss, double s) { *loss *= s; }
+
+int elem_grid(long n)
+{
+    long g = (n + 255) / 256;
+    return (int)(g > 152 * 8 ? 152 * 8 : (g < 1 ? 1 : g));
+}
+
+PropParams asm_params(const void *in, void *out, int ny, int nx, double dy, double dx, double lambda, double z, bool conj,
+                      const Layout &L)
+{
+    PropParams P = base_params(in, out, ny, nx, L);
+    const double NX = 2.0 * nx, NY = 2.0 * ny;
+    const double du = 1.0 / (dx * NX), dv = 1.0 / (dy * NY);
+    const double zl = z / lambda;
+    P.method = M_ASM;
+    P.conj = conj ? 1 : 0;
+    P.scale = (float)(1.0 / (NX * NY));
+    P.c0 = frac_host(zl);
+    set_quad(P.ax_hi, P.ax_lo, z * lambda * du * du / 2.0);
+    set_quad(P.ay_hi, P.ay_lo, z * lambda * dv * dv / 2.0);
+    P.tx = (float)(lambda * lambda * du * du);
+    P.ty = (float)(lambda * lambda * dv * dv);
+    P.zl = (float)zl;
+    return P;
+}
+
+size_t phase_ws(int ny, int nx, size_t *off_seed, size_t *off_g, size_t *off_loss)
+{
+    const size_t lb = layout_bytes(ny, nx, nullptr, nullptr);
+    const size_t f = align_up((size_t)ny * nx * sizeof(float2), 256);
+    if (off_seed) *off_seed = lb;
+    if (off_g) *off_g = lb + f;
+    if (off_loss) *off_loss = lb + 2 * f;
+    return lb + 2 * f + 256;
+}
+
+int phase_loss_grad(const float *phi, const float *targets, const double *z, int np, int ny, int nx, double dy,
+                    double dx, double lambda, char *ws, float2 *g, double *loss, cudaStream_t st)
+{
+    size_t os, og, ol;
+    phase_ws(ny, nx, &os, &og, &ol);
+    Layout L;
+    layout_bytes(ny, nx, &L, ws);
+    float2 *seed = (float2 *)(ws + os);
+    const long n = (long)ny * nx;
+    cudaError_t e = cudaMemsetAsync(loss, 0, sizeof(double), st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(loss)");
+    for (int p = 0; p < np; ++p) {
+        PropParams F = asm_params(nullptr, seed, ny, nx, dy, dx, lambda, z[p], false, L);
+        F.in_phase = phi;
+        F.post_mode = OP_SEED;
+        F.target = targets + (size_t)p * n;
+        F.seed_scale = (float)(2.0 / (double)n);
+        F.loss = loss;
+        if (int rc = run_passes(F, st)) return rc;
+        PropParams B = asm_params(seed, g, ny, nx, dy, dx, lambda, z[p], true, L);
+        B.accumulate = p > 0 ? 1 : 0;
+        if (int rc = run_passes(B, st)) return rc;
+    }
+    k_loss_scale<<<1, 1, 0, st>>>(loss, 1.0 / (double)n);
+    count_launch();
+    return check_launch("k_loss_scale");
+}
+
+int phase_checks(const void *phi, const void *targets, const double *z, int np, int ny, int nx)
+{
+    if (!phi || !targets || !z || np <= 0) return fail(OLG_ERR_INVALID_ARG, "null pointer or no planes");
+    if (((uintptr_t)phi & 7) || ((uintptr_t)targets & 7)) return fail(OLG_ERR_INVALID_ARG, "phi / targets must be 8-byte aligned");
+    if (!is_pow2(nx) || !is_pow2(ny) || nx < 16 || ny < 16 || 2 * nx > FFT_MAX || 2 * ny > FFT_MAX)
+        return fail(OLG_ERR_UNSUPPORTED_SIZE, "ny, nx must be powers of two in [16, 4096]");
+    return OLG_OK;
+}
+
+} // namespace olg
+
+extern "C" size_t olg_phase_opt_workspace_bytes(int ny, int nx)
+{
+    if (ny <= 0 || nx <= 0) return 0;
+    return phase_ws(ny, nx, nullptr, nullptr, nullptr);
+}
+
+extern "C" int olg_phase_loss_grad(const float *phi, const float *targets, const double *z, int n_planes, int ny,
+                                   int nx, double dy, double dx, double lambda, float *grad, double *loss,
+                                   void *work, size_t work_bytes, olg_stream_t stream)
+{
+    if (int rc = phase_checks(phi, targets, z, n_planes, ny, nx)) return rc;
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, phase_ws(ny, nx, nullptr, nullptr, nullptr), st)) return rc;
+    size_t os, og, ol;
+    phase_ws(ny, nx, &os, &og, &ol);
+    char *ws = (char *)sc.ptr;
+    float2 *g = (float2 *)(ws + og);
+    double *dl = loss ? loss : (double *)(ws + ol);
+    if (int rc = phase_loss_grad(phi, targets, z, n_planes, ny, nx, dy, dx, lambda, ws, g, dl, st)) return rc;
+    if (grad) {
+        const long n = (long)ny * nx;
+        k_phase_grad<<<elem_grid(n), 256, 0, st>>>(phi, g, grad, n);
+        count_launch();
+        return check_launch("k_phase_grad");
+    }
+    return OLG_OK;
+}
+
+extern "C" int olg_phase_adam_step(float *phi, float *m, float *v, const float *targets, const double *z, int n_planes,
+                                   int ny, int nx, double dy, double dx, double lambda, double lr, double beta1,
+                                   double beta2, double eps, int step, double *loss, void *work, size_t work_bytes,
+                                   olg_stream_t stream)
+{
+    if (int rc = phase_checks(phi, targets, z, n_planes, ny, nx)) return rc;
+    if (!m || !v || step < 1) return fail(OLG_ERR_INVALID_ARG, "Adam state missing or step < 1");
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, phase_ws(ny, nx, nullptr, nullptr, nullptr), st)) return rc;
+    size_t os, og, ol;
+    phase_ws(ny, nx, &os, &og, &ol);
+    char *ws = (char *)sc.ptr;
+    float2 *g = (float2 *)(ws + og);
+    double *dl = loss ? loss : (double *)(ws + ol);
+    if (int rc = phase_loss_grad(phi, targets, z, n_planes, ny, nx, dy, dx, lambda, ws, g, dl, st)) return rc;
+    const long n = (long)ny * nx;
+    const float bc1 = (float)(1.0 - std::pow(beta1, step)), bc2 = (float)(1.0 - std::pow(beta2, step));
+    k_adam<<<elem_grid(n), 256, 0, st>>>(phi, m, v, g, n, (float)lr, (float)beta1, (float)beta2, (float)eps, bc1, bc2);
+    count_launch();
+    return check_launch("k_adam");
 }
 
 // ------------------------------------------------------- no-allocation entry

@@ -234,3 +234,29 @@ def binarize(u):
     img = np.zeros(u.shape, np.uint8)
     cpu().olc_binarize(_ptr(u), _ptr(img), u.shape[0], u.shape[1])
     return img
+
+
+# ------------------------------------------------------ phase optimisation
+def phase_loss_grad(phi, targets, zs, p, lam):
+    """FP64 loss sum_p mean((|ASM_z(e^{i phi})|^2 - t_p)^2) and dL/dphi, by the
+    adjoint (conj transfer function) of the FP64 ASM restatement."""
+    u = np.exp(1j * np.asarray(phi, np.float64))
+    n = u.size
+    L = 0.0
+    g = np.zeros_like(u)
+    for t, z in zip(targets, zs):
+        v = asm_prop(u, p, p, lam, z)
+        r = np.abs(v) ** 2 - np.asarray(t, np.float64)
+        L += float(np.mean(r * r))
+        g += asm_prop(2.0 * r * v / n, p, p, lam, z, flags=1)
+    return L, -2.0 * np.imag(u * np.conj(g))
+
+
+def phase_loss(phi, targets, zs, p, lam):
+    u = np.exp(1j * np.asarray(phi, np.float64))
+    L = 0.0
+    for t, z in zip(targets, zs):
+        v = asm_prop(u, p, p, lam, z)
+        r = np.abs(v) ** 2 - np.asarray(t, np.float64)
+        L += float(np.mean(r * r))
+    return L
