@@ -6,7 +6,10 @@ Default workload (N = 1): point-cloud CGH on a 1920 x 1080 hologram, pitch
 (W/2 p, H/2 p, 100 mm), amplitudes U[0.5, 1], phases U[0, 2 pi) -- metric
 point.pixel/s (one step = one hologram = 2.07e10 point.pixels).  Other
 workloads: ``--workload asm`` (1024^2 field padded to 2048^2, p = 8 um,
-532 nm, z = 50 mm; props/s).
+532 nm, z = 50 mm; props/s), ``--workload wrp`` (200,000 points 1-5 mm behind
+a 4096^2 WRP, p = 4 um, then ASM by 150 mm and the binarised 8-bit hologram;
+holograms/s), ``--workload adam`` (2048^2 phase, 8 planes at 80..150 mm,
+p = 6.4 um; one Adam step with the adjoint gradient; grad-steps/s).
 
 Our arm prints one JSON line with value (device-resident inputs, CUDA events
 on the launching stream, L2 flushed between steps), e2e (host buffers, copies
@@ -35,8 +38,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+WRP_DESC = "wrp 200000 points 1-5mm behind a 4096x4096 WRP, p=4um, lambda=532nm, ASM 150mm, binarised 8-bit"
+ADAM_DESC = "adam 2048x2048 phase, 8 planes z=80..150mm, p=6.4um, lambda=532nm, 5% sparse targets"
 CGH = dict(ny=1080, nx=1920, p=8e-6, lam=532e-9, n=10000, zc=0.1, box=5e-3, seed=20261203 + 2)
 ASM = dict(n=1024, p=8e-6, lam=532e-9, z=0.05, seed=20261203 + 1)
+WRP = dict(N=4096, p=4e-6, lam=532e-9, n=200000, zw=0.15, ext=10e-3, seed=20261203 + 3)
+ADAM = dict(n=2048, p=6.4e-6, lam=532e-9, planes=8, z0=0.08, dz=0.01, lr=0.05, seed=20261203 + 4)
 
 
 def peaks():
@@ -147,6 +154,50 @@ def cpu_asm_sample():
     return 1.0 / (time.perf_counter() - t0)
 
 
+def wrp_points():
+    c = WRP
+    rng = np.random.default_rng(c["seed"])
+    ctr = c["N"] * c["p"] / 2
+    x = ctr + (rng.random(c["n"]) - 0.5) * c["ext"]
+    y = ctr + (rng.random(c["n"]) - 0.5) * c["ext"]
+    z = c["zw"] + 1e-3 + rng.random(c["n"]) * 4e-3
+    return np.stack([x, y, z], 1).astype(np.float32)
+
+
+def adam_problem():
+    from openol_gb300.optim import make_targets
+    c = ADAM
+    rng = np.random.default_rng(c["seed"])
+    phi = (2 * np.pi * rng.random((c["n"], c["n"]))).astype(np.float32)
+    t = make_targets(c["n"], c["n"], c["planes"], seed=c["seed"] + 1)
+    zs = [c["z0"] + c["dz"] * k for k in range(c["planes"])]
+    return phi, t, zs
+
+
+def cpu_wrp_sample(frac=0.01):
+    """FP64 oracle WRP step 1 on a seeded 1% subset of the points + the 4096^2 ASM (FP64), scaled."""
+    import oracle as O
+    c = WRP
+    pts = wrp_points()
+    sub = pts[: int(len(pts) * frac)]
+    t0 = time.perf_counter()
+    U = O.wrp_step1(sub, c["N"], c["N"], np.float32(c["p"]), np.float32(c["lam"]), np.float32(c["zw"]))
+    t1 = time.perf_counter()
+    O.asm_prop(U, c["p"], c["p"], c["lam"], c["zw"])
+    t2 = time.perf_counter()
+    return 1.0 / ((t1 - t0) / frac + (t2 - t1)), (t1 - t0, t2 - t1)
+
+
+def cpu_adam_sample():
+    """FP64 oracle loss+gradient for one of the 8 planes at 2048^2 (2 propagations), scaled x8."""
+    import oracle as O
+    phi, t, zs = adam_problem()
+    t0 = time.perf_counter()
+    O.phase_loss_grad(phi, t[:1], zs[:1], ADAM["p"], ADAM["lam"])
+    dt = time.perf_counter() - t0
+    return 1.0 / (dt * ADAM["planes"]), dt
+
+
 def cpu_threads():
     return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
 
@@ -167,7 +218,7 @@ def run_reference(args):
         metric, unit = "CGH point.pixel/s", "point.pixel/s"
         sample = f"{rows} of {CGH['ny']} rows x {CGH['nx']} px x {CGH['n']} points per step (FP64 Fresnel-form sum)"
         config = {"workload": "cgh 1920x1080, 10000 points, p=8um, lambda=532nm, 5mm box at z=100mm"}
-    else:
+    elif wl == "asm":
         for k in range(args.warmup + args.steps):
             v = cpu_asm_sample()
             if k >= args.warmup:
@@ -175,6 +226,22 @@ def run_reference(args):
         metric, unit = "ASM props/s", "props/s"
         sample = "one full 1024^2 -> 2048^2 FP64 ASM propagation per step"
         config = {"workload": "asm 1024x1024 padded 2048x2048, p=8um, lambda=532nm, z=50mm"}
+    elif wl == "wrp":
+        for k in range(1 + min(args.steps, 2)):
+            v, _ = cpu_wrp_sample()
+            if k >= 1:
+                vals.append(v)
+        metric, unit = "WRP holograms/s", "holograms/s"
+        sample = "WRP step 1 on a seeded 1% point subset (scaled x100) + full 4096^2 FP64 ASM, per step"
+        config = {"workload": WRP_DESC}
+    else:
+        for k in range(1 + min(args.steps, 3)):
+            v, _ = cpu_adam_sample()
+            if k >= 1:
+                vals.append(v)
+        metric, unit = "grad-steps/s", "grad-steps/s"
+        sample = "loss + adjoint gradient for 1 of 8 planes at 2048^2 per step (scaled x8), FP64"
+        config = {"workload": ADAM_DESC}
     v = statistics.median(vals)
     line = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
@@ -259,8 +326,13 @@ def run_ours(args):
             og.cgh_fresnel_gemm(obj, U, ny=c["ny"], nx=c["nx"], py=c["p"], px=c["p"], lam=c["lam"], amp=a,
                                 phase0=f, work=gws, reuse_operands=True)
 
+        from openol_gb300.plain import plain_cgh_fresnel
+
+        def step_plain():
+            plain_cgh_fresnel(obj, U, ny=c["ny"], nx=c["nx"], p=c["p"], lam=c["lam"])
+
         forms = {"fresnel_gemm": step_gemm, "fresnel_gemm_kernel_only": step_gemm_only,
-                 "fresnel_direct": step_fresnel, "exact": step_exact}
+                 "fresnel_direct": step_fresnel, "exact": step_exact, "plain_simt": step_plain}
         chosen = "fresnel_gemm"
         res = {}
         with ClockSampler(local) as clk:
@@ -325,7 +397,7 @@ def run_ours(args):
             out["cpu_baseline"] = {"value": v, "unit": "point.pixel/s", "cores": cpu_threads(), "kind": "port",
                                    "sample": f"{args.cpu_rows} of 1080 rows x 1920 px x 10000 points, FP64 oracle, "
                                              f"{dt:.1f} s"}
-    else:
+    elif args.workload == "asm":
         n = ASM["n"]
         u0 = asm_input()
         src = torch.from_numpy(u0).cuda()
@@ -335,10 +407,16 @@ def run_ours(args):
         def step():
             og.asm_prop(src, dst, dy=ASM["p"], dx=ASM["p"], lam=ASM["lam"], z=ASM["z"], work=ws_buf)
 
+        from openol_gb300.plain import plain_asm_prop
+
+        def step_plain():
+            plain_asm_prop(src, dst, dy=ASM["p"], dx=ASM["p"], lam=ASM["lam"], z=ASM["z"])
+
         with ClockSampler(local) as clk:
             l0 = og.launch_count()
             ms = timed(torch, step, K, W, flush, stream, barrier)
             launches = (og.launch_count() - l0) // (K + W) * K
+            ms_plain = timed(torch, step_plain, K, W, flush, stream, barrier)
         clocks = clk.summary()
         t_step = max_over_ranks(statistics.mean(ms))
         hsrc = torch.from_numpy(u0).pin_memory()
@@ -365,11 +443,154 @@ def run_ours(args):
                          "frac": ach / pk["hbm_gbs"], "traffic": None,
                          "note": f"80 n bytes per propagation (n = 1024^2) over the 3-pass propagation time; "
                                  f"peak {pk_kind}"},
+            "forms": {"fused": {"props/s": 1e3 / statistics.mean(ms), "ms": statistics.mean(ms)},
+                      "plain_cufft": {"props/s": 1e3 / statistics.mean(ms_plain), "ms": statistics.mean(ms_plain)}},
             "clocks": clocks,
         }
         if rank == 0 and ws == 1 and not args.no_cpu:
             out["cpu_baseline"] = {"value": cpu_asm_sample(), "unit": "props/s", "cores": cpu_threads(),
                                    "kind": "port", "sample": "one full 1024^2 FP64 ASM propagation"}
+
+    elif args.workload == "wrp":
+        c = WRP
+        N = c["N"]
+        pts = wrp_points()
+        obj = og.gObject(pts)
+        U = torch.zeros((N, N), dtype=torch.complex64, device="cuda")
+        img = torch.empty((N, N), dtype=torch.uint8, device="cuda")
+        pws = og.workspace(N, N)
+        p, lam, zw = np.float32(c["p"]), np.float32(c["lam"]), np.float32(c["zw"])
+
+        def step1():
+            og.WRPStep1(obj, U, N, N, p, lam, zw)
+
+        def step2():
+            og.asm_prop(U, dy=float(p), dx=float(p), lam=float(lam), z=float(zw), work=pws)
+
+        def step():
+            step1()
+            step2()
+            og.binarize(U, N, N, img)
+
+        with ClockSampler(local) as clk:
+            l0 = og.launch_count()
+            ms = timed(torch, step, K, W, flush, stream, barrier)
+            launches = (og.launch_count() - l0) // (K + W) * K
+            ms1 = timed(torch, step1, K, W, flush, stream, barrier)
+            ms2 = timed(torch, step2, K, W, flush, stream, barrier)
+        clocks = clk.summary()
+        t_step = max_over_ranks(statistics.mean(ms))
+        hp = torch.from_numpy(pts).pin_memory()
+        himg = torch.empty((N, N), dtype=torch.uint8).pin_memory()
+
+        def step_e2e():
+            obj.points.copy_(hp, non_blocking=True)
+            step()
+            himg.copy_(img, non_blocking=True)
+
+        ms_e = timed(torch, step_e2e, K, W, flush, stream, barrier)
+        t_e2e = max_over_ranks(statistics.mean(ms_e))
+        # useful window terms sum_j pi W_j^2 / p^2 (W_j as the reference computes it)
+        dz = pts[:, 2].astype(np.float64) - float(zw)
+        Wj = np.abs(dz) / np.sqrt(4 * (float(p) / float(lam)) ** 2 - 1)
+        terms = float(np.sum(np.pi * Wj ** 2) / float(p) ** 2)
+        b_alg = 80 * N * N
+        ach = b_alg / (statistics.mean(ms2) * 1e-3) / 1e9
+        out = {
+            "metric": "WRP holograms/s", "value": ws / (t_step * 1e-3), "unit": "holograms/s", "ms_per_step": t_step,
+            "dtype": "f32 (double-float phase anchor)",
+            "config": {"workload": WRP_DESC, "l2": "flushed between steps (256 MiB write)"},
+            "e2e": {"value": ws / (t_e2e * 1e-3), "unit": "holograms/s", "h2d_bytes_per_step": pts.nbytes,
+                    "d2h_bytes_per_step": N * N},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": ach / pk["hbm_gbs"], "traffic": None,
+                         "note": f"step 2 (4096^2 -> 8192^2 ASM, {statistics.mean(ms2):.3f} ms): 80 n bytes; "
+                                 f"peak {pk_kind}"},
+            "forms": {"step1_ms": statistics.mean(ms1), "step2_ms": statistics.mean(ms2),
+                      "step1_window_terms": terms,
+                      "step1_terms_per_s": terms / (statistics.mean(ms1) * 1e-3),
+                      "window_radius_px": [float(Wj.min() / float(p)), float(Wj.max() / float(p))]},
+            "clocks": clocks,
+        }
+        if rank == 0 and ws == 1 and not args.no_cpu:
+            v, (t1, t2) = cpu_wrp_sample()
+            out["cpu_baseline"] = {"value": v, "unit": "holograms/s", "cores": cpu_threads(), "kind": "port",
+                                   "sample": f"FP64 WRP step 1 on 1% of the points ({t1:.1f} s, scaled x100) + "
+                                             f"full FP64 4096^2 ASM ({t2:.1f} s)"}
+    elif args.workload == "adam":
+        c = ADAM
+        n = c["n"]
+        phi0, t, zs = adam_problem()
+        phi = torch.from_numpy(phi0.copy()).cuda()
+        tt = torch.from_numpy(t).cuda()
+        opt = og.PhaseOptimizer(phi, tt, zs, dy=c["p"], dx=c["p"], lam=c["lam"], lr=c["lr"])
+
+        def step():
+            opt.step()
+
+        # plain form: autograd through torch.fft (cuFFT) + torch.optim.Adam
+        import math
+        pphi = torch.from_numpy(phi0.copy()).cuda().requires_grad_(True)
+        popt = torch.optim.Adam([pphi], lr=c["lr"])
+        N2 = 2 * n
+        fx = torch.fft.fftfreq(N2, d=c["p"], device="cuda", dtype=torch.float64)
+        FY, FX = torch.meshgrid(fx, fx, indexing="ij")
+        Hs = [torch.exp(1j * (2 * math.pi * z * torch.sqrt(1 / c["lam"] ** 2 - FX ** 2 - FY ** 2)))
+              .to(torch.complex64) / (N2 * N2) for z in zs]
+
+        def step_plain():
+            popt.zero_grad(set_to_none=True)
+            u = torch.polar(torch.ones_like(pphi), pphi)
+            up = torch.nn.functional.pad(u, (n // 2, n // 2, n // 2, n // 2))
+            F = torch.fft.fft2(up)
+            loss = 0
+            for k, H in enumerate(Hs):
+                v = torch.fft.ifft2(F * H, norm="forward")[n // 2: n // 2 + n, n // 2: n // 2 + n]
+                loss = loss + torch.mean((v.real ** 2 + v.imag ** 2 - tt[k]) ** 2)
+            loss.backward()
+            popt.step()
+
+        with ClockSampler(local) as clk:
+            l0 = og.launch_count()
+            ms = timed(torch, step, K, W, flush, stream, barrier)
+            launches = (og.launch_count() - l0) // (K + W) * K
+            ms_plain = timed(torch, step_plain, K, W, flush, stream, barrier)
+        clocks = clk.summary()
+        t_step = max_over_ranks(statistics.mean(ms))
+        hphi = torch.from_numpy(phi0.copy()).pin_memory()
+        hout = torch.empty_like(hphi).pin_memory()
+
+        def step_e2e():
+            opt.phi.copy_(hphi, non_blocking=True)
+            opt.step()
+            hout.copy_(opt.phi, non_blocking=True)
+
+        ms_e = timed(torch, step_e2e, K, W, flush, stream, barrier)
+        t_e2e = max_over_ranks(statistics.mean(ms_e))
+        b_alg = 1316 * n * n
+        ach = b_alg / (statistics.mean(ms) * 1e-3) / 1e9
+        out = {
+            "metric": "grad-steps/s", "value": ws / (t_step * 1e-3), "unit": "grad-steps/s", "ms_per_step": t_step,
+            "dtype": "f32",
+            "config": {"workload": ADAM_DESC, "lr": c["lr"], "l2": "flushed between steps (256 MiB write)"},
+            "e2e": {"value": ws / (t_e2e * 1e-3), "unit": "grad-steps/s", "h2d_bytes_per_step": phi0.nbytes,
+                    "d2h_bytes_per_step": phi0.nbytes},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": ach / pk["hbm_gbs"], "traffic": None,
+                         "note": f"1316 n bytes per step (16 propagations x 80 n + elementwise), n = 2048^2; "
+                                 f"peak {pk_kind}"},
+            "forms": {"fused_adjoint": {"grad-steps/s": 1e3 / statistics.mean(ms), "ms": statistics.mean(ms)},
+                      "plain_torch_autograd_cufft": {"grad-steps/s": 1e3 / statistics.mean(ms_plain),
+                                                      "ms": statistics.mean(ms_plain)},
+                      "loss_after_steps": float(opt.loss.item())},
+            "clocks": clocks,
+        }
+        if rank == 0 and ws == 1 and not args.no_cpu:
+            v, dt = cpu_adam_sample()
+            out["cpu_baseline"] = {"value": v, "unit": "grad-steps/s", "cores": cpu_threads(), "kind": "port",
+                                   "sample": f"FP64 loss + adjoint gradient of 1 of 8 planes ({dt:.1f} s), scaled x8"}
 
     if rank == 0:
         line = {"metric": out["metric"], "value": out["value"], "unit": out["unit"], "n_gpus": ws, "steps": K,
@@ -390,7 +611,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cgh", choices=["cgh", "asm"])
+    ap.add_argument("--workload", default="cgh", choices=["cgh", "asm", "wrp", "adam"])
     ap.add_argument("--cpu-rows", type=int, default=48)
     ap.add_argument("--ref-rows", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")

@@ -1,0 +1,28 @@
+/*
+ * olgb300_plain.h -- "plain form" GPU baselines exported by libolgb300.so for
+ * measurement only: the reference's own GPU structure re-expressed on this
+ * GPU, so that the fused kernels can be timed against it on the same device.
+ */
+#ifndef OLGB300_PLAIN_H
+#define OLGB300_PLAIN_H
+#include "olgb300.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ASM the way golprop.h:507-534 chains it: pad kernel, cuFFT forward, 1/Np,
+ * FP32 transfer function (golprop.h:307-322), fftshift, multiply, cuFFT
+ * inverse, crop.  cuFFT plan and padded buffers are cached per size. */
+int olg_plain_asm_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                           double z, olg_stream_t stream);
+
+/* Fresnel-form CGH the way gCghShared (golcgh.h:47-88) computes it: one
+ * thread per pixel, points staged in shared memory, FP32 phase with
+ * full-precision sin/cos.  Unit amplitudes. */
+int olg_plain_cgh_fresnel_c64(const float *points, int n_points, void *U, int ny, int nx, double p, double lambda,
+                              olg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -12,11 +12,11 @@ from conftest import ROOT
 from openol_gb300 import _lib
 from openol_gb300 import build as B
 
-HEADER = os.path.join(ROOT, "include", "olgb300.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("olgb300.h", "olgb300_plain.h")]
 
 
 def declared_symbols():
-    txt = open(HEADER).read()
+    txt = "".join(open(h).read() for h in HEADERS)
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     return sorted(set(re.findall(r"\b(olg_\w+)\s*\(", txt)))
 

@@ -104,3 +104,17 @@ def test_single_point_is_analytic_chirp():
     X, Y = np.meshgrid(w * p - np.float64(np.float32(16 * p)), w * p - np.float64(np.float32(16 * p)))
     ref = np.exp(1j * np.pi * (X ** 2 + Y ** 2) / (lam * np.float64(np.float32(z))))
     assert rel_l2(host(U), ref) < TOL
+
+
+def test_plain_forms_run_and_are_close():
+    """The plain (reference-structured) baselines: same sums, FP32 phase error."""
+    from openol_gb300.plain import plain_asm_prop, plain_cgh_fresnel
+    rng = np.random.default_rng(1)
+    u0 = ((rng.random((128, 128)) < 0.5) * np.exp(2j * np.pi * rng.random((128, 128)))).astype(np.complex64)
+    src = torch.from_numpy(u0).cuda()
+    out = plain_asm_prop(src, torch.empty_like(src), dy=8e-6, dx=8e-6, lam=532e-9, z=0.05)
+    assert rel_l2(host(out), O.asm_prop(u0.astype(np.complex128), 8e-6, 8e-6, 532e-9, 0.05)) < 0.1
+    pts = np.stack([rng.random(200) * 64 * 8e-6, rng.random(200) * 48 * 8e-6, 0.05 + rng.random(200) * 0.01], 1)
+    U = torch.zeros((48, 64), dtype=torch.complex64, device="cuda")
+    plain_cgh_fresnel(og.gObject(pts), U, ny=48, nx=64, p=8e-6, lam=532e-9)
+    assert rel_l2(host(U), O.cgh_fresnel(pts.astype(np.float32).astype(np.float64), 48, 64, 8e-6, 8e-6, 532e-9)) < 1e-2
