@@ -592,6 +592,69 @@ def run_ours(args):
             out["cpu_baseline"] = {"value": v, "unit": "grad-steps/s", "cores": cpu_threads(), "kind": "port",
                                    "sample": f"FP64 loss + adjoint gradient of 1 of 8 planes ({dt:.1f} s), scaled x8"}
 
+    elif args.workload == "batch":
+        fields = og.config5_fields()
+        plan = og.BatchPlan(fields)
+        nprop = len(fields)
+        b_alg = sum(80 * f["u_in"].numel() for f in fields)
+        gs = torch.cuda.Stream()
+        graph = torch.cuda.CUDAGraph()
+        plan.execute()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(gs):
+            with torch.cuda.graph(graph, stream=gs):
+                plan.execute(stream=gs)
+        torch.cuda.synchronize()
+
+        def step():
+            graph.replay()
+
+        def step_serial():
+            plan.execute_serial()
+
+        with ClockSampler(local) as clk:
+            l0 = og.launch_count()
+            ms_direct = timed(torch, plan.execute, K, W, flush, stream, barrier)
+            launches = (og.launch_count() - l0) // (K + W) * K
+            ms = timed(torch, step, K, W, flush, stream, barrier)
+            ms_serial = timed(torch, step_serial, K, W, flush, stream, barrier)
+        clocks = clk.summary()
+        plan.check()
+        t_step = max_over_ranks(statistics.mean(ms))
+        hin = [f["u_in"].cpu().pin_memory() for f in fields]
+        hout = [torch.empty_like(h).pin_memory() for h in hin]
+
+        def step_e2e():
+            for f, h in zip(fields, hin):
+                f["u_in"].copy_(h, non_blocking=True)
+            graph.replay()
+            for f, h in zip(fields, hout):
+                h.copy_(f["u_out"], non_blocking=True)
+
+        ms_e = timed(torch, step_e2e, K, W, flush, stream, barrier)
+        t_e2e = max_over_ranks(statistics.mean(ms_e))
+        nbytes = sum(f["u_in"].numel() * 8 for f in fields)
+        ach = b_alg / (statistics.mean(ms) * 1e-3) / 1e9
+        out = {
+            "metric": "batched props/s", "value": ws * nprop / (t_step * 1e-3), "unit": "props/s",
+            "ms_per_step": t_step, "dtype": "f32",
+            "config": {"workload": "batch 96 fields, sizes U{512,1024,2048,4096}^2, ASM/Fresnel/ARSS (s=0.5), "
+                                   "z U[10,300]mm, lambda U{640,532,450}nm, p=8um; one persistent launch in a CUDA graph",
+                       "items": plan.n_items, "l2": "inputs larger than L2 (%.1f GB)" % (nbytes / 1e9)},
+            "e2e": {"value": ws * nprop / (t_e2e * 1e-3), "unit": "props/s", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": ach / pk["hbm_gbs"], "traffic": None,
+                         "note": f"sum of 80 n bytes over the 96 propagations per step; peak {pk_kind}"},
+            "forms": {"persistent_graph": {"props/s": nprop * 1e3 / statistics.mean(ms), "ms": statistics.mean(ms)},
+                      "persistent_direct": {"ms": statistics.mean(ms_direct)},
+                      "serial_per_field": {"props/s": nprop * 1e3 / statistics.mean(ms_serial),
+                                           "ms": statistics.mean(ms_serial)}},
+            "clocks": clocks,
+        }
+        plan.close()
+
     if rank == 0:
         line = {"metric": out["metric"], "value": out["value"], "unit": out["unit"], "n_gpus": ws, "steps": K,
                 "warmup": W, "ms_per_step": out["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -611,7 +674,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cgh", choices=["cgh", "asm", "wrp", "adam"])
+    ap.add_argument("--workload", default="cgh", choices=["cgh", "asm", "wrp", "adam", "batch"])
     ap.add_argument("--cpu-rows", type=int, default=48)
     ap.add_argument("--ref-rows", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")

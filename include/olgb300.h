@@ -130,6 +130,37 @@ int olg_fresnel_prop_check(int ny, int nx, double dy, double dx, double lambda, 
 int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, double lambda, double z, int mode, int flags,
                  int *chosen, void *work, size_t work_bytes, olg_stream_t stream);
 
+/* ------------------------------------------------------ batched launch */
+/* Many propagations of different sizes, methods, distances and wavelengths
+ * in ONE persistent launch (the reference runs them one by one, each through
+ * its own chain of kernels and cuFFT calls).  Sizes: ny, nx powers of two in
+ * [256, 4096].  olg_batch_plan_create uploads the descriptors and takes all
+ * scratch (cudaMalloc; synchronous); olg_batch_execute then only resets
+ * counters and launches one kernel on `stream`, so it can be captured in a
+ * CUDA graph and replayed.  olg_batch_execute_serial runs the same fields one
+ * after another through the single-field entry points (the baseline). */
+#define OLG_BATCH_ASM 0
+#define OLG_BATCH_FRESNEL 1
+#define OLG_BATCH_ARSS 2
+#define OLG_BATCH_FRESNEL_BANDLIMIT 3
+typedef struct olg_field {
+    const void *in;  /* ny x nx complex64 device field (in == out allowed) */
+    void *out;
+    int ny, nx;
+    int method;      /* OLG_BATCH_* */
+    int flags;       /* OLG_CONJ, OLG_NO_NORMALIZE (ASM / Fresnel) */
+    double dy, dx, lambda, z;
+    double s, oy, ox; /* ARSS only */
+} olg_field;
+typedef struct olg_batch_plan_s *olg_batch_plan;
+int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_batch_plan *plan);
+int olg_batch_execute(olg_batch_plan plan, olg_stream_t stream);
+int olg_batch_execute_serial(olg_batch_plan plan, olg_stream_t stream);
+/* Synchronous: OLG_ERR_CUDA if an item of the last execution gave up on its bounded wait. */
+int olg_batch_check(olg_batch_plan plan);
+int olg_batch_plan_items(olg_batch_plan plan);
+int olg_batch_plan_destroy(olg_batch_plan plan);
+
 /* -------------------------------------------------- phase optimisation */
 /* Multi-plane phase-only hologram optimisation (the reference has none; it
  * builds on its ASM, golprop.h:507-534).  phi: ny x nx float (radians);

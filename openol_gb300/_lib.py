@@ -23,6 +23,13 @@ OLG_REUSE_OPERANDS = 0x20
 
 _d, _f, _i, _p, _sz = C.c_double, C.c_float, C.c_int, C.c_void_p, C.c_size_t
 
+class OlgField(C.Structure):
+    """olg_field (include/olgb300.h)."""
+    _fields_ = [("in_", C.c_void_p), ("out", C.c_void_p), ("ny", C.c_int), ("nx", C.c_int), ("method", C.c_int),
+                ("flags", C.c_int), ("dy", C.c_double), ("dx", C.c_double), ("lam", C.c_double), ("z", C.c_double),
+                ("s", C.c_double), ("oy", C.c_double), ("ox", C.c_double)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "olg_version": (_i, []),
@@ -37,6 +44,12 @@ SIGNATURES = {
     "olg_asm_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),
     "olg_fresnel_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),
     "olg_prop_c64": (_i, [_p, _i, _i, _d, _d, _d, _d, _i, _i, C.POINTER(_i), _p, _sz, _p]),
+    "olg_batch_plan_create": (_i, [C.POINTER(OlgField), _i, C.POINTER(_p)]),
+    "olg_batch_execute": (_i, [_p, _p]),
+    "olg_batch_execute_serial": (_i, [_p, _p]),
+    "olg_batch_check": (_i, [_p]),
+    "olg_batch_plan_items": (_i, [_p]),
+    "olg_batch_plan_destroy": (_i, [_p]),
     "olg_phase_opt_workspace_bytes": (_sz, [_i, _i]),
     "olg_phase_loss_grad": (_i, [_p, _p, C.POINTER(_d), _i, _i, _i, _d, _d, _d, _p, _p, _p, _sz, _p]),
     "olg_phase_adam_step": (_i, [_p, _p, _p, _p, C.POINTER(_d), _i, _i, _i, _d, _d, _d, _d, _d, _d, _d, _i, _p, _p,

@@ -122,17 +122,21 @@ __device__ __forceinline__ int saddr(int q, int i, int ss)
 }
 
 // One Stockham stage: radix R, NS = product of the radices already applied.
+// NT threads share the NSEQ * N / R butterflies; when NT exceeds them the
+// extra threads only take part in the barriers.
 template <int N, int R, int NS, int DIR, int NT, bool COLS, int NSEQ>
 __device__ __forceinline__ void fft_stage(float2 *s, int ss, const float2 *__restrict__ tw, int tid)
 {
     constexpr int B = N / R;
     constexpr int BT = NSEQ * B;
-    static_assert(BT % NT == 0, "threads must divide the butterflies");
-    constexpr int BPT = BT / NT;
+    static_assert(BT % NT == 0 || NT % BT == 0, "threads and butterflies must divide one another");
+    constexpr int BPT = BT >= NT ? BT / NT : 1;
+    constexpr bool GUARD = BT < NT;
     float2 v[BPT][R];
 #pragma unroll
     for (int t = 0; t < BPT; ++t) {
         const int b = tid + t * NT;
+        if (GUARD && b >= BT) continue;
         const int q = COLS ? (b % NSEQ) : (b / B);
         const int j = COLS ? (b / NSEQ) : (b % B);
 #pragma unroll
@@ -149,6 +153,7 @@ __device__ __forceinline__ void fft_stage(float2 *s, int ss, const float2 *__res
 #pragma unroll
     for (int t = 0; t < BPT; ++t) {
         const int b = tid + t * NT;
+        if (GUARD && b >= BT) continue;
         const int q = COLS ? (b % NSEQ) : (b / B);
         const int j = COLS ? (b / NSEQ) : (b % B);
         const int k = j & (NS - 1);

@@ -23,6 +23,7 @@
 // the sampled chirp exp(i pi (x^2 + y^2) / (lambda z)) is the outer product of
 // two 1-D FFTs, which k_chirp computes per call (exactly the DFT of the sampled
 // response the reference builds, golprop.h:184-187, olprop.h:133-137).
+#include <algorithm>
 #include <mutex>
 #include <vector>
 #include <cmath>
@@ -67,6 +68,9 @@ struct PropParams {
     const float *target;
     float seed_scale;
     double *loss;
+    // tables written earlier in the same launch (batched persistent kernel):
+    // read them through L2 (ld.global.cg), never the non-coherent path
+    int coherent;
 };
 
 // ---------------------------------------------------------------- launch shapes
@@ -92,6 +96,18 @@ __device__ __forceinline__ float2 apply_op(float2 v, int mode, const float2 *tx,
         if (!(abs(w - nx / 2) < wlim && abs(h - ny / 2) < hlim)) return v;
     }
     return cmul(v, cmul(__ldg(tx + w), __ldg(ty + h)));
+}
+
+__device__ __forceinline__ float2 ld_tab(const float2 *p, int coherent) { return coherent ? __ldcg(p) : __ldg(p); }
+
+__device__ __forceinline__ float2 apply_op_c(float2 v, int mode, const float2 *tx, const float2 *ty, int h, int w,
+                                             int ny, int nx, int hlim, int wlim, int coherent)
+{
+    if (mode == OP_NONE) return v;
+    if (mode == OP_TABLE_IN_WINDOW) {
+        if (!(abs(w - nx / 2) < wlim && abs(h - ny / 2) < hlim)) return v;
+    }
+    return cmul(v, cmul(ld_tab(tx + w, coherent), ld_tab(ty + h, coherent)));
 }
 
 // ------------------------------------------------------------------- pass 1
@@ -297,7 +313,7 @@ __device__ __forceinline__ float2 load_in(const PropParams &P, int h, int w)
     } else {
         x = __ldg(P.in + (size_t)h * P.nx + w);
     }
-    return apply_op(x, P.pre_mode, P.prex, P.prey, h, w, P.ny, P.nx, P.pre_hlim, P.pre_wlim);
+    return apply_op_c(x, P.pre_mode, P.prex, P.prey, h, w, P.ny, P.nx, P.pre_hlim, P.pre_wlim, P.coherent);
 }
 
 template <int N, int NT, int NSEQ>
@@ -328,7 +344,7 @@ __device__ __forceinline__ void rows_fwd_body(const PropParams &P, int r0, float
         dft<16, -1>(v);
         if (h < P.ny) {
 #pragma unroll
-            for (int k = 0; k < 16; ++k) P.S[(size_t)h * N + j + k * B] = v[outpos<16>(k)];
+            for (int k = 0; k < 16; ++k) __stcg(P.S + (size_t)h * N + j + k * B, v[outpos<16>(k)]);
         }
     }
 }
@@ -344,7 +360,7 @@ __device__ __forceinline__ void rows_inv_body(const PropParams &P, int r0, float
         float2 v[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r)
-            v[r] = h < P.ny ? P.S[(size_t)h * N + j + r * B] : make_float2(0.f, 0.f);
+            v[r] = h < P.ny ? __ldcg(P.S + (size_t)h * N + j + r * B) : make_float2(0.f, 0.f);
         dft<16, +1>(v);
 #pragma unroll
         for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
@@ -370,7 +386,8 @@ __device__ __forceinline__ void rows_inv_body(const PropParams &P, int r0, float
                 lsum = fmaf(r2, r2, lsum);
                 a = cscale(a, P.seed_scale * r2);
             } else {
-                a = apply_op(a, P.post_mode, P.postx, P.posty, h, w, P.ny, P.nx, P.post_hlim, P.post_wlim);
+                a = apply_op_c(a, P.post_mode, P.postx, P.posty, h, w, P.ny, P.nx, P.post_hlim, P.post_wlim,
+                               P.coherent);
             }
             if (P.accumulate) {
                 const float2 o = P.out[i];
@@ -389,7 +406,7 @@ __device__ __forceinline__ float2 tf_at(const PropParams &P, int ky, int kx, int
         const int fy = ky < NY / 2 ? ky : ky - NY;
         return asm_tf(P, fx, fy);
     }
-    float2 T = cmul(__ldg(P.Hx + kx), __ldg(P.Hy + ky));
+    float2 T = cmul(ld_tab(P.Hx + kx, P.coherent), ld_tab(P.Hy + ky, P.coherent));
     return P.conj ? cconj(T) : T;
 }
 
@@ -407,7 +424,7 @@ __device__ __forceinline__ void cols_body(const PropParams &P, int c0, float2 *s
         float2 v[16];
 #pragma unroll
         for (int r = 4; r < 12; ++r)
-            v[r] = kx < NX ? P.S[(size_t)(j + (r - 4) * B) * NX + kx] : make_float2(0.f, 0.f);
+            v[r] = kx < NX ? __ldcg(P.S + (size_t)(j + (r - 4) * B) * NX + kx) : make_float2(0.f, 0.f);
         dft16_in_mid<-1>(v);
 #pragma unroll
         for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = v[outpos<16>(k)];
@@ -448,7 +465,7 @@ __device__ __forceinline__ void cols_body(const PropParams &P, int c0, float2 *s
         dft16_out_mid<+1>(v);
         if (kx < NX) {
 #pragma unroll
-            for (int k = 4; k < 12; ++k) P.S[(size_t)(j + (k - 4) * B) * NX + kx] = v[outpos<16>(k)];
+            for (int k = 4; k < 12; ++k) __stcg(P.S + (size_t)(j + (k - 4) * B) * NX + kx, v[outpos<16>(k)]);
         }
     }
 }
@@ -514,13 +531,10 @@ struct ChirpCfg {
     static constexpr int SMEM = padded_len(N) * 8;
 };
 
-template <int N>
-__global__ void __launch_bounds__(ChirpCfg<N>::NT) k_chirp(ChirpAxis A)
+template <int N, int NT>
+__device__ __forceinline__ void chirp_body(const ChirpAxis &A, int part, float2 *sm, int tid)
 {
-    constexpr int NT = ChirpCfg<N>::NT;
-    extern __shared__ float2 sm[];
-    const int tid = threadIdx.x;
-    if (blockIdx.x == 0) {
+    if (part == 0) {
         for (int j = tid; j < N; j += NT) {
             const int m = j < N / 2 ? j : j - N;
             float2 c = make_float2(0.f, 0.f);
@@ -557,6 +571,13 @@ __global__ void __launch_bounds__(ChirpCfg<N>::NT) k_chirp(ChirpAxis A)
             }
         }
     }
+}
+
+template <int N>
+__global__ void __launch_bounds__(ChirpCfg<N>::NT) k_chirp(ChirpAxis A)
+{
+    extern __shared__ float2 sm[];
+    chirp_body<N, ChirpCfg<N>::NT>(A, blockIdx.x, sm, threadIdx.x);
 }
 
 // ===================================================================== host
@@ -765,18 +786,29 @@ extern "C" size_t olg_prop_workspace_bytes(int ny, int nx)
     return layout_bytes(ny, nx, nullptr, nullptr);
 }
 
-extern "C" int olg_asm_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
-                                double z, int flags, void *work, size_t work_bytes, olg_stream_t stream)
+namespace olg {
+namespace {
+
+// Parameters of one propagation: the three passes plus the per-axis chirp
+// jobs (none for ASM; spectra for Fresnel; spectra and pre/post tables for ARSS).
+struct PropSetup {
+    PropParams P;
+    ChirpAxis ax, ay;
+    bool chirps = false;
+};
+
+int check_phys(double dy, double dx, double lambda, double z, bool nonzero_z)
 {
-    if (int rc = validate(u_in, u_out, ny, nx)) return rc;
-    if (!(dy > 0) || !(dx > 0) || !(lambda > 0) || !std::isfinite(z)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
-    if (int rc = ensure_twiddles()) return rc;
-    cudaStream_t st = (cudaStream_t)stream;
-    Scratch sc;
-    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
-    Layout L;
-    layout_bytes(ny, nx, &L, (char *)sc.ptr);
-    PropParams P = base_params(u_in, u_out, ny, nx, L);
+    if (!(dy > 0) || !(dx > 0) || !(lambda > 0) || !std::isfinite(z) || (nonzero_z && z == 0.0))
+        return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    return OLG_OK;
+}
+
+int setup_asm(const void *in, void *out, int ny, int nx, double dy, double dx, double lambda, double z, int flags,
+              const Layout &L, PropSetup *S)
+{
+    if (int rc = check_phys(dy, dx, lambda, z, false)) return rc;
+    PropParams P = base_params(in, out, ny, nx, L);
     const double NX = 2.0 * nx, NY = 2.0 * ny;
     const double du = 1.0 / (dx * NX), dv = 1.0 / (dy * NY);
     const double zl = z / lambda;
@@ -789,24 +821,17 @@ extern "C" int olg_asm_prop_c64(const void *u_in, void *u_out, int ny, int nx, d
     P.tx = (float)(lambda * lambda * du * du);
     P.ty = (float)(lambda * lambda * dv * dv);
     P.zl = (float)zl;
-    return run_passes(P, st);
+    S->P = P;
+    S->chirps = false;
+    return OLG_OK;
 }
 
-extern "C" int olg_fresnel_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
-                                    double z, int bandlimit, int flags, void *work, size_t work_bytes,
-                                    olg_stream_t stream)
+int setup_fresnel(const void *in, void *out, int ny, int nx, double dy, double dx, double lambda, double z,
+                  int bandlimit, int flags, const Layout &L, PropSetup *S)
 {
-    if (int rc = validate(u_in, u_out, ny, nx)) return rc;
-    if (!(dy > 0) || !(dx > 0) || !(lambda > 0) || !std::isfinite(z) || z == 0.0)
-        return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (int rc = check_phys(dy, dx, lambda, z, true)) return rc;
     if (bandlimit < 0 || bandlimit > 2) return fail(OLG_ERR_INVALID_ARG, "bandlimit must be 0, 1 or 2");
-    if (int rc = ensure_twiddles()) return rc;
-    cudaStream_t st = (cudaStream_t)stream;
-    Scratch sc;
-    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
-    Layout L;
-    layout_bytes(ny, nx, &L, (char *)sc.ptr);
-    PropParams P = base_params(u_in, u_out, ny, nx, L);
+    PropParams P = base_params(in, out, ny, nx, L);
     const int NX = 2 * nx, NY = 2 * ny;
     const double np = (double)NX * (double)NY;
     const double sc1 = (flags & OLG_NO_NORMALIZE) ? 1.0 : 1.0 / np;
@@ -817,30 +842,23 @@ extern "C" int olg_fresnel_prop_c64(const void *u_in, void *u_out, int ny, int n
         limx = (int)floor_lim(std::fabs(lambda * z * 0.5 / dx) / dx);
         limy = (int)floor_lim(std::fabs(lambda * z * 0.5 / dy) / dy);
     }
-    ChirpAxis ax = chirp_axis_params(NX, nx, dx, lambda, z, 1.0, limx, sc1, L.Hx);
-    ChirpAxis ay = chirp_axis_params(NY, ny, dy, lambda, z, 1.0, limy, sc1, L.Hy);
-    if (int rc = chirp_axis(ax, st)) return rc;
-    if (int rc = chirp_axis(ay, st)) return rc;
+    S->ax = chirp_axis_params(NX, nx, dx, lambda, z, 1.0, limx, sc1, L.Hx);
+    S->ay = chirp_axis_params(NY, ny, dy, lambda, z, 1.0, limy, sc1, L.Hy);
+    S->chirps = true;
     P.method = M_CHIRP;
     P.conj = (flags & OLG_CONJ) ? 1 : 0;
     P.scale = 1.0f;
-    return run_passes(P, st);
+    S->P = P;
+    return OLG_OK;
 }
 
-extern "C" int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx, double lambda,
-                                 double z, double s, double oy, double ox, int flags, void *work, size_t work_bytes,
-                                 olg_stream_t stream)
+int setup_arss(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx, double lambda, double z,
+               double s, double oy, double ox, int flags, const Layout &L, PropSetup *S)
 {
-    if (int rc = validate(u_src, u_dst, ny, nx)) return rc;
-    if (!(dy > 0) || !(dx > 0) || !(lambda > 0) || !std::isfinite(z) || z == 0.0 || !std::isfinite(s))
-        return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
-    if (s == 0.0 || s == 1.0) return fail(OLG_ERR_INVALID_ARG, "ARSS is undefined for s = 0 or s = 1 (window limits divide by s|s-1|)");
-    if (int rc = ensure_twiddles()) return rc;
-    cudaStream_t st = (cudaStream_t)stream;
-    Scratch sc;
-    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
-    Layout L;
-    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    if (int rc = check_phys(dy, dx, lambda, z, true)) return rc;
+    if (!std::isfinite(s)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (s == 0.0 || s == 1.0)
+        return fail(OLG_ERR_INVALID_ARG, "ARSS is undefined for s = 0 or s = 1 (window limits divide by s|s-1|)");
     PropParams P = base_params(u_src, u_dst, ny, nx, L);
     const int NX = 2 * nx, NY = 2 * ny;
     const double np = (double)NX * (double)NY;
@@ -855,18 +873,27 @@ extern "C" int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx,
     ChirpAxis ax = chirp_axis_params(NX, nx, dx, lambda, z, s, lim_h, 1.0 / np, L.Hx);
     ChirpAxis ay = chirp_axis_params(NY, ny, dy, lambda, z, s, lim_h, 1.0 / np, L.Hy);
     // pre-chirp (golprop.h:830-841) and post-chirp (golprop.h:910-920) coefficients, cycles
-    struct Q { double a2, a1, a0; };
+    struct Q {
+        double a2, a1, a0;
+    };
     const Q prex{(s * s - s) * dx * dx / lz2, -2.0 * s * ox * dx / lz2, 0.0};
     const Q prey{(s * s - s) * dy * dy / lz2, -2.0 * s * oy * dy / lz2, 0.0};
     const Q postx{(1 - s) * dx * dx / lz2, 2.0 * ox * dx / lz2, (ox * ox + oy * oy) / lz2};
     const Q posty{(1 - s) * dy * dy / lz2, 2.0 * oy * dy / lz2, 0.0};
     auto fill = [&](ChirpAxis &A, float2 *ta, float2 *tb, const Q &qa, int alim, int aconj, const Q &qb, int blim,
                     int bconj) {
-        A.ta = ta; A.tb = tb;
-        set_quad(A.a2_hi, A.a2_lo, qa.a2); set_quad(A.a1_hi, A.a1_lo, qa.a1); A.a0 = frac_host(qa.a0);
-        A.alim = alim; A.aconj = aconj;
-        set_quad(A.b2_hi, A.b2_lo, qb.a2); set_quad(A.b1_hi, A.b1_lo, qb.a1); A.b0 = frac_host(qb.a0);
-        A.blim = blim; A.bconj = bconj;
+        A.ta = ta;
+        A.tb = tb;
+        set_quad(A.a2_hi, A.a2_lo, qa.a2);
+        set_quad(A.a1_hi, A.a1_lo, qa.a1);
+        A.a0 = frac_host(qa.a0);
+        A.alim = alim;
+        A.aconj = aconj;
+        set_quad(A.b2_hi, A.b2_lo, qb.a2);
+        set_quad(A.b1_hi, A.b1_lo, qb.a1);
+        A.b0 = frac_host(qb.a0);
+        A.blim = blim;
+        A.bconj = bconj;
     };
     if (!adj) {
         // pass 1: pre-chirp, zero outside its window; pass 3: post-chirp inside its window
@@ -874,22 +901,95 @@ extern "C" int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx,
         fill(ay, L.tay, L.tby, prey, hlim_u, 0, posty, -1, 0);
         P.pre_mode = OP_TABLE;
         P.post_mode = OP_TABLE_IN_WINDOW;
-        P.post_hlim = hlim_c; P.post_wlim = wlim_c;
+        P.post_hlim = hlim_c;
+        P.post_wlim = wlim_c;
     } else {
         // adjoint: conj(post-chirp) inside the Cz window first, conj(pre-chirp) with its window last
         fill(ax, L.tax, L.tbx, postx, -1, 1, prex, wlim_u, 1);
         fill(ay, L.tay, L.tby, posty, -1, 1, prey, hlim_u, 1);
         P.pre_mode = OP_TABLE_IN_WINDOW;
-        P.pre_hlim = hlim_c; P.pre_wlim = wlim_c;
+        P.pre_hlim = hlim_c;
+        P.pre_wlim = wlim_c;
         P.post_mode = OP_TABLE;
     }
-    P.prex = L.tax; P.prey = L.tay; P.postx = L.tbx; P.posty = L.tby;
-    if (int rc = chirp_axis(ax, st)) return rc;
-    if (int rc = chirp_axis(ay, st)) return rc;
+    P.prex = L.tax;
+    P.prey = L.tay;
+    P.postx = L.tbx;
+    P.posty = L.tby;
     P.method = M_CHIRP;
     P.conj = adj ? 1 : 0;
     P.scale = 1.0f;
-    return run_passes(P, st);
+    S->P = P;
+    S->ax = ax;
+    S->ay = ay;
+    S->chirps = true;
+    return OLG_OK;
+}
+
+int run_setup(const PropSetup &S, cudaStream_t st)
+{
+    if (S.chirps) {
+        if (int rc = chirp_axis(S.ax, st)) return rc;
+        if (int rc = chirp_axis(S.ay, st)) return rc;
+    }
+    return run_passes(S.P, st);
+}
+
+} // namespace
+} // namespace olg
+
+extern "C" int olg_asm_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                                double z, int flags, void *work, size_t work_bytes, olg_stream_t stream)
+{
+    if (int rc = validate(u_in, u_out, ny, nx)) return rc;
+    if (int rc = check_phys(dy, dx, lambda, z, false)) return rc;
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
+    Layout L;
+    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    PropSetup S;
+    if (int rc = setup_asm(u_in, u_out, ny, nx, dy, dx, lambda, z, flags, L, &S)) return rc;
+    return run_setup(S, st);
+}
+
+extern "C" int olg_fresnel_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                                    double z, int bandlimit, int flags, void *work, size_t work_bytes,
+                                    olg_stream_t stream)
+{
+    if (int rc = validate(u_in, u_out, ny, nx)) return rc;
+    if (int rc = check_phys(dy, dx, lambda, z, true)) return rc;
+    if (bandlimit < 0 || bandlimit > 2) return fail(OLG_ERR_INVALID_ARG, "bandlimit must be 0, 1 or 2");
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
+    Layout L;
+    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    PropSetup S;
+    if (int rc = setup_fresnel(u_in, u_out, ny, nx, dy, dx, lambda, z, bandlimit, flags, L, &S)) return rc;
+    return run_setup(S, st);
+}
+
+extern "C" int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx, double lambda,
+                                 double z, double s, double oy, double ox, int flags, void *work, size_t work_bytes,
+                                 olg_stream_t stream)
+{
+    if (int rc = validate(u_src, u_dst, ny, nx)) return rc;
+    if (int rc = check_phys(dy, dx, lambda, z, true)) return rc;
+    if (!std::isfinite(s)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (s == 0.0 || s == 1.0)
+        return fail(OLG_ERR_INVALID_ARG, "ARSS is undefined for s = 0 or s = 1 (window limits divide by s|s-1|)");
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
+    Layout L;
+    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    PropSetup S;
+    if (int rc = setup_arss(u_src, u_dst, ny, nx, dy, dx, lambda, z, s, oy, ox, flags, L, &S)) return rc;
+    return run_setup(S, st);
 }
 
 // ---------------------------------------------------------------- AUTO checks
@@ -956,6 +1056,328 @@ extern "C" int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, doubl
     }
     if (pick == 0) return olg_asm_prop_c64(u, u, ny, nx, dy, dx, lambda, z, f, work, work_bytes, stream);
     return olg_fresnel_prop_c64(u, u, ny, nx, dy, dx, lambda, z, pick == 2 ? 1 : 0, f, work, work_bytes, stream);
+}
+
+// ======================================================= batched persistent
+// Many propagations of uneven sizes, methods and wavelengths in one launch.
+// Work items, in queue order: every chirp job, then every pass-1 row group,
+// every pass-2 column tile, every pass-3 row group (large fields first within
+// each pass).  A CTA (one per SM, 512 threads) takes the next item with an
+// atomic ticket, waits until the item's field has finished the pass it depends
+// on (per-field counters; the wait is bounded and only ever on items taken
+// earlier by running CTAs, so it cannot deadlock), runs it with the same pass
+// bodies as the single-call kernels, then publishes its completion.
+namespace olg {
+
+constexpr int BATCH_NT = 512;
+constexpr int BATCH_SMEM = padded_len(FFT_MAX) * 8; // 8192 elements: the largest pass tile
+constexpr long long BATCH_WAIT = 4000000000LL;           // ~2 s of SM clock
+
+enum : int { BK_CHIRP = 0, BK_FWD = 1, BK_COLS = 2, BK_INV = 3 };
+
+struct BatchItem {
+    int field, kind, unit, n; // n: FFT length that selects the instantiation
+};
+
+struct BatchDev {
+    const PropParams *P;
+    const ChirpAxis *jobs;
+    const BatchItem *items;
+    int n_items;
+    int *head;
+    int *done;         // per field: chirp jobs, pass-1 units, pass-2 units finished
+    const int *target; // per field: how many of each there are
+    int *err;
+};
+
+__device__ __forceinline__ int ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ bool wait_at_least(const int *p, int target, long long budget)
+{
+    const long long t0 = clock64();
+    while (ld_acquire(p) < target) {
+        __nanosleep(100);
+        if (clock64() - t0 > budget) return false;
+    }
+    return true;
+}
+
+template <int N>
+__device__ __forceinline__ void batch_run(const PropParams &P, const ChirpAxis *jobs, const BatchItem &I, float2 *sm,
+                                          int tid)
+{
+    if (I.kind == BK_CHIRP) {
+        chirp_body<N, BATCH_NT>(jobs[I.unit >> 1], I.unit & 1, sm, tid);
+    } else if (I.kind == BK_FWD) {
+        rows_fwd_body<N, BATCH_NT, FFT_MAX / N>(P, I.unit * (FFT_MAX / N), sm, tid);
+    } else if (I.kind == BK_COLS) {
+        cols_body<N, BATCH_NT, FFT_MAX / N>(P, I.unit * (FFT_MAX / N), sm, tid);
+    } else {
+        float lsum = 0.f;
+        rows_inv_body<N, BATCH_NT, FFT_MAX / N>(P, I.unit * (FFT_MAX / N), sm, tid, lsum);
+    }
+}
+
+__global__ void __launch_bounds__(BATCH_NT, 1) k_batch(BatchDev D)
+{
+    extern __shared__ float2 sm[];
+    __shared__ int s_item, s_ok;
+    __shared__ PropParams sP;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(D.head, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= D.n_items) break;
+        const BatchItem I = D.items[it];
+        const int f = I.field;
+        if (tid == 0) {
+            bool ok = true;
+            if (I.kind == BK_FWD) ok = wait_at_least(D.done + 3 * f, D.target[3 * f], BATCH_WAIT);
+            else if (I.kind == BK_COLS)
+                ok = wait_at_least(D.done + 3 * f + 1, D.target[3 * f + 1], BATCH_WAIT) &&
+                     wait_at_least(D.done + 3 * f, D.target[3 * f], BATCH_WAIT);
+            else if (I.kind == BK_INV) ok = wait_at_least(D.done + 3 * f + 2, D.target[3 * f + 2], BATCH_WAIT);
+            if (!ok) atomicExch(D.err, 1);
+            __threadfence();
+            s_ok = ok;
+        }
+        {
+            const int *src = reinterpret_cast<const int *>(D.P + f);
+            int *dst = reinterpret_cast<int *>(&sP);
+            for (int w = tid; w < (int)(sizeof(PropParams) / 4); w += BATCH_NT) dst[w] = src[w];
+        }
+        __syncthreads();
+        if (s_ok) {
+            switch (I.n) {
+            case 512: batch_run<512>(sP, D.jobs, I, sm, tid); break;
+            case 1024: batch_run<1024>(sP, D.jobs, I, sm, tid); break;
+            case 2048: batch_run<2048>(sP, D.jobs, I, sm, tid); break;
+            case 4096: batch_run<4096>(sP, D.jobs, I, sm, tid); break;
+            case 8192: batch_run<8192>(sP, D.jobs, I, sm, tid); break;
+            default: break;
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && I.kind != BK_INV) {
+            __threadfence();
+            atomicAdd(D.done + 3 * f + (I.kind == BK_CHIRP ? 0 : I.kind == BK_FWD ? 1 : 2), 1);
+        }
+    }
+}
+
+} // namespace olg
+
+struct olg_batch_plan_s {
+    int dev = 0, n = 0, n_items = 0, grid = 0;
+    std::vector<olg_field> fields;
+    std::vector<size_t> ws_off;
+    char *mem = nullptr;
+    size_t bytes = 0;
+    BatchDev D{};
+    size_t counters_off = 0, counters_bytes = 0;
+};
+
+namespace olg {
+namespace {
+
+bool batch_size_ok(int n) { return n >= 256 && n <= FFT_MAX / 2 && is_pow2(n); }
+
+int field_setup(const olg_field &F, const Layout &L, PropSetup *S)
+{
+    switch (F.method) {
+    case OLG_BATCH_ASM: return setup_asm(F.in, F.out, F.ny, F.nx, F.dy, F.dx, F.lambda, F.z, F.flags, L, S);
+    case OLG_BATCH_FRESNEL: return setup_fresnel(F.in, F.out, F.ny, F.nx, F.dy, F.dx, F.lambda, F.z, 0, F.flags, L, S);
+    case OLG_BATCH_FRESNEL_BANDLIMIT:
+        return setup_fresnel(F.in, F.out, F.ny, F.nx, F.dy, F.dx, F.lambda, F.z, 1, F.flags, L, S);
+    case OLG_BATCH_ARSS:
+        return setup_arss(F.in, F.out, F.ny, F.nx, F.dy, F.dx, F.lambda, F.z, F.s, F.oy, F.ox, F.flags, L, S);
+    default: return fail(OLG_ERR_INVALID_ARG, "unknown batch method");
+    }
+}
+
+} // namespace
+} // namespace olg
+
+extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_batch_plan *out)
+{
+    if (!out || !fields || n_fields <= 0) return fail(OLG_ERR_INVALID_ARG, "no fields");
+    *out = nullptr;
+    for (int i = 0; i < n_fields; ++i) {
+        const olg_field &F = fields[i];
+        if (int rc = validate(F.in, F.out, F.ny, F.nx)) return rc;
+        if (!batch_size_ok(F.ny) || !batch_size_ok(F.nx))
+            return fail(OLG_ERR_UNSUPPORTED_SIZE, "batched fields must be powers of two in [256, 4096]");
+    }
+    if (int rc = ensure_twiddles()) return rc;
+    auto *plan = new olg_batch_plan_s();
+    plan->n = n_fields;
+    plan->fields.assign(fields, fields + n_fields);
+    cudaGetDevice(&plan->dev);
+    // device memory: [PropParams x n][ChirpAxis jobs][items][done 3n][target 3n][head, err][per-field scratch]
+    std::vector<PropSetup> setups(n_fields);
+    std::vector<ChirpAxis> jobs;
+    std::vector<BatchItem> items;
+    std::vector<int> target(3 * n_fields, 0);
+    size_t o = 0;
+    const size_t offP = o; o += align_up(sizeof(PropParams) * n_fields, 256);
+    // at most two axes per field
+    const size_t offJ = o; o += align_up(sizeof(ChirpAxis) * 2 * n_fields, 256);
+    // item count: chirp <= 4 per field, rows and column tiles per field
+    size_t n_items_max = 0;
+    for (auto &F : plan->fields) {
+        const int NX = 2 * F.nx, NY = 2 * F.ny;
+        const int rows = (F.ny + FFT_MAX / NX - 1) / (FFT_MAX / NX);
+        const int cols = (NX + FFT_MAX / NY - 1) / (FFT_MAX / NY);
+        n_items_max += 4 + 2 * rows + cols;
+    }
+    const size_t offI = o; o += align_up(sizeof(BatchItem) * n_items_max, 256);
+    const size_t offC = o; o += align_up(sizeof(int) * (6 * n_fields + 2), 256);
+    plan->ws_off.resize(n_fields);
+    for (int i = 0; i < n_fields; ++i) {
+        plan->ws_off[i] = o;
+        o += align_up(layout_bytes(plan->fields[i].ny, plan->fields[i].nx, nullptr, nullptr), 256);
+    }
+    plan->bytes = o;
+    cudaError_t e = cudaMalloc(&plan->mem, plan->bytes);
+    if (e != cudaSuccess) {
+        delete plan;
+        return cuda_fail(e, "cudaMalloc (batch plan)");
+    }
+    // per-field setup, chirp jobs and the item queue
+    std::vector<int> order(n_fields);
+    for (int i = 0; i < n_fields; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (long)plan->fields[a].ny * plan->fields[a].nx > (long)plan->fields[b].ny * plan->fields[b].nx;
+    });
+    for (int i = 0; i < n_fields; ++i) {
+        const olg_field &F = plan->fields[i];
+        Layout L;
+        layout_bytes(F.ny, F.nx, &L, plan->mem + plan->ws_off[i]);
+        if (int rc = field_setup(F, L, &setups[i])) {
+            cudaFree(plan->mem);
+            delete plan;
+            return rc;
+        }
+        setups[i].P.coherent = 1;
+        if (setups[i].chirps) {
+            for (int a = 0; a < 2; ++a) {
+                const ChirpAxis &A = a ? setups[i].ay : setups[i].ax;
+                const int jidx = (int)jobs.size();
+                jobs.push_back(A);
+                items.push_back({i, BK_CHIRP, 2 * jidx + 0, A.L});
+                target[3 * i] += 1;
+                if (A.ta || A.tb) {
+                    items.push_back({i, BK_CHIRP, 2 * jidx + 1, A.L});
+                    target[3 * i] += 1;
+                }
+            }
+        }
+    }
+    for (int kind = BK_FWD; kind <= BK_INV; ++kind)
+        for (int i : order) {
+            const olg_field &F = plan->fields[i];
+            const int NX = 2 * F.nx, NY = 2 * F.ny;
+            if (kind == BK_COLS) {
+                const int C = FFT_MAX / NY, units = (NX + C - 1) / C;
+                for (int u = 0; u < units; ++u) items.push_back({i, kind, u, NY});
+                target[3 * i + 2] = units;
+            } else {
+                const int R = FFT_MAX / NX, units = (F.ny + R - 1) / R;
+                for (int u = 0; u < units; ++u) items.push_back({i, kind, u, NX});
+                if (kind == BK_FWD) target[3 * i + 1] = units;
+            }
+        }
+    plan->n_items = (int)items.size();
+    std::vector<PropParams> Ps(n_fields);
+    for (int i = 0; i < n_fields; ++i) Ps[i] = setups[i].P;
+    e = cudaMemcpy(plan->mem + offP, Ps.data(), sizeof(PropParams) * n_fields, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !jobs.empty())
+        e = cudaMemcpy(plan->mem + offJ, jobs.data(), sizeof(ChirpAxis) * jobs.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan->mem + offI, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan->mem + offC + sizeof(int) * 3 * n_fields, target.data(), sizeof(int) * 3 * n_fields,
+                       cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(plan->mem);
+        delete plan;
+        return cuda_fail(e, "uploading the batch plan");
+    }
+    int* C = (int *)(plan->mem + offC);
+    plan->D.P = (const PropParams *)(plan->mem + offP);
+    plan->D.jobs = (const ChirpAxis *)(plan->mem + offJ);
+    plan->D.items = (const BatchItem *)(plan->mem + offI);
+    plan->D.n_items = plan->n_items;
+    plan->D.done = C;
+    plan->D.target = C + 3 * n_fields;
+    plan->D.head = C + 6 * n_fields;
+    plan->D.err = C + 6 * n_fields + 1;
+    plan->counters_off = offC;
+    plan->counters_bytes = sizeof(int) * 3 * n_fields;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, plan->dev);
+    plan->grid = nsm > 0 ? nsm : 1;
+    e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, BATCH_SMEM);
+    if (e != cudaSuccess) {
+        cudaFree(plan->mem);
+        delete plan;
+        return cuda_fail(e, "cudaFuncSetAttribute(k_batch)");
+    }
+    *out = plan;
+    return OLG_OK;
+}
+
+extern "C" int olg_batch_execute(olg_batch_plan plan, olg_stream_t stream)
+{
+    if (!plan) return fail(OLG_ERR_INVALID_ARG, "null plan");
+    cudaStream_t st = (cudaStream_t)stream;
+    // reset the done counters, the ticket and the error word (target stays)
+    cudaError_t e = cudaMemsetAsync(plan->D.done, 0, plan->counters_bytes, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(plan->D.head, 0, 2 * sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync (batch counters)");
+    k_batch<<<plan->grid, BATCH_NT, BATCH_SMEM, st>>>(plan->D);
+    count_launch();
+    return check_launch("k_batch");
+}
+
+extern "C" int olg_batch_execute_serial(olg_batch_plan plan, olg_stream_t stream)
+{
+    if (!plan) return fail(OLG_ERR_INVALID_ARG, "null plan");
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int i = 0; i < plan->n; ++i) {
+        const olg_field &F = plan->fields[i];
+        Layout L;
+        layout_bytes(F.ny, F.nx, &L, plan->mem + plan->ws_off[i]);
+        PropSetup S;
+        if (int rc = field_setup(F, L, &S)) return rc;
+        if (int rc = run_setup(S, st)) return rc;
+    }
+    return OLG_OK;
+}
+
+extern "C" int olg_batch_check(olg_batch_plan plan)
+{
+    if (!plan) return fail(OLG_ERR_INVALID_ARG, "null plan");
+    int err = 0;
+    cudaError_t e = cudaMemcpy(&err, plan->D.err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "reading the batch error word");
+    return err ? fail(OLG_ERR_CUDA, "a batched item gave up on a bounded wait") : OLG_OK;
+}
+
+extern "C" int olg_batch_plan_items(olg_batch_plan plan) { return plan ? plan->n_items : 0; }
+
+extern "C" int olg_batch_plan_destroy(olg_batch_plan plan)
+{
+    if (!plan) return OLG_OK;
+    cudaError_t e = cudaFree(plan->mem);
+    delete plan;
+    return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaFree (batch plan)");
 }
 
 // ------------------------------------------- multi-plane phase optimisation
