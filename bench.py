@@ -399,6 +399,7 @@ def run_ours(args):
                                              f"{dt:.1f} s"}
     elif args.workload == "asm":
         n = ASM["n"]
+        tuned = og.autotune(n, n)
         u0 = asm_input()
         src = torch.from_numpy(u0).cuda()
         dst = torch.empty_like(src)
@@ -435,7 +436,8 @@ def run_ours(args):
             "metric": "ASM props/s", "value": ws / (t_step * 1e-3), "unit": "props/s", "ms_per_step": t_step,
             "dtype": "f32",
             "config": {"workload": "asm 1024x1024 padded 2048x2048, p=8um, lambda=532nm, z=50mm",
-                       "l2": "flushed between steps (256 MiB write)"},
+                       "l2": "flushed between steps (256 MiB write)",
+                       "launch_variants": {f"{k}:{m}": v for (k, m), v in tuned.items()}},
             "e2e": {"value": ws / (t_e2e * 1e-3), "unit": "props/s", "h2d_bytes_per_step": u0.nbytes,
                     "d2h_bytes_per_step": u0.nbytes},
             "gpu_launches": int(launches),
@@ -454,6 +456,7 @@ def run_ours(args):
     elif args.workload == "wrp":
         c = WRP
         N = c["N"]
+        tuned = og.autotune(N, N)
         pts = wrp_points()
         obj = og.gObject(pts)
         U = torch.zeros((N, N), dtype=torch.complex64, device="cuda")
@@ -499,7 +502,8 @@ def run_ours(args):
         out = {
             "metric": "WRP holograms/s", "value": ws / (t_step * 1e-3), "unit": "holograms/s", "ms_per_step": t_step,
             "dtype": "f32 (double-float phase anchor)",
-            "config": {"workload": WRP_DESC, "l2": "flushed between steps (256 MiB write)"},
+            "config": {"workload": WRP_DESC, "l2": "flushed between steps (256 MiB write)",
+                       "launch_variants": {f"{k}:{m}": v for (k, m), v in tuned.items()}},
             "e2e": {"value": ws / (t_e2e * 1e-3), "unit": "holograms/s", "h2d_bytes_per_step": pts.nbytes,
                     "d2h_bytes_per_step": N * N},
             "gpu_launches": int(launches),
@@ -521,6 +525,7 @@ def run_ours(args):
     elif args.workload == "adam":
         c = ADAM
         n = c["n"]
+        tuned = og.autotune(n, n)
         phi0, t, zs = adam_problem()
         phi = torch.from_numpy(phi0.copy()).cuda()
         tt = torch.from_numpy(t).cuda()
@@ -573,7 +578,8 @@ def run_ours(args):
         out = {
             "metric": "grad-steps/s", "value": ws / (t_step * 1e-3), "unit": "grad-steps/s", "ms_per_step": t_step,
             "dtype": "f32",
-            "config": {"workload": ADAM_DESC, "lr": c["lr"], "l2": "flushed between steps (256 MiB write)"},
+            "config": {"workload": ADAM_DESC, "lr": c["lr"], "l2": "flushed between steps (256 MiB write)",
+                       "launch_variants": {f"{k}:{m}": v for (k, m), v in tuned.items()}},
             "e2e": {"value": ws / (t_e2e * 1e-3), "unit": "grad-steps/s", "h2d_bytes_per_step": phi0.nbytes,
                     "d2h_bytes_per_step": phi0.nbytes},
             "gpu_launches": int(launches),

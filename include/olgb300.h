@@ -117,6 +117,18 @@ int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy,
 int olg_asm_prop_noalloc_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
                              double z, int flags, olg_stream_t stream);
 
+/* Launch-shape autotuner of the three propagation passes (project-written;
+ * the reference has none).  Each pass has a few launch variants per FFT
+ * length (threads per CTA, elements per CTA, registers); olg_autotune_prop
+ * times every valid one on the device for an ny x nx field (real kernels,
+ * real shapes; synchronises `stream`) and keeps the fastest for the rest of
+ * the process.  kind: 0 row forward pass, 1 column pass, 2 row inverse pass;
+ * n: FFT length (2 nx or 2 ny).  Untuned lengths use variant 0. */
+int olg_autotune_prop(int ny, int nx, int reps, olg_stream_t stream);
+int olg_prop_variant_count(void);
+int olg_prop_get_variant(int kind, int n);
+int olg_prop_set_variant(int kind, int n, int idx);
+
 /* AUTO method selection, ol::AsmPropCheck (olprop.h:209-225) and
  * ol::FresnelPropCheck (olprop.h:109-123); single_precision != 0 evaluates
  * them in float like the reference's PREC_T=float instantiation.  1 = pass. */

@@ -13,6 +13,6 @@ from .batch import BatchPlan, config5_fields  # noqa: F401
 from .optim import PhaseOptimizer, make_targets, phase_loss_grad  # noqa: F401
 from .prop import (ASM, AUTO, FRESNEL, PROPMODE, ARSSFresnelProp, AsmPropCheck, FresnelPropCheck,  # noqa: F401
                    Prop, arss_prop, asm_prop, fresnel_prop, gAsmProp, gFresnelProp, gFresnelPropBandLimit,
-                   workspace, workspace_bytes)
+                   autotune, get_variant, set_variant, variant_count, workspace, workspace_bytes)
 
 __version__ = "0.1.0"

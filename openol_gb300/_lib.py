@@ -41,6 +41,10 @@ SIGNATURES = {
     "olg_asm_prop_noalloc_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _p]),
     "olg_fresnel_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _i, _p, _sz, _p]),
     "olg_arss_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_autotune_prop": (_i, [_i, _i, _i, _p]),
+    "olg_prop_variant_count": (_i, []),
+    "olg_prop_get_variant": (_i, [_i, _i]),
+    "olg_prop_set_variant": (_i, [_i, _i, _i]),
     "olg_asm_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),
     "olg_fresnel_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),
     "olg_prop_c64": (_i, [_p, _i, _i, _d, _d, _d, _d, _i, _i, C.POINTER(_i), _p, _sz, _p]),

@@ -290,20 +290,6 @@ __global__ void __launch_bounds__(ColCfg<N>::NT) k_cols(PropParams P)
 
 // =========================================================== v2 passes
 // N >= 256: register-resident first / last radix-16 stages (fft2.cuh).
-template <int N>
-struct Row2Cfg {
-    static constexpr int NT = N >= 8192 ? 512 : 256;
-    static constexpr int NSEQ = N >= 4096 ? 1 : 4096 / N;
-    static constexpr int SMEM = NSEQ * padded_len(N) * 8;
-};
-template <int N>
-struct Col2Cfg {
-    static constexpr int E = N >= 8192 ? 2 * N : 8192;
-    static constexpr int C = E / N;
-    static constexpr int NT = 512;
-    static constexpr int SMEM = padded_len(N) * C * 8;
-};
-
 __device__ __forceinline__ float2 load_in(const PropParams &P, int h, int w)
 {
     float2 x;
@@ -483,27 +469,69 @@ __device__ __forceinline__ void loss_reduce(float lsum, double *loss, int tid, i
     }
 }
 
-template <int N>
-__global__ void __launch_bounds__(Row2Cfg<N>::NT) k_rows_fwd2(PropParams P)
+// Launch-shape variants of the v2 passes (threads, elements per CTA, minimum
+// resident CTAs); olg_autotune_prop times them on the device and keeps the
+// fastest per FFT length.
+template <int NT_, int E_, int MINB_>
+struct Shape {
+    static constexpr int NT = NT_, E = E_, MINB = MINB_;
+};
+// rows: E = row elements per CTA (NSEQ = E / N rows, at least one)
+template <int I> struct RowVar;
+template <> struct RowVar<0> : Shape<256, 4096, 2> {};
+template <> struct RowVar<1> : Shape<256, 4096, 4> {};
+template <> struct RowVar<2> : Shape<512, 8192, 2> {};
+template <> struct RowVar<3> : Shape<128, 2048, 4> {};
+constexpr int N_ROW_VARIANTS = 4;
+// columns: E = elements per CTA (C = E / N adjacent columns)
+template <int I> struct ColVar;
+template <> struct ColVar<0> : Shape<512, 8192, 1> {};
+template <> struct ColVar<1> : Shape<512, 16384, 1> {};
+template <> struct ColVar<2> : Shape<256, 4096, 2> {};
+template <> struct ColVar<3> : Shape<256, 8192, 2> {};
+constexpr int N_COL_VARIANTS = 4;
+
+template <int N, class V>
+struct RowShape {
+    static constexpr int NT = V::NT;
+    static constexpr int NSEQ = V::E >= N ? V::E / N : 1;
+    static constexpr int SMEM = NSEQ * padded_len(N) * 8;
+    static constexpr bool valid = (NSEQ * (N / 16)) % NT == 0 && SMEM <= 200 * 1024;
+};
+template <int N, class V>
+struct ColShape {
+    static constexpr int NT = V::NT;
+    static constexpr int C = V::E / N;
+    static constexpr int SMEM = padded_len(N) * (C > 0 ? C : 1) * 8;
+    static constexpr bool valid = C >= 1 && (C * (N / 16)) % NT == 0 && SMEM <= 200 * 1024;
+};
+
+template <int N, class V>
+__global__ void __launch_bounds__(V::NT, V::MINB) k_rows_fwd2(PropParams P)
 {
     extern __shared__ float2 sm[];
-    rows_fwd_body<N, Row2Cfg<N>::NT, Row2Cfg<N>::NSEQ>(P, blockIdx.x * Row2Cfg<N>::NSEQ, sm, threadIdx.x);
+    using S = RowShape<N, V>;
+    if constexpr (S::valid) rows_fwd_body<N, S::NT, S::NSEQ>(P, blockIdx.x * S::NSEQ, sm, threadIdx.x);
 }
 
-template <int N>
-__global__ void __launch_bounds__(Row2Cfg<N>::NT) k_rows_inv2(PropParams P)
+template <int N, class V>
+__global__ void __launch_bounds__(V::NT, V::MINB) k_rows_inv2(PropParams P)
 {
     extern __shared__ float2 sm[];
-    float lsum = 0.f;
-    rows_inv_body<N, Row2Cfg<N>::NT, Row2Cfg<N>::NSEQ>(P, blockIdx.x * Row2Cfg<N>::NSEQ, sm, threadIdx.x, lsum);
-    if (P.post_mode == OP_SEED) loss_reduce(lsum, P.loss, threadIdx.x, Row2Cfg<N>::NT);
+    using S = RowShape<N, V>;
+    if constexpr (S::valid) {
+        float lsum = 0.f;
+        rows_inv_body<N, S::NT, S::NSEQ>(P, blockIdx.x * S::NSEQ, sm, threadIdx.x, lsum);
+        if (P.post_mode == OP_SEED) loss_reduce(lsum, P.loss, threadIdx.x, S::NT);
+    }
 }
 
-template <int N>
-__global__ void __launch_bounds__(Col2Cfg<N>::NT) k_cols2(PropParams P)
+template <int N, class V>
+__global__ void __launch_bounds__(V::NT, V::MINB) k_cols2(PropParams P)
 {
     extern __shared__ float2 sm[];
-    cols_body<N, Col2Cfg<N>::NT, Col2Cfg<N>::C>(P, blockIdx.x * Col2Cfg<N>::C, sm, threadIdx.x);
+    using S = ColShape<N, V>;
+    if constexpr (S::valid) cols_body<N, S::NT, S::C>(P, blockIdx.x * S::C, sm, threadIdx.x);
 }
 
 // ------------------------------------------------------------- chirp tables
@@ -613,21 +641,79 @@ int prep_smem(K kern, int bytes)
     return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaFuncSetAttribute");
 }
 
+// selected variant per FFT length (index log2 N) and pass kind (0 rows fwd, 1 cols, 2 rows inv)
+int g_variant[3][14] = {};
+
+template <int N, int I>
+int launch_rows_v(const PropParams &P, bool inverse, cudaStream_t st)
+{
+    using S = RowShape<N, RowVar<I>>;
+    if constexpr (!S::valid) {
+        return fail(OLG_ERR_INVALID_ARG, "row variant not valid for this length");
+    } else {
+        const int grid = (P.ny + S::NSEQ - 1) / S::NSEQ;
+        if (!inverse) {
+            if (int rc = prep_smem(k_rows_fwd2<N, RowVar<I>>, S::SMEM)) return rc;
+            k_rows_fwd2<N, RowVar<I>><<<grid, S::NT, S::SMEM, st>>>(P);
+        } else {
+            if (int rc = prep_smem(k_rows_inv2<N, RowVar<I>>, S::SMEM)) return rc;
+            k_rows_inv2<N, RowVar<I>><<<grid, S::NT, S::SMEM, st>>>(P);
+        }
+        count_launch();
+        return check_launch(inverse ? "k_rows_inv2" : "k_rows_fwd2");
+    }
+}
+
+template <int N, int I>
+int launch_cols_v(const PropParams &P, cudaStream_t st)
+{
+    using S = ColShape<N, ColVar<I>>;
+    if constexpr (!S::valid) {
+        return fail(OLG_ERR_INVALID_ARG, "column variant not valid for this length");
+    } else {
+        const int grid = (P.NX + S::C - 1) / S::C;
+        if (int rc = prep_smem(k_cols2<N, ColVar<I>>, S::SMEM)) return rc;
+        k_cols2<N, ColVar<I>><<<grid, S::NT, S::SMEM, st>>>(P);
+        count_launch();
+        return check_launch("k_cols2");
+    }
+}
+
+template <int N>
+bool row_variant_valid(int i)
+{
+    switch (i) {
+    case 0: return RowShape<N, RowVar<0>>::valid;
+    case 1: return RowShape<N, RowVar<1>>::valid;
+    case 2: return RowShape<N, RowVar<2>>::valid;
+    case 3: return RowShape<N, RowVar<3>>::valid;
+    default: return false;
+    }
+}
+template <int N>
+bool col_variant_valid(int i)
+{
+    switch (i) {
+    case 0: return ColShape<N, ColVar<0>>::valid;
+    case 1: return ColShape<N, ColVar<1>>::valid;
+    case 2: return ColShape<N, ColVar<2>>::valid;
+    case 3: return ColShape<N, ColVar<3>>::valid;
+    default: return false;
+    }
+}
+
+constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+
 template <int N>
 int launch_rows(const PropParams &P, bool inverse, cudaStream_t st)
 {
     if constexpr (N >= 256) {
-        using C2 = Row2Cfg<N>;
-        const int grid = (P.ny + C2::NSEQ - 1) / C2::NSEQ;
-        if (!inverse) {
-            if (int rc = prep_smem(k_rows_fwd2<N>, C2::SMEM)) return rc;
-            k_rows_fwd2<N><<<grid, C2::NT, C2::SMEM, st>>>(P);
-        } else {
-            if (int rc = prep_smem(k_rows_inv2<N>, C2::SMEM)) return rc;
-            k_rows_inv2<N><<<grid, C2::NT, C2::SMEM, st>>>(P);
+        switch (g_variant[inverse ? 2 : 0][ilog2(N)]) {
+        case 1: return launch_rows_v<N, 1>(P, inverse, st);
+        case 2: return launch_rows_v<N, 2>(P, inverse, st);
+        case 3: return launch_rows_v<N, 3>(P, inverse, st);
+        default: return launch_rows_v<N, 0>(P, inverse, st);
         }
-        count_launch();
-        return check_launch(inverse ? "k_rows_inv2" : "k_rows_fwd2");
     }
     using C = RowCfg<N>;
     const int grid = (P.ny + C::NSEQ - 1) / C::NSEQ;
@@ -646,12 +732,12 @@ template <int N>
 int launch_cols(const PropParams &P, cudaStream_t st)
 {
     if constexpr (N >= 256) {
-        using C2 = Col2Cfg<N>;
-        const int grid = (P.NX + C2::C - 1) / C2::C;
-        if (int rc = prep_smem(k_cols2<N>, C2::SMEM)) return rc;
-        k_cols2<N><<<grid, C2::NT, C2::SMEM, st>>>(P);
-        count_launch();
-        return check_launch("k_cols2");
+        switch (g_variant[1][ilog2(N)]) {
+        case 1: return launch_cols_v<N, 1>(P, st);
+        case 2: return launch_cols_v<N, 2>(P, st);
+        case 3: return launch_cols_v<N, 3>(P, st);
+        default: return launch_cols_v<N, 0>(P, st);
+        }
     }
     using C = ColCfg<N>;
     const int grid = (P.NX + C::C - 1) / C::C;
@@ -990,6 +1076,108 @@ extern "C" int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx,
     PropSetup S;
     if (int rc = setup_arss(u_src, u_dst, ny, nx, dy, dx, lambda, z, s, oy, ox, flags, L, &S)) return rc;
     return run_setup(S, st);
+}
+
+// ------------------------------------------------------------- autotuner
+namespace olg {
+namespace {
+
+#define OLG_N_SWITCH(n, EXPR)                                                                                           \
+    switch (n) {                                                                                                       \
+    case 256: { constexpr int NN = 256; EXPR; }                                                                        \
+    case 512: { constexpr int NN = 512; EXPR; }                                                                        \
+    case 1024: { constexpr int NN = 1024; EXPR; }                                                                      \
+    case 2048: { constexpr int NN = 2048; EXPR; }                                                                      \
+    case 4096: { constexpr int NN = 4096; EXPR; }                                                                      \
+    case 8192: { constexpr int NN = 8192; EXPR; }                                                                      \
+    default: return false;                                                                                             \
+    }
+
+bool variant_valid(int kind, int n, int i)
+{
+    if (kind == 1) { OLG_N_SWITCH(n, return col_variant_valid<NN>(i)) }
+    OLG_N_SWITCH(n, return row_variant_valid<NN>(i))
+}
+
+int log2i(int n)
+{
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    return l;
+}
+
+} // namespace
+} // namespace olg
+
+extern "C" int olg_prop_variant_count(void) { return N_ROW_VARIANTS > N_COL_VARIANTS ? N_ROW_VARIANTS : N_COL_VARIANTS; }
+
+extern "C" int olg_prop_get_variant(int kind, int n)
+{
+    if (kind < 0 || kind > 2 || !is_pow2(n) || n < 256 || n > FFT_MAX) return -1;
+    return g_variant[kind][log2i(n)];
+}
+
+extern "C" int olg_prop_set_variant(int kind, int n, int idx)
+{
+    if (kind < 0 || kind > 2 || !is_pow2(n) || n < 256 || n > FFT_MAX) return fail(OLG_ERR_INVALID_ARG, "bad pass kind or length");
+    if (!variant_valid(kind, n, idx)) return fail(OLG_ERR_INVALID_ARG, "launch variant not valid for this length");
+    g_variant[kind][log2i(n)] = idx;
+    return OLG_OK;
+}
+
+// Times every valid launch variant of the three passes on an ny x nx ASM
+// propagation (the real kernels on the real shapes) and keeps the fastest.
+extern "C" int olg_autotune_prop(int ny, int nx, int reps, olg_stream_t stream)
+{
+    if (!is_pow2(nx) || !is_pow2(ny) || nx < 128 || ny < 128 || 2 * nx > FFT_MAX || 2 * ny > FFT_MAX)
+        return fail(OLG_ERR_UNSUPPORTED_SIZE, "autotuning covers fields with ny, nx powers of two in [128, 4096]");
+    if (reps < 1) reps = 5;
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch buf, sc;
+    if (int rc = buf.acquire(nullptr, 0, (size_t)ny * nx * sizeof(float2), st)) return rc;
+    if (int rc = sc.acquire(nullptr, 0, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
+    cudaError_t e = cudaMemsetAsync(buf.ptr, 0, (size_t)ny * nx * sizeof(float2), st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    Layout L;
+    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    PropSetup S;
+    if (int rc = setup_asm(buf.ptr, buf.ptr, ny, nx, 8e-6, 8e-6, 532e-9, 0.05, 0, L, &S)) return rc;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int lens[3] = {2 * nx, 2 * ny, 2 * nx};
+    for (int kind = 0; kind < 3; ++kind) {
+        const int n = lens[kind], ln = log2i(n);
+        float best = 1e30f;
+        int best_i = g_variant[kind][ln];
+        for (int i = 0; i < olg_prop_variant_count(); ++i) {
+            if (!variant_valid(kind, n, i)) continue;
+            g_variant[kind][ln] = i;
+            auto run = [&]() { return kind == 1 ? cols_pass(S.P, st) : rows_pass(S.P, kind == 2, st); };
+            int rc = OLG_OK;
+            for (int w = 0; w < 2 && !rc; ++w) rc = run();
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps && !rc; ++r) rc = run();
+            cudaEventRecord(e1, st);
+            if (rc) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return rc;
+            }
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                best_i = i;
+            }
+        }
+        g_variant[kind][ln] = best_i;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return OLG_OK;
 }
 
 // ---------------------------------------------------------------- AUTO checks

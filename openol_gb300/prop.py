@@ -167,3 +167,23 @@ def Prop(u, ny, nx, dy, dx, lam, d, propmode=PROPMODE.AUTO, verbose=True, single
 
 
 Prop.last_choice = -1
+
+
+# ------------------------------------------------------------------ autotuner
+def autotune(ny, nx, reps=5, stream=None):
+    """Time every launch variant of the three passes for an ny x nx field and keep
+    the fastest (olg_autotune_prop).  Returns {(kind, n): variant}."""
+    call("olg_autotune_prop", int(ny), int(nx), int(reps), _stream(stream))
+    return {(k, n): int(lib().olg_prop_get_variant(k, n)) for k, n in ((0, 2 * nx), (1, 2 * ny), (2, 2 * nx))}
+
+
+def set_variant(kind, n, idx):
+    call("olg_prop_set_variant", int(kind), int(n), int(idx))
+
+
+def get_variant(kind, n):
+    return int(lib().olg_prop_get_variant(int(kind), int(n)))
+
+
+def variant_count():
+    return int(lib().olg_prop_variant_count())
