@@ -1265,7 +1265,9 @@ enum : int { BK_CHIRP = 0, BK_FWD = 1, BK_COLS = 2, BK_INV = 3 };
 
 struct BatchItem {
     int field, kind, unit, n; // n: FFT length that selects the instantiation
+    int count;                // consecutive units processed by this item
 };
+constexpr int BATCH_UNITS_PER_ITEM = 16; // 16 x 8192 elements per item
 
 struct BatchDev {
     const PropParams *P;
@@ -1317,6 +1319,7 @@ __global__ void __launch_bounds__(BATCH_NT, 1) k_batch(BatchDev D)
     __shared__ int s_item, s_ok;
     __shared__ PropParams sP;
     const int tid = threadIdx.x;
+    int loaded_field = -1;
     for (;;) {
         if (tid == 0) s_item = atomicAdd(D.head, 1);
         __syncthreads();
@@ -1335,26 +1338,32 @@ __global__ void __launch_bounds__(BATCH_NT, 1) k_batch(BatchDev D)
             __threadfence();
             s_ok = ok;
         }
-        {
+        if (f != loaded_field) {
             const int *src = reinterpret_cast<const int *>(D.P + f);
             int *dst = reinterpret_cast<int *>(&sP);
             for (int w = tid; w < (int)(sizeof(PropParams) / 4); w += BATCH_NT) dst[w] = src[w];
+            loaded_field = f;
         }
         __syncthreads();
         if (s_ok) {
-            switch (I.n) {
-            case 512: batch_run<512>(sP, D.jobs, I, sm, tid); break;
-            case 1024: batch_run<1024>(sP, D.jobs, I, sm, tid); break;
-            case 2048: batch_run<2048>(sP, D.jobs, I, sm, tid); break;
-            case 4096: batch_run<4096>(sP, D.jobs, I, sm, tid); break;
-            case 8192: batch_run<8192>(sP, D.jobs, I, sm, tid); break;
-            default: break;
+            for (int u = 0; u < I.count; ++u) {
+                BatchItem J = I;
+                J.unit = I.unit + u;
+                switch (I.n) {
+                case 512: batch_run<512>(sP, D.jobs, J, sm, tid); break;
+                case 1024: batch_run<1024>(sP, D.jobs, J, sm, tid); break;
+                case 2048: batch_run<2048>(sP, D.jobs, J, sm, tid); break;
+                case 4096: batch_run<4096>(sP, D.jobs, J, sm, tid); break;
+                case 8192: batch_run<8192>(sP, D.jobs, J, sm, tid); break;
+                default: break;
+                }
+                __syncthreads();
             }
         }
         __syncthreads();
         if (tid == 0 && I.kind != BK_INV) {
             __threadfence();
-            atomicAdd(D.done + 3 * f + (I.kind == BK_CHIRP ? 0 : I.kind == BK_FWD ? 1 : 2), 1);
+            atomicAdd(D.done + 3 * f + (I.kind == BK_CHIRP ? 0 : I.kind == BK_FWD ? 1 : 2), I.count);
         }
     }
 }
@@ -1458,10 +1467,10 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
                 const ChirpAxis &A = a ? setups[i].ay : setups[i].ax;
                 const int jidx = (int)jobs.size();
                 jobs.push_back(A);
-                items.push_back({i, BK_CHIRP, 2 * jidx + 0, A.L});
+                items.push_back({i, BK_CHIRP, 2 * jidx + 0, A.L, 1});
                 target[3 * i] += 1;
                 if (A.ta || A.tb) {
-                    items.push_back({i, BK_CHIRP, 2 * jidx + 1, A.L});
+                    items.push_back({i, BK_CHIRP, 2 * jidx + 1, A.L, 1});
                     target[3 * i] += 1;
                 }
             }
@@ -1473,11 +1482,13 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
             const int NX = 2 * F.nx, NY = 2 * F.ny;
             if (kind == BK_COLS) {
                 const int C = FFT_MAX / NY, units = (NX + C - 1) / C;
-                for (int u = 0; u < units; ++u) items.push_back({i, kind, u, NY});
+                for (int u = 0; u < units; u += BATCH_UNITS_PER_ITEM)
+                    items.push_back({i, kind, u, NY, std::min(BATCH_UNITS_PER_ITEM, units - u)});
                 target[3 * i + 2] = units;
             } else {
                 const int R = FFT_MAX / NX, units = (F.ny + R - 1) / R;
-                for (int u = 0; u < units; ++u) items.push_back({i, kind, u, NX});
+                for (int u = 0; u < units; u += BATCH_UNITS_PER_ITEM)
+                    items.push_back({i, kind, u, NX, std::min(BATCH_UNITS_PER_ITEM, units - u)});
                 if (kind == BK_FWD) target[3 * i + 1] = units;
             }
         }
