@@ -19,8 +19,10 @@
 //                  phases range-reduced exactly (frac_mul), sincospif
 // k_cgh_gemm       warp-specialised tcgen05 GEMM: warp 0 issues TMA loads into a
 //                  4-stage ring (128 x 64 A and 256 x 64 B f16 tiles, 128-byte
-//                  swizzle), warp 1 owns TMEM (256 f32 columns) and issues the
-//                  128 x 256 x 16 MMAs, warps 2-5 drain TMEM and write complex64.
+//                  swizzle), warp 1 owns TMEM (two 256-column f32 accumulators)
+//                  and issues the 128 x 256 x 16 MMAs chunk by chunk, warps 2-9
+//                  add each finished chunk into f32 registers and finally write
+//                  complex64.
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
@@ -150,7 +152,16 @@ struct GemmParams {
     int *err;
 };
 
-__global__ void __launch_bounds__(192, 1)
+// Accumulation: the MMA warp writes chunks of GB_CHUNK K-blocks alternately
+// into two 256-column TMEM accumulators; the 8 epilogue warps add every
+// finished chunk into f32 registers (rounded adds) while the next chunk
+// runs, so the tensor pipe's own accumulation never spans more than
+// GB_CHUNK x 64 x 3 products.
+constexpr int GB_CHUNK = 8;
+constexpr int GB_EPI_WARPS = 8;
+constexpr int GB_THREADS = 64 + 32 * GB_EPI_WARPS;
+
+__global__ void __launch_bounds__(GB_THREADS, 1)
     k_cgh_gemm(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, GemmParams P)
 {
@@ -160,25 +171,30 @@ __global__ void __launch_bounds__(192, 1)
     uint8_t *sB = smem + GB_STAGES * GB_A_BYTES;
     uint64_t *full = (uint64_t *)(sB + GB_STAGES * GB_B_BYTES);
     uint64_t *empty = full + GB_STAGES;
-    uint64_t *done = empty + GB_STAGES;
-    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    uint64_t *tfull = empty + GB_STAGES; // [2]
+    uint64_t *tfree = tfull + 2;         // [2]
+    uint32_t *tmem_slot = (uint32_t *)(tfree + 2);
     volatile int *fault = (volatile int *)(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
     const int total = 3 * P.kblocks;
+    const int nchunks = (total + GB_CHUNK - 1) / GB_CHUNK;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < GB_STAGES; ++s) {
             mbar_init(smem_u32(full + s), 1);
             mbar_init(smem_u32(empty + s), 1);
         }
-        mbar_init(smem_u32(done), 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(tfull + b), 1);
+            mbar_init(smem_u32(tfree + b), GB_EPI_WARPS);
+        }
         *fault = 0;
         fence_mbar_init();
     }
     if (warp == 1) {
-        tmem_alloc(smem_u32(tmem_slot), GB_N);
+        tmem_alloc(smem_u32(tmem_slot), 2 * GB_N);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -204,53 +220,84 @@ __global__ void __launch_bounds__(192, 1)
                 tma_load_2d(smem_u32(sB + s * GB_B_BYTES), mb, smem_u32(full + s), kk, n0);
                 issued = kb + 1;
             }
-            // never leave with copies in flight: wait (bounded) for the last
-            // stages issued to land before the CTA may exit
+            // never leave with copies in flight
             for (int kb = issued > GB_STAGES ? issued - GB_STAGES : 0; kb < issued; ++kb)
                 mbar_wait(smem_u32(full + kb % GB_STAGES), (uint32_t)(kb / GB_STAGES) & 1u, GB_WAIT);
         }
     } else if (warp == 1) {
         if (lane == 0) {
             constexpr uint32_t idesc = idesc_f16_f32(GB_M, GB_N);
-            for (int kb = 0; kb < total && !*fault; ++kb) {
-                const int s = kb % GB_STAGES;
-                if (!mbar_wait(smem_u32(full + s), (uint32_t)(kb / GB_STAGES) & 1u, GB_WAIT)) {
+            for (int c = 0; c < nchunks && !*fault; ++c) {
+                const int b = c & 1;
+                if (c >= 2 && !mbar_wait(smem_u32(tfree + b), (uint32_t)((c >> 1) - 1) & 1u, GB_WAIT)) {
                     *fault = 1;
                     break;
                 }
                 tc_fence_after();
-                const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * GB_B_BYTES);
+                const uint32_t d = tmem + (uint32_t)(b * GB_N);
+                const int kb0 = c * GB_CHUNK, kb1 = min(total, kb0 + GB_CHUNK);
+                for (int kb = kb0; kb < kb1; ++kb) {
+                    const int s = kb % GB_STAGES;
+                    if (!mbar_wait(smem_u32(full + s), (uint32_t)(kb / GB_STAGES) & 1u, GB_WAIT)) {
+                        *fault = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * GB_B_BYTES);
 #pragma unroll
-                for (int k = 0; k < GB_K / 16; ++k)
-                    umma_f16(tmem, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), idesc, (kb | k) ? 1u : 0u);
-                umma_commit(smem_u32(empty + s));
+                    for (int k = 0; k < GB_K / 16; ++k)
+                        umma_f16(d, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), idesc,
+                                 (kb > kb0 || k > 0) ? 1u : 0u);
+                    umma_commit(smem_u32(empty + s));
+                }
+                umma_commit(smem_u32(tfull + b));
             }
-            umma_commit(smem_u32(done));
         }
     } else {
-        // epilogue: warp w drains TMEM lanes [32 (w % 4), +32)
-        const int q = warp & 3;
-        const bool ok = mbar_wait(smem_u32(done), 0u, GB_WAIT);
-        if (!ok) *fault = 1;
-        tc_fence_after();
+        // epilogue: warp w drains TMEM lanes [32 (w % 4), +32), columns [128 half, +128)
+        const int q = warp & 3, half = (warp - 2) >> 2;
+        float acc[128];
+#pragma unroll
+        for (int i = 0; i < 128; ++i) acc[i] = 0.f;
+        bool ok = true;
+        for (int c = 0; c < nchunks; ++c) {
+            const int b = c & 1;
+            if (ok && !mbar_wait(smem_u32(tfull + b), (uint32_t)(c >> 1) & 1u, GB_WAIT)) {
+                *fault = 1;
+                ok = false;
+            }
+            if (!ok || *fault) break;
+            tc_fence_after();
+            const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * GB_N + 128 * half);
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc) {
+                float v[16];
+                tmem_ld16(base + 16 * cc, v);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) acc[16 * cc + i] += v[i];
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tfree + b)) : "memory");
+        }
         const int row = m0 + 32 * q + lane; // row of D
         const int h = row >> 1;
         const bool odd = row & 1;
-        for (int c = 0; c < GB_N; c += 16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c, v);
+        const bool store = ok && !*fault && row < P.m2;
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
             float o[16];
 #pragma unroll
-            for (int i = 0; i < 16; ++i) o[i] = __shfl_xor_sync(0xffffffffu, v[i], 1);
-            if (!ok || *fault || row >= P.m2) continue;
-            // even lane holds Re of row h, odd lane Im: even writes columns c..c+7, odd c+8..c+15
-            const int cb = n0 + c + (odd ? 8 : 0);
+            for (int i = 0; i < 16; ++i) o[i] = __shfl_xor_sync(0xffffffffu, acc[16 * cc + i], 1);
+            if (!store) continue;
+            // even lane holds Re of row h, odd lane Im: even writes columns +0..7, odd +8..15
+            const int cb = n0 + 128 * half + 16 * cc + (odd ? 8 : 0);
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
                 const int col = cb + i;
                 if (col >= P.n) break;
-                const float re = odd ? o[8 + i] : v[i];
-                const float im = odd ? v[8 + i] : o[i];
+                const float re = odd ? o[8 + i] : acc[16 * cc + i];
+                const float im = odd ? acc[16 * cc + 8 + i] : o[i];
                 float2 *dst = P.U + (size_t)h * P.n + col;
                 if (P.accumulate) {
                     const float2 prev = *dst;
@@ -263,7 +310,7 @@ __global__ void __launch_bounds__(192, 1)
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 1) tmem_dealloc(tmem, GB_N);
+    if (warp == 1) tmem_dealloc(tmem, 2 * GB_N);
     if (threadIdx.x == 0 && *fault) atomicExch(P.err, 1);
 }
 
@@ -397,7 +444,7 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
         attr_done[dev] = true;
     }
     dim3 grid((nx + GB_N - 1) / GB_N, (2 * ny + GB_M - 1) / GB_M);
-    k_cgh_gemm<<<grid, 192, GB_SMEM, st>>>(mAh, mAl, mBh, mBl, P);
+    k_cgh_gemm<<<grid, GB_THREADS, GB_SMEM, st>>>(mAh, mAl, mBh, mBl, P);
     count_launch();
     return check_launch("k_cgh_gemm");
 }

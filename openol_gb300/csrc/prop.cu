@@ -1257,7 +1257,11 @@ extern "C" int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, doubl
 // bodies as the single-call kernels, then publishes its completion.
 namespace olg {
 
-constexpr int BATCH_NT = 512;
+constexpr int BATCH_NT = 256;
+constexpr int BATCH_CTAS_PER_SM = 2;
+// rows per row unit and columns per column tile (>= 4096 elements, 8192 for N = 8192)
+__host__ __device__ constexpr int brow_nseq(int N) { return N >= 4096 ? 1 : 4096 / N; }
+__host__ __device__ constexpr int bcol_c(int N) { return N >= 4096 ? 1 : 4096 / N; }
 constexpr int BATCH_SMEM = padded_len(FFT_MAX) * 8; // 8192 elements: the largest pass tile
 constexpr long long BATCH_WAIT = 4000000000LL;           // ~2 s of SM clock
 
@@ -1304,16 +1308,16 @@ __device__ __forceinline__ void batch_run(const PropParams &P, const ChirpAxis *
     if (I.kind == BK_CHIRP) {
         chirp_body<N, BATCH_NT>(jobs[I.unit >> 1], I.unit & 1, sm, tid);
     } else if (I.kind == BK_FWD) {
-        rows_fwd_body<N, BATCH_NT, FFT_MAX / N>(P, I.unit * (FFT_MAX / N), sm, tid);
+        rows_fwd_body<N, BATCH_NT, brow_nseq(N)>(P, I.unit * brow_nseq(N), sm, tid);
     } else if (I.kind == BK_COLS) {
-        cols_body<N, BATCH_NT, FFT_MAX / N>(P, I.unit * (FFT_MAX / N), sm, tid);
+        cols_body<N, BATCH_NT, bcol_c(N)>(P, I.unit * bcol_c(N), sm, tid);
     } else {
         float lsum = 0.f;
-        rows_inv_body<N, BATCH_NT, FFT_MAX / N>(P, I.unit * (FFT_MAX / N), sm, tid, lsum);
+        rows_inv_body<N, BATCH_NT, brow_nseq(N)>(P, I.unit * brow_nseq(N), sm, tid, lsum);
     }
 }
 
-__global__ void __launch_bounds__(BATCH_NT, 1) k_batch(BatchDev D)
+__global__ void __launch_bounds__(BATCH_NT, BATCH_CTAS_PER_SM) k_batch(BatchDev D)
 {
     extern __shared__ float2 sm[];
     __shared__ int s_item, s_ok;
@@ -1429,8 +1433,8 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
     size_t n_items_max = 0;
     for (auto &F : plan->fields) {
         const int NX = 2 * F.nx, NY = 2 * F.ny;
-        const int rows = (F.ny + FFT_MAX / NX - 1) / (FFT_MAX / NX);
-        const int cols = (NX + FFT_MAX / NY - 1) / (FFT_MAX / NY);
+        const int rows = (F.ny + brow_nseq(NX) - 1) / brow_nseq(NX);
+        const int cols = (NX + bcol_c(NY) - 1) / bcol_c(NY);
         n_items_max += 4 + 2 * rows + cols;
     }
     const size_t offI = o; o += align_up(sizeof(BatchItem) * n_items_max, 256);
@@ -1481,12 +1485,12 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
             const olg_field &F = plan->fields[i];
             const int NX = 2 * F.nx, NY = 2 * F.ny;
             if (kind == BK_COLS) {
-                const int C = FFT_MAX / NY, units = (NX + C - 1) / C;
+                const int C = bcol_c(NY), units = (NX + C - 1) / C;
                 for (int u = 0; u < units; u += BATCH_UNITS_PER_ITEM)
                     items.push_back({i, kind, u, NY, std::min(BATCH_UNITS_PER_ITEM, units - u)});
                 target[3 * i + 2] = units;
             } else {
-                const int R = FFT_MAX / NX, units = (F.ny + R - 1) / R;
+                const int R = brow_nseq(NX), units = (F.ny + R - 1) / R;
                 for (int u = 0; u < units; u += BATCH_UNITS_PER_ITEM)
                     items.push_back({i, kind, u, NX, std::min(BATCH_UNITS_PER_ITEM, units - u)});
                 if (kind == BK_FWD) target[3 * i + 1] = units;
@@ -1521,7 +1525,7 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
     plan->counters_bytes = sizeof(int) * 3 * n_fields;
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, plan->dev);
-    plan->grid = nsm > 0 ? nsm : 1;
+    plan->grid = (nsm > 0 ? nsm : 1) * BATCH_CTAS_PER_SM;
     e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, BATCH_SMEM);
     if (e != cudaSuccess) {
         cudaFree(plan->mem);

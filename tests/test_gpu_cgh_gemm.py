@@ -1,7 +1,8 @@
 """GPU parity: the split-FP16 tensor-core (tcgen05) Fresnel CGH against the FP64
-oracle and against the FP32 direct kernel.  Gate for this path: relative
-L2 <= 1e-3 against FP64 (the tensor cores' f32 accumulation is the limiting
-term, not the 22-bit operand split)."""
+oracle and against the FP32 direct kernel.  The gate stated for this path is
+relative L2 <= 1e-3 against FP64; with the operands split into f16 hi + lo
+(22 bits) and the tensor-core partial sums promoted into f32 registers every
+few K-blocks, the kernel holds the FP32 paths' 1e-5."""
 import numpy as np
 import pytest
 import torch
@@ -11,7 +12,7 @@ import openol_gb300 as og
 from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
-TOL = 1e-3
+TOL = 1e-5
 
 
 def host(t):
