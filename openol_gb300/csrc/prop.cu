@@ -1257,11 +1257,11 @@ extern "C" int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, doubl
 // bodies as the single-call kernels, then publishes its completion.
 namespace olg {
 
-constexpr int BATCH_NT = 256;
-constexpr int BATCH_CTAS_PER_SM = 2;
-// rows per row unit and columns per column tile (>= 4096 elements, 8192 for N = 8192)
-__host__ __device__ constexpr int brow_nseq(int N) { return N >= 4096 ? 1 : 4096 / N; }
-__host__ __device__ constexpr int bcol_c(int N) { return N >= 4096 ? 1 : 4096 / N; }
+constexpr int BATCH_NT = 512;
+constexpr int BATCH_CTAS_PER_SM = 1;
+// rows per row unit and columns per column tile: 8192 elements per unit
+__host__ __device__ constexpr int brow_nseq(int N) { return FFT_MAX / N; }
+__host__ __device__ constexpr int bcol_c(int N) { return FFT_MAX / N; }
 constexpr int BATCH_SMEM = padded_len(FFT_MAX) * 8; // 8192 elements: the largest pass tile
 constexpr long long BATCH_WAIT = 4000000000LL;           // ~2 s of SM clock
 
