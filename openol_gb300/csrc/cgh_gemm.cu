@@ -16,7 +16,7 @@
 //
 // k_cgh_gemm_prep  per point, FP64: expansion coefficients of the x / y phases
 // k_cgh_gemm_ops   builds A_hi/A_lo/B_hi/B_lo (f16, K-contiguous, zero padded),
-//                  phases range-reduced exactly (frac_mul), sincospif
+//                  phases range-reduced exactly (frac_mul), MUFU sin/cos
 // k_cgh_gemm       warp-specialised tcgen05 GEMM: warp 0 issues TMA loads into a
 //                  4-stage ring (128 x 64 A and 256 x 64 B f16 tiles, 128-byte
 //                  swizzle), warp 1 owns TMEM (two 256-column f32 accumulators)
@@ -87,61 +87,66 @@ __device__ __forceinline__ void split2(float v, __half &hi, __half &lo)
     lo = __float2half_rn(v - __half2float(hi));
 }
 
-// grid.y = row block of (N rows of B, then M rows of A); x = point index
+// grid.y = operand row (N rows of B, then M rows of A); x = pair of points.
+// Each thread forms two points' entries and writes them with 8-byte stores.
+// Phases are reduced exactly to [-0.5, 0.5] cycles (frac_mul on the FP64
+// coefficients) before the MUFU sin/cos, whose error there (~4e-7) is below
+// the f16 hi + lo representation (2^-22 relative).
+__device__ __forceinline__ void ops_entry(const GemmOps &G, int j, bool isB, int r, float &re, float &im)
+{
+    if (j >= G.n) {
+        re = im = 0.f;
+        return;
+    }
+    const PointCoef c = G.coef[j];
+    float s, co;
+    if (isB) {
+        const float w = (float)r;
+        const float cyc = frac_mul(c.ax_hi, c.ax_lo, w * w) - frac_mul(c.bx_hi, c.bx_lo, w) + c.gx;
+        __sincosf(6.283185307179586f * wrap_cycles(cyc), &s, &co);
+        re = co;
+        im = s;
+    } else {
+        const float h = (float)(r - G.nx);
+        const float cyc = frac_mul(c.ay_hi, c.ay_lo, h * h) - frac_mul(c.by_hi, c.by_lo, h) + c.gy;
+        __sincosf(6.283185307179586f * wrap_cycles(cyc), &s, &co);
+        re = c.cr * co - c.ci * s;
+        im = c.cr * s + c.ci * co;
+    }
+}
+
 __global__ void k_cgh_gemm_ops(GemmOps G)
 {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x; // point index (pairs of K columns)
-    const int r = blockIdx.y;                            // 0..nx-1: B row w; nx..nx+ny-1: A rows 2h, 2h+1
-    if (2 * j >= G.kp) return;
-    __half2 hi0, lo0, hi1, lo1;
+    const int jp = blockIdx.x * blockDim.x + threadIdx.x; // pair of points: j = 2 jp, 2 jp + 1
+    const int r = blockIdx.y;
+    if (4 * jp >= G.kp) return;
     const bool isB = r < G.nx;
-    if (j >= G.n) {
-        hi0 = lo0 = hi1 = lo1 = __floats2half2_rn(0.f, 0.f);
-    } else {
-        const PointCoef c = G.coef[j];
-        float re, im;
-        if (isB) {
-            const float w = (float)r;
-            const float cyc = frac_mul(c.ax_hi, c.ax_lo, w * w) - frac_mul(c.bx_hi, c.bx_lo, w) + c.gx;
-            sincospif(2.0f * wrap_cycles(cyc), &im, &re);
-        } else {
-            const float h = (float)(r - G.nx);
-            const float cyc = frac_mul(c.ay_hi, c.ay_lo, h * h) - frac_mul(c.by_hi, c.by_lo, h) + c.gy;
-            float s, co;
-            sincospif(2.0f * wrap_cycles(cyc), &s, &co);
-            re = c.cr * co - c.ci * s;
-            im = c.cr * s + c.ci * co;
-        }
-        __half h0, l0, h1, l1;
-        if (isB) {
-            split2(re, h0, l0);
-            split2(im, h1, l1);
-            hi0 = __halves2half2(h0, h1);
-            lo0 = __halves2half2(l0, l1);
-        } else {
-            // row 2h: [re, -im], row 2h+1: [im, re]
-            __half hr, lr, hm, lm, hmn, lmn;
-            split2(re, hr, lr);
-            split2(im, hm, lm);
-            hmn = __hneg(hm);
-            lmn = __hneg(lm);
-            hi0 = __halves2half2(hr, hmn);
-            lo0 = __halves2half2(lr, lmn);
-            hi1 = __halves2half2(hm, hr);
-            lo1 = __halves2half2(lm, lr);
-        }
-    }
+    float re0, im0, re1, im1;
+    ops_entry(G, 2 * jp, isB, r, re0, im0);
+    ops_entry(G, 2 * jp + 1, isB, r, re1, im1);
+    __half hr0, lr0, hm0, lm0, hr1, lr1, hm1, lm1;
+    split2(re0, hr0, lr0);
+    split2(im0, hm0, lm0);
+    split2(re1, hr1, lr1);
+    split2(im1, hm1, lm1);
+    auto pack = [](__half a, __half b, __half c, __half d) {
+        uint2 u;
+        u.x = (uint32_t)__half_as_ushort(a) | ((uint32_t)__half_as_ushort(b) << 16);
+        u.y = (uint32_t)__half_as_ushort(c) | ((uint32_t)__half_as_ushort(d) << 16);
+        return u;
+    };
     if (isB) {
-        const size_t o = (size_t)r * G.kp + 2 * j;
-        *reinterpret_cast<__half2 *>(G.b_hi + o) = hi0;
-        *reinterpret_cast<__half2 *>(G.b_lo + o) = lo0;
+        const size_t o = (size_t)r * G.kp + 4 * jp;
+        *reinterpret_cast<uint2 *>(G.b_hi + o) = pack(hr0, hm0, hr1, hm1);
+        *reinterpret_cast<uint2 *>(G.b_lo + o) = pack(lr0, lm0, lr1, lm1);
     } else {
+        // row 2h: [re, -im] per point, row 2h + 1: [im, re]
         const int h = r - G.nx;
-        const size_t o0 = (size_t)(2 * h) * G.kp + 2 * j, o1 = o0 + G.kp;
-        *reinterpret_cast<__half2 *>(G.a_hi + o0) = hi0;
-        *reinterpret_cast<__half2 *>(G.a_lo + o0) = lo0;
-        *reinterpret_cast<__half2 *>(G.a_hi + o1) = hi1;
-        *reinterpret_cast<__half2 *>(G.a_lo + o1) = lo1;
+        const size_t o0 = (size_t)(2 * h) * G.kp + 4 * jp, o1 = o0 + G.kp;
+        *reinterpret_cast<uint2 *>(G.a_hi + o0) = pack(hr0, __hneg(hm0), hr1, __hneg(hm1));
+        *reinterpret_cast<uint2 *>(G.a_lo + o0) = pack(lr0, __hneg(lm0), lr1, __hneg(lm1));
+        *reinterpret_cast<uint2 *>(G.a_hi + o1) = pack(hm0, hr0, hm1, hr1);
+        *reinterpret_cast<uint2 *>(G.a_lo + o1) = pack(lm0, lr0, lm1, lr1);
     }
 }
 
@@ -418,7 +423,7 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
         if (int rc = check_launch("k_cgh_gemm_prep")) return rc;
     }
     if (!reuse) {
-        dim3 og((kp / 2 + 127) / 128, nx + ny);
+        dim3 og((kp / 4 + 127) / 128, nx + ny);
         k_cgh_gemm_ops<<<og, 128, 0, st>>>(G);
         count_launch();
         if (int rc = check_launch("k_cgh_gemm_ops")) return rc;
