@@ -87,66 +87,58 @@ __device__ __forceinline__ void split2(float v, __half &hi, __half &lo)
     lo = __float2half_rn(v - __half2float(hi));
 }
 
-// grid.y = operand row (N rows of B, then M rows of A); x = pair of points.
-// Each thread forms two points' entries and writes them with 8-byte stores.
+// grid.x = point j (one per thread), grid.y = block of OPS_ROWS operand rows
+// (the nx rows of B, then the ny row pairs of A).  Each thread keeps its
+// point's coefficients in registers across the rows; for each row a warp
+// writes 32 consecutive points (128 contiguous bytes per f16 plane).
 // Phases are reduced exactly to [-0.5, 0.5] cycles (frac_mul on the FP64
 // coefficients) before the MUFU sin/cos, whose error there (~4e-7) is below
 // the f16 hi + lo representation (2^-22 relative).
-__device__ __forceinline__ void ops_entry(const GemmOps &G, int j, bool isB, int r, float &re, float &im)
-{
-    if (j >= G.n) {
-        re = im = 0.f;
-        return;
-    }
-    const PointCoef c = G.coef[j];
-    float s, co;
-    if (isB) {
-        const float w = (float)r;
-        const float cyc = frac_mul(c.ax_hi, c.ax_lo, w * w) - frac_mul(c.bx_hi, c.bx_lo, w) + c.gx;
-        __sincosf(6.283185307179586f * wrap_cycles(cyc), &s, &co);
-        re = co;
-        im = s;
-    } else {
-        const float h = (float)(r - G.nx);
-        const float cyc = frac_mul(c.ay_hi, c.ay_lo, h * h) - frac_mul(c.by_hi, c.by_lo, h) + c.gy;
-        __sincosf(6.283185307179586f * wrap_cycles(cyc), &s, &co);
-        re = c.cr * co - c.ci * s;
-        im = c.cr * s + c.ci * co;
-    }
-}
+constexpr int OPS_ROWS = 16;
 
 __global__ void k_cgh_gemm_ops(GemmOps G)
 {
-    const int jp = blockIdx.x * blockDim.x + threadIdx.x; // pair of points: j = 2 jp, 2 jp + 1
-    const int r = blockIdx.y;
-    if (4 * jp >= G.kp) return;
-    const bool isB = r < G.nx;
-    float re0, im0, re1, im1;
-    ops_entry(G, 2 * jp, isB, r, re0, im0);
-    ops_entry(G, 2 * jp + 1, isB, r, re1, im1);
-    __half hr0, lr0, hm0, lm0, hr1, lr1, hm1, lm1;
-    split2(re0, hr0, lr0);
-    split2(im0, hm0, lm0);
-    split2(re1, hr1, lr1);
-    split2(im1, hm1, lm1);
-    auto pack = [](__half a, __half b, __half c, __half d) {
-        uint2 u;
-        u.x = (uint32_t)__half_as_ushort(a) | ((uint32_t)__half_as_ushort(b) << 16);
-        u.y = (uint32_t)__half_as_ushort(c) | ((uint32_t)__half_as_ushort(d) << 16);
-        return u;
-    };
-    if (isB) {
-        const size_t o = (size_t)r * G.kp + 4 * jp;
-        *reinterpret_cast<uint2 *>(G.b_hi + o) = pack(hr0, hm0, hr1, hm1);
-        *reinterpret_cast<uint2 *>(G.b_lo + o) = pack(lr0, lm0, lr1, lm1);
-    } else {
-        // row 2h: [re, -im] per point, row 2h + 1: [im, re]
-        const int h = r - G.nx;
-        const size_t o0 = (size_t)(2 * h) * G.kp + 4 * jp, o1 = o0 + G.kp;
-        *reinterpret_cast<uint2 *>(G.a_hi + o0) = pack(hr0, __hneg(hm0), hr1, __hneg(hm1));
-        *reinterpret_cast<uint2 *>(G.a_lo + o0) = pack(lr0, __hneg(lm0), lr1, __hneg(lm1));
-        *reinterpret_cast<uint2 *>(G.a_hi + o1) = pack(hm0, hr0, hm1, hr1);
-        *reinterpret_cast<uint2 *>(G.a_lo + o1) = pack(lm0, lr0, lm1, lr1);
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (2 * j >= G.kp) return;
+    const bool live = j < G.n;
+    PointCoef c{};
+    if (live) c = G.coef[j];
+    const int r0 = blockIdx.y * OPS_ROWS, r1 = min(r0 + OPS_ROWS, G.nx + G.ny);
+    for (int r = r0; r < r1; ++r) {
+        const bool isB = r < G.nx;
+        float re = 0.f, im = 0.f;
+        if (live) {
+            float s, co;
+            if (isB) {
+                const float w = (float)r;
+                const float cyc = frac_mul(c.ax_hi, c.ax_lo, w * w) - frac_mul(c.bx_hi, c.bx_lo, w) + c.gx;
+                __sincosf(6.283185307179586f * wrap_cycles(cyc), &s, &co);
+                re = co;
+                im = s;
+            } else {
+                const float h = (float)(r - G.nx);
+                const float cyc = frac_mul(c.ay_hi, c.ay_lo, h * h) - frac_mul(c.by_hi, c.by_lo, h) + c.gy;
+                __sincosf(6.283185307179586f * wrap_cycles(cyc), &s, &co);
+                re = c.cr * co - c.ci * s;
+                im = c.cr * s + c.ci * co;
+            }
+        }
+        __half hr, lr, hm, lm;
+        split2(re, hr, lr);
+        split2(im, hm, lm);
+        if (isB) {
+            const size_t o = (size_t)r * G.kp + 2 * j;
+            *reinterpret_cast<__half2 *>(G.b_hi + o) = __halves2half2(hr, hm);
+            *reinterpret_cast<__half2 *>(G.b_lo + o) = __halves2half2(lr, lm);
+        } else {
+            // row 2h: [re, -im] per point, row 2h + 1: [im, re]
+            const int h = r - G.nx;
+            const size_t o0 = (size_t)(2 * h) * G.kp + 2 * j, o1 = o0 + G.kp;
+            *reinterpret_cast<__half2 *>(G.a_hi + o0) = __halves2half2(hr, __hneg(hm));
+            *reinterpret_cast<__half2 *>(G.a_lo + o0) = __halves2half2(lr, __hneg(lm));
+            *reinterpret_cast<__half2 *>(G.a_hi + o1) = __halves2half2(hm, hr);
+            *reinterpret_cast<__half2 *>(G.a_lo + o1) = __halves2half2(lm, lr);
+        }
     }
 }
 
@@ -423,7 +415,7 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
         if (int rc = check_launch("k_cgh_gemm_prep")) return rc;
     }
     if (!reuse) {
-        dim3 og((kp / 4 + 127) / 128, nx + ny);
+        dim3 og((kp / 2 + 127) / 128, (nx + ny + OPS_ROWS - 1) / OPS_ROWS);
         k_cgh_gemm_ops<<<og, 128, 0, st>>>(G);
         count_launch();
         if (int rc = check_launch("k_cgh_gemm_ops")) return rc;
