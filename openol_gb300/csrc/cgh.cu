@@ -9,16 +9,18 @@
 // to [-0.5, 0.5] cycles, and each pixel adds a small local expansion in FP32:
 //   Fresnel: cycles(w,h) = c0 + ax dw + ay dh + bx dw^2 + by dh^2   (exact: quadratic)
 //   exact:   x = (r^2 - r0^2) / r0^2 = ax dw + ay dh + bx dw^2 + by dh^2,
-//            cycles = c0 + R (x/2 - x^2/8 + x^3/16),  amplitude = A (1 - x/2 + 3x^2/8)
-// with (dw, dh) the pixel offset from the tile centre (|d| <= 7.5).  The
+//            cycles = c0 + R (x/2 - x^2/8 + x^3/16),  amplitude = A (1 - x/2)
+// with (dw, dh) the pixel offset from the subtile centre (|d| <= 7.5).  The
 // series is used while |x| <= 2e-3 for every point of a batch (truncation
 // < 1e-7 cycles); otherwise the batch uses the closed form
-// R x / (1 + sqrt(1 + x)).  Per term: 2 MUFU (sin, cos) + ~10 FP32 ops.
+// R x / (1 + sqrt(1 + x)).  Per term: 2 MUFU (sin, cos) and about 12 other
+// instructions (exact form), 9 (Fresnel form), two pixels per paired
+// FP32 instruction (fma/add/mul .f32x2).
 //
-// CTA = 256 threads over a 16 x 32 pixel tile (two 16 x 16 subtiles, each
-// with its own anchor), 2 pixels per thread; 256 points per batch, thread t
-// preparing point t's constants for both subtiles.  Summation is sequential
-// over points (deterministic), in per-batch partial sums.
+// CTA = 256 threads over a 32 x 32 pixel tile (four 16 x 16 subtiles, each
+// with its own anchor), 4 pixels per thread; 128 points per batch.
+// Summation is sequential over points (deterministic), in per-batch partial
+// sums.
 #include <cmath>
 #include <cstdio>
 
@@ -37,19 +39,25 @@ struct CghParams {
     int accumulate;
 };
 
-constexpr int CGH_BATCH = 256;
+constexpr int CGH_BATCH = 128;
 constexpr float SERIES_XMAX = 2e-3f;
 
-// per (subtile, point) constants
+// Per (subtile, point) record, three float4 in shared memory:
+//   [c0 ax ay bx] [by h1 h2 h3] [A Ah R -]
+// Fresnel: cycles = c0 + ax dw + ay dh + bx dw^2 + by dh^2, amplitude A,
+//          stored in the h1 slot (two float4 per record are read).
+// exact:   x as above without c0, cycles = c0 + x (h1 + x (h2 + x h3)) with
+//          h1 = R/2, h2 = -R/8, h3 = R/16, amplitude A + Ah x (Ah = -A/2; the
+//          dropped 3x^2/8 is below 1.5e-6 relative while |x| <= 2e-3).
 struct Sub {
-    float c0, ax, ay, bx, by, R, A, pad;
+    float c0, ax, ay, bx, by, h1, h2, h3, A, Ah, R, pad;
 };
 
 template <bool EXACT>
 __device__ __forceinline__ Sub prep_sub(const CghParams &P, float x, float y, float z, float a, float ph, float wc,
                                         float hc)
 {
-    Sub s;
+    Sub s{};
     const df2 Xc = df_add(df_two_prod(P.px_hi, wc), df2{P.px_lo * wc, 0.f});
     const df2 Yc = df_add(df_two_prod(P.py_hi, hc), df2{P.py_lo * hc, 0.f});
     const df2 Dx = df_add_f(Xc, -x);
@@ -67,7 +75,6 @@ __device__ __forceinline__ Sub prep_sub(const CghParams &P, float x, float y, fl
         s.ay = 2.0f * Dy.hi * py * k;
         s.bx = px * px * k;
         s.by = py * py * k;
-        s.R = 0.f;
         s.A = a;
     } else {
         const df2 r02 = df_add(rho2, df_two_prod(z, z));
@@ -79,9 +86,12 @@ __device__ __forceinline__ Sub prep_sub(const CghParams &P, float x, float y, fl
         s.bx = px * px * inv;
         s.by = py * py * inv;
         s.R = r0.hi * P.il_hi;
+        s.h1 = 0.5f * s.R;
+        s.h2 = -0.125f * s.R;
+        s.h3 = 0.0625f * s.R;
         s.A = a / r0.hi;
+        s.Ah = -0.5f * s.A;
     }
-    s.pad = 0.f;
     return s;
 }
 
@@ -90,81 +100,137 @@ __device__ __forceinline__ float xbound(const Sub &s)
     return fabsf(s.ax) * 7.5f + fabsf(s.ay) * 7.5f + (fabsf(s.bx) + fabsf(s.by)) * 56.25f;
 }
 
+// t - round(t) with the rounding done by adding and removing 1.5 * 2^23
+// (round to nearest even, exact for |t| < 2^22): plain FP32 adds.
+__device__ __forceinline__ float wrap_add(float t)
+{
+    const float r = __fsub_rn(__fadd_rn(t, 12582912.0f), 12582912.0f);
+    return t - r;
+}
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
+// Two terms at once on the paired FP32 pipe: phases cyc (cycles) and
+// amplitudes amp for the pixels of lanes x and y; ba += amp.x e^{2 pi i cyc.x},
+// bb += amp.y e^{2 pi i cyc.y}.  Same roundings as the scalar form.
+__device__ __forceinline__ void accumulate_pair(float2 &ba, float2 &bb, float2 amp, float2 cyc)
+{
+    const float2 r = __fadd2_rn(__fadd2_rn(cyc, f2(12582912.0f)), f2(-12582912.0f));
+    const float2 a = __fmul2_rn(__ffma2_rn(r, f2(-1.0f), cyc), f2(6.283185307179586f));
+    float s0, c0, s1, c1;
+    __sincosf(a.x, &s0, &c0);
+    __sincosf(a.y, &s1, &c1);
+    ba = __ffma2_rn(f2(amp.x), make_float2(c0, s0), ba);
+    bb = __ffma2_rn(f2(amp.y), make_float2(c1, s1), bb);
+}
+
+// CTA = 256 threads over a 32 x 32 pixel tile: four 16 x 16 subtiles (one
+// anchor each), two warps per subtile, each thread one column of 4 pixels
+// (rows tq, tq + 4, tq + 8, tq + 12 of its subtile).  The dw terms of x and
+// the record loads are shared by the 4 pixels.
 template <bool EXACT>
 __global__ void __launch_bounds__(256) k_cgh(CghParams P)
 {
-    __shared__ float4 sp[CGH_BATCH][4]; // [point][sub0 c0..by | sub0 R,A | sub1 ... ]
+    __shared__ float4 sp[4][CGH_BATCH][3];
     const int tid = threadIdx.x;
-    const int tx = tid & 15, ty = tid >> 4;
-    const int w0 = blockIdx.x * 16, h0 = blockIdx.y * 32;
-    const float dw = (float)tx - 7.5f, dh = (float)ty - 7.5f;
-    const float dw2 = dw * dw, dh2 = dh * dh;
-    const float wc = (float)w0 + 7.5f, hc0 = (float)h0 + 7.5f, hc1 = (float)h0 + 23.5f;
-    float2 acc0 = make_float2(0.f, 0.f), acc1 = acc0;
+    const int sub = tid >> 6, l = tid & 63;
+    const int tx = l & 15, tq = l >> 4;
+    const int w0 = blockIdx.x * 32, h0 = blockIdx.y * 32;
+    const float dw = (float)tx - 7.5f, dw2 = dw * dw;
+    float dh[4], dh2[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        dh[k] = (float)(tq + 4 * k) - 7.5f;
+        dh2[k] = dh[k] * dh[k];
+    }
+    // pixel pairs (i, i + 2) share one paired FP32 instruction per step
+    const float2 dhp[2] = {make_float2(dh[0], dh[2]), make_float2(dh[1], dh[3])};
+    const float2 dh2p[2] = {make_float2(dh2[0], dh2[2]), make_float2(dh2[1], dh2[3])};
+    float2 acc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] = make_float2(0.f, 0.f);
 
+    // preparation: thread t builds point (t mod 128) for subtiles 2 (t / 128) and 2 (t / 128) + 1
+    const int pp = tid & (CGH_BATCH - 1), ps = 2 * (tid >> 7);
     for (int base = 0; base < P.n; base += CGH_BATCH) {
-        const int j = base + tid;
-        Sub s0{}, s1{};
+        const int j = base + pp;
         float xb = 0.f;
-        if (j < P.n) {
-            const float x = __ldg(P.pts + 3 * j), y = __ldg(P.pts + 3 * j + 1), z = __ldg(P.pts + 3 * j + 2);
-            const float a = P.amp ? __ldg(P.amp + j) : 1.0f;
-            const float ph = P.ph0 ? __ldg(P.ph0 + j) : 0.0f;
-            s0 = prep_sub<EXACT>(P, x, y, z, a, ph, wc, hc0);
-            s1 = prep_sub<EXACT>(P, x, y, z, a, ph, wc, hc1);
-            if (EXACT) xb = fmaxf(xbound(s0), xbound(s1));
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int s = ps + q;
+            Sub r{};
+            if (j < P.n) {
+                const float x = __ldg(P.pts + 3 * j), y = __ldg(P.pts + 3 * j + 1), z = __ldg(P.pts + 3 * j + 2);
+                const float a = P.amp ? __ldg(P.amp + j) : 1.0f;
+                const float ph = P.ph0 ? __ldg(P.ph0 + j) : 0.0f;
+                r = prep_sub<EXACT>(P, x, y, z, a, ph, (float)(w0 + 16 * (s & 1)) + 7.5f,
+                                    (float)(h0 + 16 * (s >> 1)) + 7.5f);
+                if (EXACT) xb = fmaxf(xb, xbound(r));
+            }
+            sp[s][pp][0] = make_float4(r.c0, r.ax, r.ay, r.bx);
+            sp[s][pp][1] = EXACT ? make_float4(r.by, r.h1, r.h2, r.h3) : make_float4(r.by, r.A, 0.f, 0.f);
+            sp[s][pp][2] = make_float4(r.A, r.Ah, r.R, 0.f);
         }
-        sp[tid][0] = make_float4(s0.c0, s0.ax, s0.ay, s0.bx);
-        sp[tid][1] = make_float4(s0.by, s0.R, s0.A, 0.f);
-        sp[tid][2] = make_float4(s1.c0, s1.ax, s1.ay, s1.bx);
-        sp[tid][3] = make_float4(s1.by, s1.R, s1.A, 0.f);
         const int use_closed = EXACT ? __syncthreads_or(xb > SERIES_XMAX) : (__syncthreads(), 0);
         const int cnt = min(CGH_BATCH, P.n - base);
-        float2 b0 = make_float2(0.f, 0.f), b1 = b0;
-#pragma unroll 4
-        for (int k = 0; k < cnt; ++k) {
-            const float4 p0 = sp[k][0], q0 = sp[k][1], p1 = sp[k][2], q1 = sp[k][3];
-            if (!EXACT) {
-                float c = fmaf(p0.y, dw, fmaf(p0.z, dh, fmaf(p0.w, dw2, fmaf(q0.x, dh2, p0.x))));
-                float2 e = cis_cycles(wrap_cycles(c));
-                b0.x = fmaf(q0.z, e.x, b0.x);
-                b0.y = fmaf(q0.z, e.y, b0.y);
-                c = fmaf(p1.y, dw, fmaf(p1.z, dh, fmaf(p1.w, dw2, fmaf(q1.x, dh2, p1.x))));
-                e = cis_cycles(wrap_cycles(c));
-                b1.x = fmaf(q1.z, e.x, b1.x);
-                b1.y = fmaf(q1.z, e.y, b1.y);
-            } else {
+        float2 b[4];
 #pragma unroll
-                for (int sidx = 0; sidx < 2; ++sidx) {
-                    const float4 p = sidx ? p1 : p0, q = sidx ? q1 : q0;
-                    const float x = fmaf(p.y, dw, fmaf(p.z, dh, fmaf(p.w, dw2, q.x * dh2)));
-                    float cyc, amp;
-                    if (!use_closed) {
-                        const float poly = fmaf(x, fmaf(x, 0.0625f, -0.125f), 0.5f);
-                        cyc = fmaf(q.y * x, poly, p.x);
-                        amp = q.z * fmaf(x, fmaf(x, 0.375f, -0.5f), 1.0f);
-                    } else {
-                        const float sq = sqrtf(1.0f + x);
-                        cyc = fmaf(q.y, x / (1.0f + sq), p.x);
-                        amp = q.z / sq;
-                    }
-                    const float2 e = cis_cycles(wrap_cycles(cyc));
-                    float2 &b = sidx ? b1 : b0;
-                    b.x = fmaf(amp, e.x, b.x);
-                    b.y = fmaf(amp, e.y, b.y);
+        for (int k = 0; k < 4; ++k) b[k] = make_float2(0.f, 0.f);
+        const float4 (*rec)[3] = sp[sub];
+        if (!EXACT) {
+#pragma unroll 2
+            for (int k = 0; k < cnt; ++k) {
+                const float4 r0 = rec[k][0], r1 = rec[k][1];
+                const float u = fmaf(r0.w, dw2, fmaf(r0.y, dw, r0.x));
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    const float2 c = __ffma2_rn(f2(r1.x), dh2p[i], __ffma2_rn(f2(r0.z), dhp[i], f2(u)));
+                    accumulate_pair(b[i], b[i + 2], f2(r1.y), c);
+                }
+            }
+        } else if (!use_closed) {
+#pragma unroll 2
+            for (int k = 0; k < cnt; ++k) {
+                const float4 r0 = rec[k][0], r1 = rec[k][1], r2 = rec[k][2];
+                const float u = fmaf(r0.w, dw2, r0.y * dw);
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    const float2 x = __ffma2_rn(f2(r1.x), dh2p[i], __ffma2_rn(f2(r0.z), dhp[i], f2(u)));
+                    const float2 cyc =
+                        __ffma2_rn(x, __ffma2_rn(x, __ffma2_rn(x, f2(r1.w), f2(r1.z)), f2(r1.y)), f2(r0.x));
+                    accumulate_pair(b[i], b[i + 2], __ffma2_rn(f2(r2.y), x, f2(r2.x)), cyc);
+                }
+            }
+        } else {
+            for (int k = 0; k < cnt; ++k) {
+                const float4 r0 = rec[k][0], r2 = rec[k][2];
+                const float4 r1 = rec[k][1];
+                const float u = fmaf(r0.w, dw2, r0.y * dw);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float x = fmaf(r1.x, dh2[i], fmaf(r0.z, dh[i], u));
+                    const float sq = sqrtf(1.0f + x);
+                    const float cyc = fmaf(r2.z, x / (1.0f + sq), r0.x);
+                    const float amp = r2.x / sq;
+                    const float2 e = cis_cycles(wrap_add(cyc));
+                    b[i].x = fmaf(amp, e.x, b[i].x);
+                    b[i].y = fmaf(amp, e.y, b[i].y);
                 }
             }
         }
-        acc0.x += b0.x; acc0.y += b0.y;
-        acc1.x += b1.x; acc1.y += b1.y;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            acc[k].x += b[k].x;
+            acc[k].y += b[k].y;
+        }
         __syncthreads();
     }
-    const int w = w0 + tx;
+    const int w = w0 + 16 * (sub & 1) + tx;
 #pragma unroll
-    for (int sidx = 0; sidx < 2; ++sidx) {
-        const int h = h0 + ty + 16 * sidx;
+    for (int k = 0; k < 4; ++k) {
+        const int h = h0 + 16 * (sub >> 1) + tq + 4 * k;
         if (w >= P.nx || h >= P.ny) continue;
-        const float2 a = sidx ? acc1 : acc0;
+        const float2 a = acc[k];
         const size_t i = (size_t)h * P.nx + w;
         if (P.U) {
             float2 v = a;
@@ -197,7 +263,7 @@ static int cgh_launch(bool exact, const float *points, const float *amp, const f
     P.U = (float2 *)U;
     P.phase_out = phase_out;
     P.accumulate = (flags & OLG_ACCUMULATE) ? 1 : 0;
-    dim3 grid((nx + 15) / 16, (ny + 31) / 32);
+    dim3 grid((nx + 31) / 32, (ny + 31) / 32);
     cudaStream_t st = (cudaStream_t)stream;
     if (exact) k_cgh<true><<<grid, 256, 0, st>>>(P);
     else k_cgh<false><<<grid, 256, 0, st>>>(P);

@@ -83,6 +83,36 @@ def test_cgh_edges(form, shape, n):
         assert rel_l2(host(U), ref) < TOL
 
 
+def test_cgh_exact_near_points_closed_form():
+    """Points 0.6-0.9 mm from a 48 x 48 hologram (p = 2 um), inside the cone
+    that the pitch samples without aliasing.  |x| over the 16 x 16 subtiles
+    exceeds the series bound (2e-3) in every 32 x 32 CTA tile, so every batch
+    takes the closed-form branch; the host recomputes that bound below."""
+    ny, nx, p, lam = 48, 48, 2e-6, 633e-9
+    rng = np.random.default_rng(7)
+    n = 300
+    c = np.array([nx / 2 * p, ny / 2 * p])
+    lat = c + (rng.random((n, 2)) - 0.5) * 20e-6
+    pts = np.concatenate([lat, (6e-4 + rng.random(n) * 3e-4)[:, None]], 1).astype(np.float32)
+    amp = (0.5 + 0.5 * rng.random(n)).astype(np.float32)
+    P = pts.astype(np.float64)
+    for h0 in range(0, ny, 32):
+        for w0 in range(0, nx, 32):
+            xb = 0.0
+            for sw in (0, 1):
+                for sh in (0, 1):
+                    dx = p * (w0 + 16 * sw + 7.5) - P[:, 0]
+                    dy = p * (h0 + 16 * sh + 7.5) - P[:, 1]
+                    r2 = dx * dx + dy * dy + P[:, 2] ** 2
+                    b = (np.abs(2 * dx * p / r2) + np.abs(2 * dy * p / r2)) * 7.5 + 2 * p * p / r2 * 56.25
+                    xb = max(xb, b.max())
+            assert xb > 2.5e-3, (h0, w0, xb)
+    U = torch.zeros((ny, nx), dtype=torch.complex64, device="cuda")
+    og.cgh_exact(og.gObject(pts), U, ny=ny, nx=nx, py=p, px=p, lam=lam, amp=torch.from_numpy(amp).cuda())
+    ref = O.cgh_exact(pts.astype(np.float64), ny, nx, p, p, lam, amp=amp.astype(np.float64))
+    assert rel_l2(host(U), ref) < TOL
+
+
 def test_cgh_reduction_accumulates():
     rng = np.random.default_rng(4)
     pts = np.stack([rng.random(40) * 32 * 8e-6, rng.random(40) * 32 * 8e-6, 0.02 + rng.random(40) * 0.01], 1)
