@@ -32,10 +32,23 @@
 #include "common.cuh"
 #include "fft.cuh"
 #include "fft2.cuh"
+#include "fftp.cuh"
 
 namespace olg {
 
+// Programmatic dependent launch: a pass lets the next one launch as soon as all
+// of its CTAs are running, and waits for the previous grid's completion (and
+// memory) before touching any field data.  Both are no-ops when the launch
+// carries no programmatic-serialisation attribute.
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 static __device__ float2 g_tw[FFT_MAX];
+// the same table as (c, c, s, s) for the paired-sequence passes
+static __device__ float4 g_tw4[FFT_MAX];
 
 enum : int { M_ASM = 0, M_CHIRP = 1 };
 // pre/post operation modes
@@ -114,6 +127,7 @@ __device__ __forceinline__ float2 apply_op_c(float2 v, int mode, const float2 *t
 template <int N>
 __global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_fwd(PropParams P)
 {
+    pdl_enter();
     using Cfg = RowCfg<N>;
     extern __shared__ float2 sm[];
     constexpr int SS = padded_len(N);
@@ -164,6 +178,7 @@ __global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_fwd(PropParams P)
 template <int N>
 __global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_inv(PropParams P)
 {
+    pdl_enter();
     using Cfg = RowCfg<N>;
     extern __shared__ float2 sm[];
     constexpr int SS = padded_len(N);
@@ -239,6 +254,7 @@ __device__ __forceinline__ float2 asm_tf(const PropParams &P, int fx, int fy)
 template <int N>
 __global__ void __launch_bounds__(ColCfg<N>::NT) k_cols(PropParams P)
 {
+    pdl_enter();
     using Cfg = ColCfg<N>;
     constexpr int C = Cfg::C, NT = Cfg::NT;
     extern __shared__ float2 sm[];
@@ -456,6 +472,188 @@ __device__ __forceinline__ void cols_body(const PropParams &P, int c0, float2 *s
     }
 }
 
+// ======================================================= paired passes
+// Two rows (passes 1 and 3) or two adjacent columns (pass 2) per butterfly,
+// in planar pairs on the paired FP32 pipe (fftp.cuh).  Same stages, pruning
+// and fusion as the v2 passes.
+template <int N, int NT, int NSP>
+__device__ __forceinline__ void rows_fwd_body_p(const PropParams &P, int r0, float4 *sm, int tid)
+{
+    constexpr int SS = padded_len(N), B = N / 16;
+    static_assert((NSP * B) % NT == 0, "threads must divide the butterflies");
+    constexpr int BPT = NSP * B / NT;
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + 2 * q;
+        cpair v[16];
+#pragma unroll
+        for (int r = 4; r < 12; ++r) {
+            const int w = j + (r - 4) * B;
+            const float2 x0 = h < P.ny ? load_in(P, h, w) : make_float2(0.f, 0.f);
+            const float2 x1 = h + 1 < P.ny ? load_in(P, h + 1, w) : make_float2(0.f, 0.f);
+            v[r] = cp_pack(x0, x1);
+        }
+        cp_dft16_in_mid<-1>(v);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) cp_st(sm + q * SS + pidx(j * 16 + k), v[outpos<16>(k)]);
+    }
+    __syncthreads();
+    cp_mid_stages<N, -1, NT, false, NSP>(sm, SS, g_tw4, tid);
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + 2 * q;
+        cpair v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = cp_ld(sm + q * SS + pidx(j + r * B));
+        cp_last_twiddle<N, -1>(v, j, g_tw4);
+        cp_dft<16, -1>(v);
+        if (h < P.ny) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) __stcg(P.S + (size_t)h * N + j + k * B, cp_lane0(v[outpos<16>(k)]));
+        }
+        if (h + 1 < P.ny) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) __stcg(P.S + (size_t)(h + 1) * N + j + k * B, cp_lane1(v[outpos<16>(k)]));
+        }
+    }
+}
+
+__device__ __forceinline__ void store_out(const PropParams &P, int h, int w, float2 a, float &lsum)
+{
+    const size_t i = (size_t)h * P.nx + w;
+    if (P.post_mode == OP_SEED) {
+        const float r2 = a.x * a.x + a.y * a.y - __ldg(P.target + i);
+        lsum = fmaf(r2, r2, lsum);
+        a = cscale(a, P.seed_scale * r2);
+    } else {
+        a = apply_op_c(a, P.post_mode, P.postx, P.posty, h, w, P.ny, P.nx, P.post_hlim, P.post_wlim, P.coherent);
+    }
+    if (P.accumulate) {
+        const float2 o = P.out[i];
+        a.x += o.x;
+        a.y += o.y;
+    }
+    P.out[i] = a;
+}
+
+template <int N, int NT, int NSP>
+__device__ __forceinline__ void rows_inv_body_p(const PropParams &P, int r0, float4 *sm, int tid, float &lsum)
+{
+    constexpr int SS = padded_len(N), B = N / 16;
+    constexpr int BPT = NSP * B / NT;
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + 2 * q;
+        cpair v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const float2 x0 = h < P.ny ? __ldcg(P.S + (size_t)h * N + j + r * B) : make_float2(0.f, 0.f);
+            const float2 x1 = h + 1 < P.ny ? __ldcg(P.S + (size_t)(h + 1) * N + j + r * B) : make_float2(0.f, 0.f);
+            v[r] = cp_pack(x0, x1);
+        }
+        cp_dft<16, +1>(v);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) cp_st(sm + q * SS + pidx(j * 16 + k), v[outpos<16>(k)]);
+    }
+    __syncthreads();
+    cp_mid_stages<N, +1, NT, false, NSP>(sm, SS, g_tw4, tid);
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + 2 * q;
+        cpair v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = cp_ld(sm + q * SS + pidx(j + r * B));
+        cp_last_twiddle<N, +1>(v, j, g_tw4);
+        cp_dft16_out_mid<+1>(v);
+        if (h < P.ny) {
+#pragma unroll
+            for (int k = 4; k < 12; ++k) store_out(P, h, j + (k - 4) * B, cp_lane0(v[outpos<16>(k)]), lsum);
+        }
+        if (h + 1 < P.ny) {
+#pragma unroll
+            for (int k = 4; k < 12; ++k) store_out(P, h + 1, j + (k - 4) * B, cp_lane1(v[outpos<16>(k)]), lsum);
+        }
+    }
+}
+
+template <int N, int NT, int CP>
+__device__ __forceinline__ void cols_body_p(const PropParams &P, int c0, float4 *sm, int tid)
+{
+    constexpr int B = N / 16;
+    static_assert((CP * B) % NT == 0, "threads must divide the butterflies");
+    constexpr int BPT = CP * B / NT;
+    const int NX = P.NX;
+    // forward first stage, straight from the ny stored rows (the rest is zero padding)
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, c = b % CP, j = b / CP, kx = c0 + 2 * c;
+        cpair v[16];
+#pragma unroll
+        for (int r = 4; r < 12; ++r) {
+            const float4 f = kx < NX ? __ldcg(reinterpret_cast<const float4 *>(P.S + (size_t)(j + (r - 4) * B) * NX + kx))
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+            v[r] = {make_float2(f.x, f.z), make_float2(f.y, f.w)};
+        }
+        cp_dft16_in_mid<-1>(v);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) cp_st(sm + pidx(j * 16 + k) * CP + c, v[outpos<16>(k)]);
+    }
+    __syncthreads();
+    cp_mid_stages<N, -1, NT, true, CP>(sm, 0, g_tw4, tid);
+    // forward last stage -> x T(ky, kx) -> inverse first stage, in registers
+    cpair vv[BPT][16];
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, c = b % CP, j = b / CP;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) vv[t][r] = cp_ld(sm + pidx(j + r * B) * CP + c);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, c = b % CP, j = b / CP, kx = c0 + 2 * c;
+        cp_last_twiddle<N, -1>(vv[t], j, g_tw4);
+        cp_dft<16, -1>(vv[t]);
+        cpair w[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const cpair x = vv[t][outpos<16>(k)];
+            if (kx < NX) {
+                const int ky = j + k * B;
+                const cpair T = cp_pack(tf_at(P, ky, kx, N), tf_at(P, ky, kx + 1, N));
+                w[k] = {__ffma2_rn(x.im, pneg(T.im), __fmul2_rn(x.re, T.re)),
+                        __ffma2_rn(x.re, T.im, __fmul2_rn(x.im, T.re))};
+            } else {
+                w[k] = x;
+            }
+        }
+        cp_dft<16, +1>(w);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) cp_st(sm + pidx(j * 16 + k) * CP + c, w[outpos<16>(k)]);
+    }
+    __syncthreads();
+    cp_mid_stages<N, +1, NT, true, CP>(sm, 0, g_tw4, tid);
+    // inverse last stage: only the central ny rows, back in place
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, c = b % CP, j = b / CP, kx = c0 + 2 * c;
+        cpair v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = cp_ld(sm + pidx(j + r * B) * CP + c);
+        cp_last_twiddle<N, +1>(v, j, g_tw4);
+        cp_dft16_out_mid<+1>(v);
+        if (kx < NX) {
+#pragma unroll
+            for (int k = 4; k < 12; ++k) {
+                const cpair x = v[outpos<16>(k)];
+                __stcg(reinterpret_cast<float4 *>(P.S + (size_t)(j + (k - 4) * B) * NX + kx),
+                       make_float4(x.re.x, x.im.x, x.re.y, x.im.y));
+            }
+        }
+    }
+}
+
+
 __device__ __forceinline__ void loss_reduce(float lsum, double *loss, int tid, int nt)
 {
     __shared__ float red[32];
@@ -472,43 +670,62 @@ __device__ __forceinline__ void loss_reduce(float lsum, double *loss, int tid, i
 // Launch-shape variants of the v2 passes (threads, elements per CTA, minimum
 // resident CTAs); olg_autotune_prop times them on the device and keeps the
 // fastest per FFT length.
-template <int NT_, int E_, int MINB_>
+template <int NT_, int E_, int MINB_, bool PAIRED_ = false>
 struct Shape {
     static constexpr int NT = NT_, E = E_, MINB = MINB_;
+    static constexpr bool PAIRED = PAIRED_;
 };
-// rows: E = row elements per CTA (NSEQ = E / N rows, at least one)
+// rows: E = row elements per CTA (NSEQ = E / N rows, at least one; paired
+// variants: NSEQ = E / 2N row pairs, at least one)
 template <int I> struct RowVar;
 template <> struct RowVar<0> : Shape<256, 4096, 2> {};
 template <> struct RowVar<1> : Shape<256, 4096, 4> {};
 template <> struct RowVar<2> : Shape<512, 8192, 2> {};
 template <> struct RowVar<3> : Shape<128, 2048, 4> {};
-constexpr int N_ROW_VARIANTS = 4;
-// columns: E = elements per CTA (C = E / N adjacent columns)
+template <> struct RowVar<4> : Shape<128, 4096, 4, true> {};
+template <> struct RowVar<5> : Shape<256, 8192, 2, true> {};
+template <> struct RowVar<6> : Shape<512, 16384, 1, true> {};
+template <> struct RowVar<7> : Shape<64, 2048, 8, true> {};
+constexpr int N_ROW_VARIANTS = 8;
+// columns: E = elements per CTA (C = E / N adjacent columns; paired variants:
+// C = E / 2N adjacent column pairs)
 template <int I> struct ColVar;
 template <> struct ColVar<0> : Shape<512, 8192, 1> {};
 template <> struct ColVar<1> : Shape<512, 16384, 1> {};
 template <> struct ColVar<2> : Shape<256, 4096, 2> {};
 template <> struct ColVar<3> : Shape<256, 8192, 2> {};
-constexpr int N_COL_VARIANTS = 4;
+template <> struct ColVar<4> : Shape<256, 8192, 2, true> {};
+template <> struct ColVar<5> : Shape<512, 16384, 1, true> {};
+template <> struct ColVar<6> : Shape<128, 4096, 4, true> {};
+template <> struct ColVar<7> : Shape<64, 2048, 8, true> {};
+constexpr int N_COL_VARIANTS = 8;
 
 template <int N, class V>
 struct RowShape {
     static constexpr int NT = V::NT;
-    static constexpr int NSEQ = V::E >= N ? V::E / N : 1;
-    static constexpr int SMEM = NSEQ * padded_len(N) * 8;
-    static constexpr bool valid = (NSEQ * (N / 16)) % NT == 0 && SMEM <= 200 * 1024;
+    static constexpr bool PAIRED = V::PAIRED;
+    static constexpr int NSEQ = PAIRED ? (V::E >= 2 * N ? V::E / (2 * N) : 1) : (V::E >= N ? V::E / N : 1);
+    static constexpr int ROWS = PAIRED ? 2 * NSEQ : NSEQ; // field rows per CTA
+    static constexpr int SMEM = NSEQ * padded_len(N) * (PAIRED ? 16 : 8);
+    // paired variants: exactly one butterfly pair per thread in the end stages
+    static constexpr bool valid = (NSEQ * (N / 16)) % NT == 0 && SMEM <= 200 * 1024 &&
+                                  (!PAIRED || (NSEQ * (N / 16) == NT && cp_mid_bpt<N, NT, NSEQ>() <= 32));
 };
 template <int N, class V>
 struct ColShape {
     static constexpr int NT = V::NT;
-    static constexpr int C = V::E / N;
-    static constexpr int SMEM = padded_len(N) * (C > 0 ? C : 1) * 8;
-    static constexpr bool valid = C >= 1 && (C * (N / 16)) % NT == 0 && SMEM <= 200 * 1024;
+    static constexpr bool PAIRED = V::PAIRED;
+    static constexpr int C = PAIRED ? V::E / (2 * N) : V::E / N;
+    static constexpr int COLS = PAIRED ? 2 * C : C; // field columns per CTA
+    static constexpr int SMEM = padded_len(N) * (C > 0 ? C : 1) * (PAIRED ? 16 : 8);
+    static constexpr bool valid = C >= 1 && (C * (N / 16)) % NT == 0 && SMEM <= 200 * 1024 &&
+                                  (!PAIRED || (C * (N / 16) == NT && cp_mid_bpt<N, NT, (C > 0 ? C : 1)>() <= 32));
 };
 
 template <int N, class V>
 __global__ void __launch_bounds__(V::NT, V::MINB) k_rows_fwd2(PropParams P)
 {
+    pdl_enter();
     extern __shared__ float2 sm[];
     using S = RowShape<N, V>;
     if constexpr (S::valid) rows_fwd_body<N, S::NT, S::NSEQ>(P, blockIdx.x * S::NSEQ, sm, threadIdx.x);
@@ -517,6 +734,7 @@ __global__ void __launch_bounds__(V::NT, V::MINB) k_rows_fwd2(PropParams P)
 template <int N, class V>
 __global__ void __launch_bounds__(V::NT, V::MINB) k_rows_inv2(PropParams P)
 {
+    pdl_enter();
     extern __shared__ float2 sm[];
     using S = RowShape<N, V>;
     if constexpr (S::valid) {
@@ -529,9 +747,41 @@ __global__ void __launch_bounds__(V::NT, V::MINB) k_rows_inv2(PropParams P)
 template <int N, class V>
 __global__ void __launch_bounds__(V::NT, V::MINB) k_cols2(PropParams P)
 {
+    pdl_enter();
     extern __shared__ float2 sm[];
     using S = ColShape<N, V>;
     if constexpr (S::valid) cols_body<N, S::NT, S::C>(P, blockIdx.x * S::C, sm, threadIdx.x);
+}
+
+template <int N, class V>
+__global__ void __launch_bounds__(V::NT, V::MINB) k_rows_fwd3(PropParams P)
+{
+    pdl_enter();
+    extern __shared__ float4 sm4[];
+    using S = RowShape<N, V>;
+    if constexpr (S::valid && S::PAIRED) rows_fwd_body_p<N, S::NT, S::NSEQ>(P, blockIdx.x * S::ROWS, sm4, threadIdx.x);
+}
+
+template <int N, class V>
+__global__ void __launch_bounds__(V::NT, V::MINB) k_rows_inv3(PropParams P)
+{
+    pdl_enter();
+    extern __shared__ float4 sm4[];
+    using S = RowShape<N, V>;
+    if constexpr (S::valid && S::PAIRED) {
+        float lsum = 0.f;
+        rows_inv_body_p<N, S::NT, S::NSEQ>(P, blockIdx.x * S::ROWS, sm4, threadIdx.x, lsum);
+        if (P.post_mode == OP_SEED) loss_reduce(lsum, P.loss, threadIdx.x, S::NT);
+    }
+}
+
+template <int N, class V>
+__global__ void __launch_bounds__(V::NT, V::MINB) k_cols3(PropParams P)
+{
+    pdl_enter();
+    extern __shared__ float4 sm4[];
+    using S = ColShape<N, V>;
+    if constexpr (S::valid && S::PAIRED) cols_body_p<N, S::NT, S::C>(P, blockIdx.x * S::COLS, sm4, threadIdx.x);
 }
 
 // ------------------------------------------------------------- chirp tables
@@ -604,6 +854,7 @@ __device__ __forceinline__ void chirp_body(const ChirpAxis &A, int part, float2 
 template <int N>
 __global__ void __launch_bounds__(ChirpCfg<N>::NT) k_chirp(ChirpAxis A)
 {
+    pdl_enter();
     extern __shared__ float2 sm[];
     chirp_body<N, ChirpCfg<N>::NT>(A, blockIdx.x, sm, threadIdx.x);
 }
@@ -629,6 +880,10 @@ int ensure_twiddles()
     }
     e = cudaMemcpyToSymbol(g_tw, t.data(), sizeof(float2) * FFT_MAX);
     if (e != cudaSuccess) return cuda_fail(e, "twiddle table upload");
+    std::vector<float4> t4(FFT_MAX);
+    for (int m = 0; m < FFT_MAX; ++m) t4[m] = make_float4(t[m].x, t[m].x, t[m].y, t[m].y);
+    e = cudaMemcpyToSymbol(g_tw4, t4.data(), sizeof(float4) * FFT_MAX);
+    if (e != cudaSuccess) return cuda_fail(e, "paired twiddle table upload");
     g_tw_ready[dev] = true;
     return OLG_OK;
 }
@@ -641,6 +896,26 @@ int prep_smem(K kern, int bytes)
     return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaFuncSetAttribute");
 }
 
+// Launch with programmatic stream serialisation (see pdl_enter).
+template <typename Arg>
+int launch_pdl(void (*kern)(Arg), int grid, int block, int smem, cudaStream_t st, const Arg &a, const char *what)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, a);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    count_launch();
+    return check_launch(what);
+}
+
 // selected variant per FFT length (index log2 N) and pass kind (0 rows fwd, 1 cols, 2 rows inv)
 int g_variant[3][14] = {};
 
@@ -650,17 +925,22 @@ int launch_rows_v(const PropParams &P, bool inverse, cudaStream_t st)
     using S = RowShape<N, RowVar<I>>;
     if constexpr (!S::valid) {
         return fail(OLG_ERR_INVALID_ARG, "row variant not valid for this length");
+    } else if constexpr (S::PAIRED) {
+        const int grid = (P.ny + S::ROWS - 1) / S::ROWS;
+        if (!inverse) {
+            if (int rc = prep_smem(k_rows_fwd3<N, RowVar<I>>, S::SMEM)) return rc;
+            return launch_pdl(k_rows_fwd3<N, RowVar<I>>, grid, S::NT, S::SMEM, st, P, "k_rows_fwd3");
+        }
+        if (int rc = prep_smem(k_rows_inv3<N, RowVar<I>>, S::SMEM)) return rc;
+        return launch_pdl(k_rows_inv3<N, RowVar<I>>, grid, S::NT, S::SMEM, st, P, "k_rows_inv3");
     } else {
-        const int grid = (P.ny + S::NSEQ - 1) / S::NSEQ;
+        const int grid = (P.ny + S::ROWS - 1) / S::ROWS;
         if (!inverse) {
             if (int rc = prep_smem(k_rows_fwd2<N, RowVar<I>>, S::SMEM)) return rc;
-            k_rows_fwd2<N, RowVar<I>><<<grid, S::NT, S::SMEM, st>>>(P);
-        } else {
-            if (int rc = prep_smem(k_rows_inv2<N, RowVar<I>>, S::SMEM)) return rc;
-            k_rows_inv2<N, RowVar<I>><<<grid, S::NT, S::SMEM, st>>>(P);
+            return launch_pdl(k_rows_fwd2<N, RowVar<I>>, grid, S::NT, S::SMEM, st, P, "k_rows_fwd2");
         }
-        count_launch();
-        return check_launch(inverse ? "k_rows_inv2" : "k_rows_fwd2");
+        if (int rc = prep_smem(k_rows_inv2<N, RowVar<I>>, S::SMEM)) return rc;
+        return launch_pdl(k_rows_inv2<N, RowVar<I>>, grid, S::NT, S::SMEM, st, P, "k_rows_inv2");
     }
 }
 
@@ -670,12 +950,14 @@ int launch_cols_v(const PropParams &P, cudaStream_t st)
     using S = ColShape<N, ColVar<I>>;
     if constexpr (!S::valid) {
         return fail(OLG_ERR_INVALID_ARG, "column variant not valid for this length");
+    } else if constexpr (S::PAIRED) {
+        const int grid = (P.NX + S::COLS - 1) / S::COLS;
+        if (int rc = prep_smem(k_cols3<N, ColVar<I>>, S::SMEM)) return rc;
+        return launch_pdl(k_cols3<N, ColVar<I>>, grid, S::NT, S::SMEM, st, P, "k_cols3");
     } else {
-        const int grid = (P.NX + S::C - 1) / S::C;
+        const int grid = (P.NX + S::COLS - 1) / S::COLS;
         if (int rc = prep_smem(k_cols2<N, ColVar<I>>, S::SMEM)) return rc;
-        k_cols2<N, ColVar<I>><<<grid, S::NT, S::SMEM, st>>>(P);
-        count_launch();
-        return check_launch("k_cols2");
+        return launch_pdl(k_cols2<N, ColVar<I>>, grid, S::NT, S::SMEM, st, P, "k_cols2");
     }
 }
 
@@ -687,6 +969,10 @@ bool row_variant_valid(int i)
     case 1: return RowShape<N, RowVar<1>>::valid;
     case 2: return RowShape<N, RowVar<2>>::valid;
     case 3: return RowShape<N, RowVar<3>>::valid;
+    case 4: return RowShape<N, RowVar<4>>::valid;
+    case 5: return RowShape<N, RowVar<5>>::valid;
+    case 6: return RowShape<N, RowVar<6>>::valid;
+    case 7: return RowShape<N, RowVar<7>>::valid;
     default: return false;
     }
 }
@@ -698,6 +984,10 @@ bool col_variant_valid(int i)
     case 1: return ColShape<N, ColVar<1>>::valid;
     case 2: return ColShape<N, ColVar<2>>::valid;
     case 3: return ColShape<N, ColVar<3>>::valid;
+    case 4: return ColShape<N, ColVar<4>>::valid;
+    case 5: return ColShape<N, ColVar<5>>::valid;
+    case 6: return ColShape<N, ColVar<6>>::valid;
+    case 7: return ColShape<N, ColVar<7>>::valid;
     default: return false;
     }
 }
@@ -712,20 +1002,22 @@ int launch_rows(const PropParams &P, bool inverse, cudaStream_t st)
         case 1: return launch_rows_v<N, 1>(P, inverse, st);
         case 2: return launch_rows_v<N, 2>(P, inverse, st);
         case 3: return launch_rows_v<N, 3>(P, inverse, st);
+        case 4: return launch_rows_v<N, 4>(P, inverse, st);
+        case 5: return launch_rows_v<N, 5>(P, inverse, st);
+        case 6: return launch_rows_v<N, 6>(P, inverse, st);
+        case 7: return launch_rows_v<N, 7>(P, inverse, st);
         default: return launch_rows_v<N, 0>(P, inverse, st);
         }
-    }
-    using C = RowCfg<N>;
-    const int grid = (P.ny + C::NSEQ - 1) / C::NSEQ;
-    if (!inverse) {
-        if (int rc = prep_smem(k_rows_fwd<N>, C::SMEM)) return rc;
-        k_rows_fwd<N><<<grid, C::NT, C::SMEM, st>>>(P);
     } else {
+        using C = RowCfg<N>;
+        const int grid = (P.ny + C::NSEQ - 1) / C::NSEQ;
+        if (!inverse) {
+            if (int rc = prep_smem(k_rows_fwd<N>, C::SMEM)) return rc;
+            return launch_pdl(k_rows_fwd<N>, grid, C::NT, C::SMEM, st, P, "k_rows_fwd");
+        }
         if (int rc = prep_smem(k_rows_inv<N>, C::SMEM)) return rc;
-        k_rows_inv<N><<<grid, C::NT, C::SMEM, st>>>(P);
+        return launch_pdl(k_rows_inv<N>, grid, C::NT, C::SMEM, st, P, "k_rows_inv");
     }
-    count_launch();
-    return check_launch(inverse ? "k_rows_inv" : "k_rows_fwd");
 }
 
 template <int N>
@@ -736,15 +1028,18 @@ int launch_cols(const PropParams &P, cudaStream_t st)
         case 1: return launch_cols_v<N, 1>(P, st);
         case 2: return launch_cols_v<N, 2>(P, st);
         case 3: return launch_cols_v<N, 3>(P, st);
+        case 4: return launch_cols_v<N, 4>(P, st);
+        case 5: return launch_cols_v<N, 5>(P, st);
+        case 6: return launch_cols_v<N, 6>(P, st);
+        case 7: return launch_cols_v<N, 7>(P, st);
         default: return launch_cols_v<N, 0>(P, st);
         }
+    } else {
+        using C = ColCfg<N>;
+        const int grid = (P.NX + C::C - 1) / C::C;
+        if (int rc = prep_smem(k_cols<N>, C::SMEM)) return rc;
+        return launch_pdl(k_cols<N>, grid, C::NT, C::SMEM, st, P, "k_cols");
     }
-    using C = ColCfg<N>;
-    const int grid = (P.NX + C::C - 1) / C::C;
-    if (int rc = prep_smem(k_cols<N>, C::SMEM)) return rc;
-    k_cols<N><<<grid, C::NT, C::SMEM, st>>>(P);
-    count_launch();
-    return check_launch("k_cols");
 }
 
 template <int N>
@@ -1146,34 +1441,55 @@ extern "C" int olg_autotune_prop(int ny, int nx, int reps, olg_stream_t stream)
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    // Coordinate descent over the three passes, timing whole propagations:
+    // a pass's speed depends on its neighbours (L2 contents, dependent-launch
+    // overlap), so passes are not timed alone.
     const int lens[3] = {2 * nx, 2 * ny, 2 * nx};
-    for (int kind = 0; kind < 3; ++kind) {
-        const int n = lens[kind], ln = log2i(n);
-        float best = 1e30f;
-        int best_i = g_variant[kind][ln];
-        for (int i = 0; i < olg_prop_variant_count(); ++i) {
-            if (!variant_valid(kind, n, i)) continue;
-            g_variant[kind][ln] = i;
-            auto run = [&]() { return kind == 1 ? cols_pass(S.P, st) : rows_pass(S.P, kind == 2, st); };
-            int rc = OLG_OK;
-            for (int w = 0; w < 2 && !rc; ++w) rc = run();
+    int lns[3];
+    for (int k = 0; k < 3; ++k) lns[k] = log2i(lens[k]);
+    // Each timed propagation starts from a cold L2 (a 256 MiB write first),
+    // like a propagation of a field that was not just touched.
+    const size_t flush_bytes = (size_t)256 << 20;
+    Scratch flush;
+    if (int rc = flush.acquire(nullptr, 0, flush_bytes, st)) return rc;
+    auto time_prop = [&](float *ms) -> int {
+        int rc = run_passes(S.P, st);
+        *ms = 0.f;
+        for (int r = 0; r < reps && !rc; ++r) {
+            const cudaError_t fe = cudaMemsetAsync(flush.ptr, r & 0xff, flush_bytes, st);
+            if (fe != cudaSuccess) return cuda_fail(fe, "cudaMemsetAsync (L2 flush)");
             cudaEventRecord(e0, st);
-            for (int r = 0; r < reps && !rc; ++r) rc = run();
+            rc = run_passes(S.P, st);
             cudaEventRecord(e1, st);
-            if (rc) {
-                cudaEventDestroy(e0);
-                cudaEventDestroy(e1);
-                return rc;
-            }
+            if (rc) break;
             cudaEventSynchronize(e1);
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (ms < best) {
-                best = ms;
-                best_i = i;
-            }
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            *ms += t;
         }
-        g_variant[kind][ln] = best_i;
+        return rc;
+    };
+    for (int round = 0; round < 2; ++round) {
+        for (int kind = 0; kind < 3; ++kind) {
+            const int n = lens[kind], ln = lns[kind];
+            float best = 1e30f;
+            int best_i = g_variant[kind][ln];
+            for (int i = 0; i < olg_prop_variant_count(); ++i) {
+                if (!variant_valid(kind, n, i)) continue;
+                g_variant[kind][ln] = i;
+                float ms = 0.f;
+                if (int rc = time_prop(&ms)) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return rc;
+                }
+                if (ms < best) {
+                    best = ms;
+                    best_i = i;
+                }
+            }
+            g_variant[kind][ln] = best_i;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
