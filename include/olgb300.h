@@ -46,8 +46,9 @@ extern "C" {
 #define OLG_NO_NORMALIZE 0x2 /* host-pointer overload convention: no 1/Np factors */
 #define OLG_ACCUMULATE 0x4   /* out += result (gCghReduction semantics) */
 #define OLG_VERBOSE 0x8      /* print the chosen method like the reference's printf */
-#define OLG_CHECK_F32 0x10   /* olg_prop_c64: evaluate the AUTO checks in float (PREC_T=float) */
+#define OLG_CHECK_F32 0x10   /* evaluate the AUTO checks (olg_prop_c64) / the shifted band window in float (PREC_T=float) */
 #define OLG_REUSE_OPERANDS 0x20 /* olg_cgh_fresnel_gemm_c64: operands already in `work` from a call with the same points */
+#define OLG_BANDLIMIT 0x40   /* shifted ASM: the band window of the host overload (olprop.h:251-305) */
 
 /* propagation modes, ol::PROPMODE (oldefine.h:7-9) */
 #define OLG_ASM 0
@@ -100,6 +101,46 @@ int olg_fresnel_prop_c64(const void *u_in, void *u_out, int ny, int nx, double d
 int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx, double lambda,
                       double z, double s, double oy, double ox, int flags, void *work, size_t work_bytes,
                       olg_stream_t stream);
+
+/* Shifted angular spectrum method: the destination plane is offset by
+ * (oy, ox).  Replaces ol::gshiftedAsmProp (golprop.h:335-420, 537-575):
+ * T = exp(2 pi i (w z + ox u + oy v)), 1/Np.  OLG_BANDLIMIT adds the band
+ * window of the host overload ol::shiftedAsmProp (olprop.h:251-327), which
+ * also scales by a further 1/Np (apply it, or not, on the caller's side);
+ * with OLG_CHECK_F32 the window is decided in float, as that overload's
+ * PREC_T = float instantiation decides it.  OLG_NO_NORMALIZE drops the 1/Np,
+ * OLG_CONJ gives the adjoint. */
+int olg_shifted_asm_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                             double z, double oy, double ox, int flags, void *work, size_t work_bytes,
+                             olg_stream_t stream);
+
+/* Shifted (scaled) Fresnel propagation.  Replaces ol::gshiftedFresnelProp
+ * (golprop.h:606-752): the ARSS chirps without windows; any finite s. */
+int olg_shifted_fresnel_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx,
+                                 double lambda, double z, double s, double oy, double ox, int flags, void *work,
+                                 size_t work_bytes, olg_stream_t stream);
+
+/* ol::shiftedProp (golprop.h:755-768): OLG_ASM -> shifted ASM, OLG_FRESNEL ->
+ * shifted Fresnel with s = 1; any other mode is OLG_ERR_INVALID_ARG (the
+ * reference prints "error" and exits). */
+int olg_shifted_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx, double lambda,
+                         double z, double oy, double ox, int propmode, int flags, void *work, size_t work_bytes,
+                         olg_stream_t stream);
+
+/* Split propagation.  Replaces ol::gsplitProp (golprop.h:772-813) and
+ * ol::splitAsmProp (olprop.h:618-654) on device fields: the ny x nx field
+ * is cut into blocks_y x blocks_x blocks (powers of two, >= 16), and every
+ * (source, destination) block pair adds olg_shifted_prop_c64 of the source
+ * block, offset by the blocks' distance, into the destination block.  u_out
+ * must not overlap u_in; it is zeroed first unless OLG_ACCUMULATE.  Flags
+ * pass on to the shifted propagations: OLG_BANDLIMIT | OLG_CHECK_F32 gives
+ * splitAsmProp's per-block window (its only instantiation is PREC_T = float);
+ * each block then carries its further 1/Np_block on the caller's side.
+ * Scratch: olg_split_prop_workspace_bytes, reused for every pair. */
+size_t olg_split_prop_workspace_bytes(int ny, int nx, int blocks_y, int blocks_x);
+int olg_split_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda, double z,
+                       int propmode, int blocks_y, int blocks_x, int flags, void *work, size_t work_bytes,
+                       olg_stream_t stream);
 
 /* Angular spectrum method that allocates nothing -- no counterpart in the
  * reference.  Same computation and flags as olg_asm_prop_c64, but its scratch

@@ -13,6 +13,8 @@ from .batch import BatchPlan, config5_fields  # noqa: F401
 from .optim import PhaseOptimizer, make_targets, phase_loss_grad  # noqa: F401
 from .prop import (ASM, AUTO, FRESNEL, PROPMODE, ARSSFresnelProp, AsmPropCheck, FresnelPropCheck,  # noqa: F401
                    Prop, arss_prop, asm_prop, fresnel_prop, gAsmProp, gFresnelProp, gFresnelPropBandLimit,
-                   autotune, get_variant, set_variant, variant_count, workspace, workspace_bytes)
+                   autotune, get_variant, set_variant, variant_count, workspace, workspace_bytes,
+                   gshiftedAsmProp, gshiftedFresnelProp, gsplitProp, shiftedAsmProp, shiftedFresnelProp, shiftedProp,
+                   shifted_asm_prop, shifted_fresnel_prop, split_prop, split_workspace, splitAsmProp)
 
 __version__ = "0.1.0"

@@ -20,6 +20,7 @@ OLG_ACCUMULATE = 0x4
 OLG_VERBOSE = 0x8
 OLG_CHECK_F32 = 0x10
 OLG_REUSE_OPERANDS = 0x20
+OLG_BANDLIMIT = 0x40
 
 _d, _f, _i, _p, _sz = C.c_double, C.c_float, C.c_int, C.c_void_p, C.c_size_t
 
@@ -38,6 +39,11 @@ SIGNATURES = {
     "olg_launch_count": (C.c_ulonglong, []),
     "olg_prop_workspace_bytes": (_sz, [_i, _i]),
     "olg_asm_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_shifted_asm_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_shifted_fresnel_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_shifted_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _i, _i, _p, _sz, _p]),
+    "olg_split_prop_workspace_bytes": (_sz, [_i, _i, _i, _i]),
+    "olg_split_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _i, _i, _i, _p, _sz, _p]),
     "olg_asm_prop_noalloc_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _p]),
     "olg_fresnel_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _i, _p, _sz, _p]),
     "olg_arss_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _d, _i, _p, _sz, _p]),

@@ -49,16 +49,22 @@ inline DF split_df(double v)
 // exactly representable float m (|m| <= 2^24).  The product c.hi * m is split
 // exactly with an FMA, its integer part removed exactly, and the rounding
 // error terms added back at small magnitude.
+// Round to an integer by adding and removing 1.5 * 2^23: round to nearest
+// even, exact for |x| < 2^22; beyond that an integer near x (callers only use
+// the result modulo 1, and every caller wraps its final sum again).  Plain
+// FP32 adds, cheaper than a rounding instruction.
+__device__ __forceinline__ float round_int(float x) { return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f); }
+
 __device__ __forceinline__ float frac_mul(float chi, float clo, float m)
 {
     const float p = __fmul_rn(chi, m); // never contracted into an FMA
     const float e = __fmaf_rn(chi, m, -p);
-    const float r = p - rintf(p);
+    const float r = p - round_int(p);
     float t = r + (e + clo * m);
-    return t - rintf(t);
+    return t - round_int(t);
 }
 
-__device__ __forceinline__ float wrap_cycles(float t) { return t - rintf(t); }
+__device__ __forceinline__ float wrap_cycles(float t) { return t - round_int(t); }
 
 // exp(2 pi i t) for t in cycles (|t| <= ~1 after wrapping).
 __device__ __forceinline__ float2 cis_cycles(float t)

@@ -84,6 +84,13 @@ struct PropParams {
     // tables written earlier in the same launch (batched persistent kernel):
     // read them through L2 (ld.global.cg), never the non-coherent path
     int coherent;
+    // row strides (elements) of in / in_phase and of out (sub-blocks of a larger field)
+    long in_ld, out_ld;
+    // shifted ASM: extra phase ox u + oy v = lx fx + ly fy cycles; optional band
+    // window fx in [fx_lo, fx_hi], fy in [fy_lo, fy_hi] (T = 0 outside)
+    int shift, band;
+    float lx_hi, lx_lo, ly_hi, ly_lo;
+    int fx_lo, fx_hi, fy_lo, fy_hi;
 };
 
 // ---------------------------------------------------------------- launch shapes
@@ -148,11 +155,11 @@ __global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_fwd(PropParams P)
         float2 a = make_float2(0.f, 0.f), b = a;
         if (h < P.ny) {
             if (P.in_phase) {
-                const float2 ph = __ldg(reinterpret_cast<const float2 *>(P.in_phase + (size_t)h * nx + w2));
+                const float2 ph = __ldg(reinterpret_cast<const float2 *>(P.in_phase + (size_t)h * P.in_ld + w2));
                 sincosf(ph.x, &a.y, &a.x);
                 sincosf(ph.y, &b.y, &b.x);
             } else {
-                const float4 v = __ldg(reinterpret_cast<const float4 *>(P.in + (size_t)h * nx + w2));
+                const float4 v = __ldg(reinterpret_cast<const float4 *>(P.in + (size_t)h * P.in_ld + w2));
                 a = make_float2(v.x, v.y);
                 b = make_float2(v.z, v.w);
             }
@@ -211,7 +218,7 @@ __global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_inv(PropParams P)
             a = apply_op(a, P.post_mode, P.postx, P.posty, h, w2, P.ny, nx, P.post_hlim, P.post_wlim);
             b = apply_op(b, P.post_mode, P.postx, P.posty, h, w2 + 1, P.ny, nx, P.post_hlim, P.post_wlim);
         }
-        float4 *dst = reinterpret_cast<float4 *>(P.out + (size_t)h * nx + w2);
+        float4 *dst = reinterpret_cast<float4 *>(P.out + (size_t)h * P.out_ld + w2);
         if (P.accumulate) {
             const float4 o = *dst;
             a.x += o.x; a.y += o.y; b.x += o.z; b.y += o.w;
@@ -245,6 +252,10 @@ __device__ __forceinline__ float2 asm_tf(const PropParams &P, int fx, int fy)
     const float q = t / (1.0f + s);
     const float g = 0.5f * q * q;
     float cyc = P.c0 - frac_mul(P.ax_hi, P.ax_lo, fx2) - frac_mul(P.ay_hi, P.ay_lo, fy2) - P.zl * g;
+    if (P.shift) {
+        if (P.band && (fx < P.fx_lo || fx > P.fx_hi || fy < P.fy_lo || fy > P.fy_hi)) return make_float2(0.f, 0.f);
+        cyc += frac_mul(P.lx_hi, P.lx_lo, (float)fx) + frac_mul(P.ly_hi, P.ly_lo, (float)fy);
+    }
     cyc = wrap_cycles(cyc);
     if (P.conj) cyc = -cyc;
     return cscale(cis_cycles(cyc), P.scale);
@@ -310,10 +321,10 @@ __device__ __forceinline__ float2 load_in(const PropParams &P, int h, int w)
 {
     float2 x;
     if (P.in_phase) {
-        const float ph = __ldg(P.in_phase + (size_t)h * P.nx + w);
+        const float ph = __ldg(P.in_phase + (size_t)h * P.in_ld + w);
         sincosf(ph, &x.y, &x.x);
     } else {
-        x = __ldg(P.in + (size_t)h * P.nx + w);
+        x = __ldg(P.in + (size_t)h * P.in_ld + w);
     }
     return apply_op_c(x, P.pre_mode, P.prex, P.prey, h, w, P.ny, P.nx, P.pre_hlim, P.pre_wlim, P.coherent);
 }
@@ -351,6 +362,24 @@ __device__ __forceinline__ void rows_fwd_body(const PropParams &P, int r0, float
     }
 }
 
+__device__ __forceinline__ void store_out(const PropParams &P, int h, int w, float2 a, float &lsum)
+{
+    const size_t o = (size_t)h * P.out_ld + w;
+    if (P.post_mode == OP_SEED) {
+        const float r2 = a.x * a.x + a.y * a.y - __ldg(P.target + (size_t)h * P.nx + w);
+        lsum = fmaf(r2, r2, lsum);
+        a = cscale(a, P.seed_scale * r2);
+    } else {
+        a = apply_op_c(a, P.post_mode, P.postx, P.posty, h, w, P.ny, P.nx, P.post_hlim, P.post_wlim, P.coherent);
+    }
+    if (P.accumulate) {
+        const float2 v = P.out[o];
+        a.x += v.x;
+        a.y += v.y;
+    }
+    P.out[o] = a;
+}
+
 template <int N, int NT, int NSEQ>
 __device__ __forceinline__ void rows_inv_body(const PropParams &P, int r0, float2 *sm, int tid, float &lsum)
 {
@@ -382,21 +411,7 @@ __device__ __forceinline__ void rows_inv_body(const PropParams &P, int r0, float
         for (int k = 4; k < 12; ++k) {
             const int w = j + (k - 4) * B;
             float2 a = v[outpos<16>(k)];
-            const size_t i = (size_t)h * P.nx + w;
-            if (P.post_mode == OP_SEED) {
-                const float r2 = a.x * a.x + a.y * a.y - __ldg(P.target + i);
-                lsum = fmaf(r2, r2, lsum);
-                a = cscale(a, P.seed_scale * r2);
-            } else {
-                a = apply_op_c(a, P.post_mode, P.postx, P.posty, h, w, P.ny, P.nx, P.post_hlim, P.post_wlim,
-                               P.coherent);
-            }
-            if (P.accumulate) {
-                const float2 o = P.out[i];
-                a.x += o.x;
-                a.y += o.y;
-            }
-            P.out[i] = a;
+            store_out(P, h, w, a, lsum);
         }
     }
 }
@@ -518,23 +533,6 @@ __device__ __forceinline__ void rows_fwd_body_p(const PropParams &P, int r0, flo
     }
 }
 
-__device__ __forceinline__ void store_out(const PropParams &P, int h, int w, float2 a, float &lsum)
-{
-    const size_t i = (size_t)h * P.nx + w;
-    if (P.post_mode == OP_SEED) {
-        const float r2 = a.x * a.x + a.y * a.y - __ldg(P.target + i);
-        lsum = fmaf(r2, r2, lsum);
-        a = cscale(a, P.seed_scale * r2);
-    } else {
-        a = apply_op_c(a, P.post_mode, P.postx, P.posty, h, w, P.ny, P.nx, P.post_hlim, P.post_wlim, P.coherent);
-    }
-    if (P.accumulate) {
-        const float2 o = P.out[i];
-        a.x += o.x;
-        a.y += o.y;
-    }
-    P.out[i] = a;
-}
 
 template <int N, int NT, int NSP>
 __device__ __forceinline__ void rows_inv_body_p(const PropParams &P, int r0, float4 *sm, int tid, float &lsum)
@@ -1113,6 +1111,8 @@ PropParams base_params(const void *in, void *out, int ny, int nx, const Layout &
     P.S = L.S;
     P.Hx = L.Hx; P.Hy = L.Hy;
     P.pre_mode = OP_NONE; P.post_mode = OP_NONE;
+    P.in_ld = nx;
+    P.out_ld = nx;
     return P;
 }
 
@@ -1207,6 +1207,73 @@ int setup_asm(const void *in, void *out, int ny, int nx, double dy, double dx, d
     return OLG_OK;
 }
 
+// Shifted ASM (golprop.h:335-420, 536-576): T gains the phase ox u + oy v,
+// an integer multiple of (lx, ly) = (ox du, oy dv) cycles per frequency index.
+// OLG_BANDLIMIT adds the band window of the host overload (olprop.h:251-300):
+// T = 0 unless |u - u0| 2 < uw and |v - v0| 2 < vw, decided here in double
+// for every frequency index exactly as that code decides it.
+// T = double decides in double; T = float mirrors the PREC_T = float
+// instantiation operation by operation (float operands, std::pow(float, int)
+// and the sqrt in double, results stored to float; this file is compiled with
+// -ffp-contract=off).  Adjacent split blocks sit exactly on a branch boundary
+// (offset == 0.5 / du), so the precision decides which branch is taken.
+template <typename T>
+void shifted_window(double pitch, int L, double o_, double z_, double lambda_, int *lo, int *hi)
+{
+    const T d = (T)1 / ((T)pitch * (T)L);
+    const T o = (T)o_, z = (T)z_, lambda = (T)lambda_;
+    const T s0 = (T)0.5 / d;
+    const T tm = o - (T)0.5 / d, tp = o + (T)0.5 / d;
+    const T lm = (T)(1 / std::sqrt(std::pow((double)tm, -2.0) * z * z + 1.0) / lambda);
+    const T lp = (T)(1 / std::sqrt(std::pow((double)tp, -2.0) * z * z + 1.0) / lambda);
+    T c, w;
+    if (s0 < o) {
+        c = (T)0.5 * (lp + lm);
+        w = lp - lm;
+    } else if (-s0 <= o && o < s0) {
+        c = (T)0.5 * (lp - lm);
+        w = lp + lm;
+    } else {
+        c = (T)-0.5 * (lp + lm);
+        w = lm - lp;
+    }
+    *lo = 1;
+    *hi = 0;
+    bool any = false;
+    for (int m = 0; m < L; ++m) {
+        const int f = m - L / 2;
+        const T u = (T)f * d;
+        if (std::fabs(u - c) * 2 < w) {
+            if (!any) *lo = f;
+            *hi = f;
+            any = true;
+        }
+    }
+}
+
+int setup_shifted_asm(const void *in, void *out, int ny, int nx, double dy, double dx, double lambda, double z,
+                      double oy, double ox, int flags, const Layout &L, PropSetup *S)
+{
+    if (!std::isfinite(oy) || !std::isfinite(ox)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (int rc = setup_asm(in, out, ny, nx, dy, dx, lambda, z, flags, L, S)) return rc;
+    PropParams &P = S->P;
+    const double du = 1.0 / (dx * 2.0 * nx), dv = 1.0 / (dy * 2.0 * ny);
+    P.shift = 1;
+    set_quad(P.lx_hi, P.lx_lo, ox * du);
+    set_quad(P.ly_hi, P.ly_lo, oy * dv);
+    if (flags & OLG_BANDLIMIT) {
+        P.band = 1;
+        if (flags & OLG_CHECK_F32) {
+            shifted_window<float>(dx, 2 * nx, ox, z, lambda, &P.fx_lo, &P.fx_hi);
+            shifted_window<float>(dy, 2 * ny, oy, z, lambda, &P.fy_lo, &P.fy_hi);
+        } else {
+            shifted_window<double>(dx, 2 * nx, ox, z, lambda, &P.fx_lo, &P.fx_hi);
+            shifted_window<double>(dy, 2 * ny, oy, z, lambda, &P.fy_lo, &P.fy_hi);
+        }
+    }
+    return OLG_OK;
+}
+
 int setup_fresnel(const void *in, void *out, int ny, int nx, double dy, double dx, double lambda, double z,
                   int bandlimit, int flags, const Layout &L, PropSetup *S)
 {
@@ -1233,22 +1300,28 @@ int setup_fresnel(const void *in, void *out, int ny, int nx, double dy, double d
     return OLG_OK;
 }
 
+// windows == false: the shifted Fresnel propagation (golprop.h:606-752), the
+// same three chirps without any window.
 int setup_arss(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx, double lambda, double z,
-               double s, double oy, double ox, int flags, const Layout &L, PropSetup *S)
+               double s, double oy, double ox, int flags, const Layout &L, PropSetup *S, bool windows = true)
 {
     if (int rc = check_phys(dy, dx, lambda, z, true)) return rc;
-    if (!std::isfinite(s)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
-    if (s == 0.0 || s == 1.0)
+    if (!std::isfinite(s) || !std::isfinite(oy) || !std::isfinite(ox))
+        return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (windows && (s == 0.0 || s == 1.0))
         return fail(OLG_ERR_INVALID_ARG, "ARSS is undefined for s = 0 or s = 1 (window limits divide by s|s-1|)");
     PropParams P = base_params(u_src, u_dst, ny, nx, L);
     const int NX = 2 * nx, NY = 2 * ny;
     const double np = (double)NX * (double)NY;
-    // windows, golprop.h:849-852, 891-892, 928-931
-    const int hlim_u = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dy)) / dy);
-    const int wlim_u = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dx)) / dx);
-    const int lim_h = (int)floor_lim(std::fabs(lambda * z * 0.5 / (dx * s)) / dx);
-    const int hlim_c = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dy)) / dy);
-    const int wlim_c = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dx)) / dx);
+    // windows, golprop.h:849-852, 891-892, 928-931 (-1: none)
+    int hlim_u = -1, wlim_u = -1, lim_h = -1, hlim_c = -1, wlim_c = -1;
+    if (windows) {
+        hlim_u = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dy)) / dy);
+        wlim_u = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dx)) / dx);
+        lim_h = (int)floor_lim(std::fabs(lambda * z * 0.5 / (dx * s)) / dx);
+        hlim_c = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dy)) / dy);
+        wlim_c = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dx)) / dx);
+    }
     const bool adj = (flags & OLG_CONJ) != 0;
     const double lz2 = 2.0 * lambda * z;
     ChirpAxis ax = chirp_axis_params(NX, nx, dx, lambda, z, s, lim_h, 1.0 / np, L.Hx);
@@ -1281,14 +1354,14 @@ int setup_arss(const void *u_src, void *u_dst, int ny, int nx, double dy, double
         fill(ax, L.tax, L.tbx, prex, wlim_u, 0, postx, -1, 0);
         fill(ay, L.tay, L.tby, prey, hlim_u, 0, posty, -1, 0);
         P.pre_mode = OP_TABLE;
-        P.post_mode = OP_TABLE_IN_WINDOW;
+        P.post_mode = windows ? OP_TABLE_IN_WINDOW : OP_TABLE;
         P.post_hlim = hlim_c;
         P.post_wlim = wlim_c;
     } else {
         // adjoint: conj(post-chirp) inside the Cz window first, conj(pre-chirp) with its window last
         fill(ax, L.tax, L.tbx, postx, -1, 1, prex, wlim_u, 1);
         fill(ay, L.tay, L.tby, posty, -1, 1, prey, hlim_u, 1);
-        P.pre_mode = OP_TABLE_IN_WINDOW;
+        P.pre_mode = windows ? OP_TABLE_IN_WINDOW : OP_TABLE;
         P.pre_hlim = hlim_c;
         P.pre_wlim = wlim_c;
         P.post_mode = OP_TABLE;
@@ -1371,6 +1444,112 @@ extern "C" int olg_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx,
     PropSetup S;
     if (int rc = setup_arss(u_src, u_dst, ny, nx, dy, dx, lambda, z, s, oy, ox, flags, L, &S)) return rc;
     return run_setup(S, st);
+}
+
+extern "C" int olg_shifted_asm_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx,
+                                        double lambda, double z, double oy, double ox, int flags, void *work,
+                                        size_t work_bytes, olg_stream_t stream)
+{
+    if (int rc = validate(u_in, u_out, ny, nx)) return rc;
+    if (int rc = check_phys(dy, dx, lambda, z, false)) return rc;
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
+    Layout L;
+    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    PropSetup S;
+    if (int rc = setup_shifted_asm(u_in, u_out, ny, nx, dy, dx, lambda, z, oy, ox, flags, L, &S)) return rc;
+    return run_setup(S, st);
+}
+
+extern "C" int olg_shifted_fresnel_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx,
+                                            double lambda, double z, double s, double oy, double ox, int flags,
+                                            void *work, size_t work_bytes, olg_stream_t stream)
+{
+    if (int rc = validate(u_src, u_dst, ny, nx)) return rc;
+    if (int rc = check_phys(dy, dx, lambda, z, true)) return rc;
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, layout_bytes(ny, nx, nullptr, nullptr), st)) return rc;
+    Layout L;
+    layout_bytes(ny, nx, &L, (char *)sc.ptr);
+    PropSetup S;
+    if (int rc = setup_arss(u_src, u_dst, ny, nx, dy, dx, lambda, z, s, oy, ox, flags, L, &S, false)) return rc;
+    return run_setup(S, st);
+}
+
+extern "C" int olg_shifted_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx,
+                                    double lambda, double z, double oy, double ox, int propmode, int flags, void *work,
+                                    size_t work_bytes, olg_stream_t stream)
+{
+    if (propmode == OLG_ASM)
+        return olg_shifted_asm_prop_c64(u_src, u_dst, ny, nx, dy, dx, lambda, z, oy, ox, flags, work, work_bytes,
+                                        stream);
+    if (propmode == OLG_FRESNEL)
+        return olg_shifted_fresnel_prop_c64(u_src, u_dst, ny, nx, dy, dx, lambda, z, 1.0, oy, ox, flags, work,
+                                            work_bytes, stream);
+    return fail(OLG_ERR_INVALID_ARG, "shifted propagation takes OLG_ASM or OLG_FRESNEL");
+}
+
+extern "C" size_t olg_split_prop_workspace_bytes(int ny, int nx, int blocks_y, int blocks_x)
+{
+    if (ny <= 0 || nx <= 0 || blocks_y <= 0 || blocks_x <= 0) return 0;
+    return layout_bytes(ny / blocks_y, nx / blocks_x, nullptr, nullptr);
+}
+
+// Split propagation (golprop.h:772-813, olprop.h:618-654): the field is cut
+// into blocks_y x blocks_x blocks; every (source block, destination block)
+// pair adds a shifted propagation of the source block, offset by the blocks'
+// distance, into the destination block.  Blocks are read and written in place
+// through row strides; u_out must not overlap u_in.
+extern "C" int olg_split_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                                  double z, int propmode, int blocks_y, int blocks_x, int flags, void *work,
+                                  size_t work_bytes, olg_stream_t stream)
+{
+    if (!u_in || !u_out || blocks_y <= 0 || blocks_x <= 0 || ny % blocks_y || nx % blocks_x)
+        return fail(OLG_ERR_INVALID_ARG, "blocks must divide the field");
+    const int bh = ny / blocks_y, bw = nx / blocks_x;
+    if (int rc = validate(u_in, u_out, bh, bw)) return rc;
+    if (propmode != OLG_ASM && propmode != OLG_FRESNEL)
+        return fail(OLG_ERR_INVALID_ARG, "split propagation takes OLG_ASM or OLG_FRESNEL");
+    const size_t bytes = (size_t)ny * nx * sizeof(float2);
+    const char *a = (const char *)u_in, *b = (const char *)u_out;
+    if (a < b + bytes && b < a + bytes) return fail(OLG_ERR_INVALID_ARG, "u_out must not overlap u_in");
+    if (int rc = check_phys(dy, dx, lambda, z, propmode == OLG_FRESNEL)) return rc;
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, layout_bytes(bh, bw, nullptr, nullptr), st)) return rc;
+    Layout L;
+    layout_bytes(bh, bw, &L, (char *)sc.ptr);
+    if (!(flags & OLG_ACCUMULATE)) {
+        const cudaError_t e = cudaMemsetAsync(u_out, 0, bytes, st);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    }
+    const int pflags = flags & (OLG_CONJ | OLG_NO_NORMALIZE | OLG_BANDLIMIT | OLG_CHECK_F32);
+    for (int gn = 0; gn < blocks_y; ++gn)
+        for (int gm = 0; gm < blocks_x; ++gm) {
+            const float2 *src = (const float2 *)u_in + (size_t)gn * bh * nx + (size_t)gm * bw;
+            for (int dn = 0; dn < blocks_y; ++dn)
+                for (int dm = 0; dm < blocks_x; ++dm) {
+                    float2 *dst = (float2 *)u_out + (size_t)dn * bh * nx + (size_t)dm * bw;
+                    // offsets as the reference forms them: an int times a float pitch, in float
+                    const double oy = (double)((float)((gn - dn) * bh) * (float)dy);
+                    const double ox = (double)((float)((gm - dm) * bw) * (float)dx);
+                    PropSetup S;
+                    int rc = propmode == OLG_ASM
+                                 ? setup_shifted_asm(src, dst, bh, bw, dy, dx, lambda, z, oy, ox, pflags, L, &S)
+                                 : setup_arss(src, dst, bh, bw, dy, dx, lambda, z, 1.0, oy, ox, pflags, L, &S, false);
+                    if (rc) return rc;
+                    S.P.in_ld = nx;
+                    S.P.out_ld = nx;
+                    S.P.accumulate = 1;
+                    if ((rc = run_setup(S, st))) return rc;
+                }
+        }
+    return OLG_OK;
 }
 
 // ------------------------------------------------------------- autotuner

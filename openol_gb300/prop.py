@@ -19,7 +19,8 @@ from enum import IntEnum
 import numpy as np
 import torch
 
-from ._lib import (OLG_CHECK_F32, OLG_CONJ, OLG_NO_NORMALIZE, OLG_VERBOSE, call, lib)
+from ._lib import (OLG_ACCUMULATE, OLG_BANDLIMIT, OLG_CHECK_F32, OLG_CONJ, OLG_NO_NORMALIZE, OLG_VERBOSE, call,
+                   lib)
 
 
 class PROPMODE(IntEnum):
@@ -167,6 +168,128 @@ def Prop(u, ny, nx, dy, dx, lam, d, propmode=PROPMODE.AUTO, verbose=True, single
 
 
 Prop.last_choice = -1
+
+
+# ------------------------------------------------------- shifted / split
+def _work(work):
+    return (work.data_ptr(), work.numel() * work.element_size()) if work is not None else (None, 0)
+
+
+def shifted_asm_prop(u_in, u_out=None, *, dy, dx, lam, z, oy, ox, bandlimit=False, window_f32=False, adjoint=False,
+                     normalize=True, stream=None, work=None):
+    """Shifted angular spectrum method (olg_shifted_asm_prop_c64): the destination
+    plane is offset by (oy, ox).  ``bandlimit`` adds the host overload's band
+    window (decided in float with ``window_f32``)."""
+    ny, nx = u_in.shape
+    _dev_field(u_in, ny, nx, "u_in")
+    u_out = u_in if u_out is None else _dev_field(u_out, ny, nx, "u_out")
+    flags = ((OLG_CONJ if adjoint else 0) | (0 if normalize else OLG_NO_NORMALIZE) |
+             (OLG_BANDLIMIT if bandlimit else 0) | (OLG_CHECK_F32 if window_f32 else 0))
+    wp, wb = _work(work)
+    call("olg_shifted_asm_prop_c64", u_in.data_ptr(), u_out.data_ptr(), ny, nx, float(dy), float(dx), float(lam),
+         float(z), float(oy), float(ox), flags, wp, wb, _stream(stream))
+    return u_out
+
+
+def shifted_fresnel_prop(u_src, u_dst=None, *, dy, dx, lam, z, s=1.0, oy=0.0, ox=0.0, adjoint=False, stream=None,
+                         work=None):
+    """Shifted (scaled) Fresnel propagation (olg_shifted_fresnel_prop_c64)."""
+    ny, nx = u_src.shape
+    _dev_field(u_src, ny, nx, "u_src")
+    u_dst = u_src if u_dst is None else _dev_field(u_dst, ny, nx, "u_dst")
+    wp, wb = _work(work)
+    call("olg_shifted_fresnel_prop_c64", u_src.data_ptr(), u_dst.data_ptr(), ny, nx, float(dy), float(dx), float(lam),
+         float(z), float(s), float(oy), float(ox), OLG_CONJ if adjoint else 0, wp, wb, _stream(stream))
+    return u_dst
+
+
+def split_workspace(ny, nx, blocks_y=2, blocks_x=2, device="cuda"):
+    n = int(lib().olg_split_prop_workspace_bytes(ny, nx, blocks_y, blocks_x))
+    return torch.empty(n, dtype=torch.uint8, device=device)
+
+
+def split_prop(u_in, u_out, *, dy, dx, lam, z, propmode=PROPMODE.ASM, blocks_y=2, blocks_x=2, bandlimit=False,
+               window_f32=False, accumulate=False, stream=None, work=None):
+    """Split propagation (olg_split_prop_c64): every (source, destination) block
+    pair adds a shifted propagation; ``u_out`` must be a separate tensor."""
+    ny, nx = u_in.shape
+    _dev_field(u_in, ny, nx, "u_in")
+    _dev_field(u_out, ny, nx, "u_out")
+    flags = ((OLG_BANDLIMIT if bandlimit else 0) | (OLG_CHECK_F32 if window_f32 else 0) |
+             (OLG_ACCUMULATE if accumulate else 0))
+    wp, wb = _work(work)
+    call("olg_split_prop_c64", u_in.data_ptr(), u_out.data_ptr(), ny, nx, float(dy), float(dx), float(lam), float(z),
+         int(propmode), int(blocks_y), int(blocks_x), flags, wp, wb, _stream(stream))
+    return u_out
+
+
+def gshiftedAsmProp(usrc, udst, ny, nx, dy, dx, lam, d, oy, ox):
+    """ol::gshiftedAsmProp, golprop.h:537-575 (device fields, no band window, 1/Np)."""
+    return shifted_asm_prop(_dev_field(usrc, ny, nx, "usrc").view(ny, nx), _dev_field(udst, ny, nx, "udst").view(ny, nx),
+                            dy=dy, dx=dx, lam=lam, z=d, oy=oy, ox=ox)
+
+
+def gshiftedFresnelProp(usrc, udst, ny, nx, dy, dx, lam, z, s, oy, ox):
+    """ol::gshiftedFresnelProp, golprop.h:706-752."""
+    return shifted_fresnel_prop(_dev_field(usrc, ny, nx, "usrc").view(ny, nx),
+                                _dev_field(udst, ny, nx, "udst").view(ny, nx), dy=dy, dx=dx, lam=lam, z=z, s=s, oy=oy,
+                                ox=ox)
+
+
+def shiftedProp(usrc, udst, ny, nx, dy, dx, lam, d, oy, ox, propmode):
+    """ol::shiftedProp, golprop.h:755-768: ASM or Fresnel (s = 1) on device fields."""
+    if int(propmode) == PROPMODE.ASM:
+        return gshiftedAsmProp(usrc, udst, ny, nx, dy, dx, lam, d, oy, ox)
+    if int(propmode) == PROPMODE.FRESNEL:
+        return gshiftedFresnelProp(usrc, udst, ny, nx, dy, dx, lam, d, 1.0, oy, ox)
+    raise ValueError("shiftedProp takes PROPMODE.ASM or PROPMODE.FRESNEL")
+
+
+def _host_c64(u, ny, nx):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(u).reshape(ny, nx), np.complex64)).cuda()
+
+
+def _write_host(u, d):
+    u[...] = d.cpu().numpy().reshape(u.shape).astype(u.dtype, copy=False)
+    return u
+
+
+def shiftedAsmProp(usrc, udst, height, width, dy, dx, lam, z, oy, ox):
+    """ol::shiftedAsmProp, olprop.h:307-327, on host arrays: the band window of
+    shiftedAsmTransferF (olprop.h:251-305) and 1/Np twice."""
+    d = _host_c64(usrc, height, width)
+    o = torch.empty_like(d)
+    shifted_asm_prop(d, o, dy=dy, dx=dx, lam=lam, z=z, oy=oy, ox=ox, bandlimit=True)
+    return _write_host(udst, o / (4.0 * height * width))
+
+
+def shiftedFresnelProp(u, height, width, dy, dx, lam, z, s, oy, ox):
+    """ol::shiftedFresnelProp, olprop.h:338-406, in place on a host array (its
+    normalisation carries one more 1/Np than the device version)."""
+    d = _host_c64(u, height, width)
+    shifted_fresnel_prop(d, dy=dy, dx=dx, lam=lam, z=z, s=s, oy=oy, ox=ox)
+    return _write_host(u, d / (4.0 * height * width))
+
+
+def splitAsmProp(u, height, width, dy, dx, lam, z, blocknum_y=2, blocknum_x=2):
+    """ol::splitAsmProp, olprop.h:618-654, in place on a host array: per-block
+    shiftedAsmProp (band window decided in float -- the template's only
+    instantiation is PREC_T = float -- and 1/Np_block twice)."""
+    d = _host_c64(u, height, width)
+    o = torch.empty_like(d)
+    split_prop(d, o, dy=dy, dx=dx, lam=lam, z=z, propmode=PROPMODE.ASM, blocks_y=blocknum_y, blocks_x=blocknum_x,
+               bandlimit=True, window_f32=True)
+    nb = 4.0 * (height // blocknum_y) * (width // blocknum_x)
+    return _write_host(u, o / nb)
+
+
+def gsplitProp(u, height, width, dy, dx, lam, z, propmode, blocknum_y=2, blocknum_x=2):
+    """ol::gsplitProp, golprop.h:772-813: a host field, each block pair through
+    the device shiftedProp (no band window)."""
+    d = _host_c64(u, height, width)
+    o = torch.empty_like(d)
+    split_prop(d, o, dy=dy, dx=dx, lam=lam, z=z, propmode=propmode, blocks_y=blocknum_y, blocks_x=blocknum_x)
+    return _write_host(u, o)
 
 
 # ------------------------------------------------------------------ autotuner

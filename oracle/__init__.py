@@ -58,6 +58,9 @@ def cpu():
         lib.olc_arss_prop.restype = _i
         lib.olc_arss_windows.argtypes = [_l, _l, _d, _d, _d, _d, _d, _p]
         lib.olc_arss_windows.restype = _i
+        lib.olc_shifted_asm_prop.argtypes = [_p, _p, _l, _l, _d, _d, _d, _d, _d, _d, _i]
+        lib.olc_split_prop.argtypes = [_p, _p, _l, _l, _d, _d, _d, _d, _i, _i, _i, _i]
+        lib.olc_split_prop.restype = _i
         lib.olc_asm_prop_check.argtypes = [_l, _l, _d, _d, _d, _d]
         lib.olc_fresnel_prop_check.argtypes = [_l, _l, _d, _d, _d, _d]
         lib.olc_cgh_fresnel.argtypes = [_p, _p, _p, _l, _p, _p, _l, _l, _d, _d, _d, _i]
@@ -94,6 +97,9 @@ def ref():
         lib.ref_cgh_phase.argtypes = [_p, _i, _p, _i, _i, _d, _d]
         lib.ref_complex2img.argtypes = [_p, _p, _i, _i, _i]
         lib.ref_quant8bit.argtypes = [_p, _p, _i, _i]
+        lib.ref_shifted_asm_prop.argtypes = [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d]
+        lib.ref_shifted_fresnel_prop.argtypes = [_p, _i, _i, _d, _d, _d, _d, _d, _d, _d]
+        lib.ref_split_asm_prop.argtypes = [_p, _i, _i, _d, _d, _d, _d, _i, _i]
         _REF = lib
     return _REF
 
@@ -121,6 +127,33 @@ def arss_prop(u, dy, dx, lam, z, s, oy=0.0, ox=0.0, flags=0):
     rc = cpu().olc_arss_prop(_ptr(u), _ptr(out), u.shape[0], u.shape[1], dy, dx, lam, z, s, oy, ox, flags)
     if rc != 0:
         raise ValueError("ARSS undefined for s in {0, 1}")
+    return out
+
+
+OLC_BANDLIMIT = 0x40
+OLC_NO_WINDOWS = 0x80
+
+
+def shifted_asm_prop(u, dy, dx, lam, z, oy, ox, flags=0):
+    """Shifted ASM (golprop.h:537-575); flags may add OLC_BANDLIMIT (olprop.h:251-305)."""
+    u = _c128(u)
+    out = np.empty_like(u)
+    cpu().olc_shifted_asm_prop(_ptr(u), _ptr(out), u.shape[0], u.shape[1], dy, dx, lam, z, oy, ox, flags)
+    return out
+
+
+def shifted_fresnel_prop(u, dy, dx, lam, z, s, oy=0.0, ox=0.0, flags=0):
+    """Shifted Fresnel (golprop.h:606-752): the ARSS chirps without windows."""
+    return arss_prop(u, dy, dx, lam, z, s, oy, ox, flags | OLC_NO_WINDOWS)
+
+
+def split_prop(u, dy, dx, lam, z, mode, blocks_y=2, blocks_x=2, flags=0):
+    """Split propagation (golprop.h:772-813); mode 0 ASM, 1 Fresnel (s = 1)."""
+    u = _c128(u)
+    out = np.zeros_like(u)
+    if cpu().olc_split_prop(_ptr(u), _ptr(out), u.shape[0], u.shape[1], dy, dx, lam, z, mode, blocks_y, blocks_x,
+                            flags) != 0:
+        raise ValueError("bad split arguments")
     return out
 
 

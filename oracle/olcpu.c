@@ -170,7 +170,11 @@ int olc_arss_prop(const double *srcd, double *dstd, long ny, long nx, double dy,
                   double lambda, double z, double s, double oy, double ox, int flags)
 {
     int64_t L[6];
-    if (olc_arss_windows(ny, nx, dy, dx, lambda, z, s, L)) return -1;
+    if (flags & OLC_NO_WINDOWS) {
+        for (int k = 0; k < 6; ++k) L[k] = 1073741824; /* every pixel inside */
+    } else if (olc_arss_windows(ny, nx, dy, dx, lambda, z, s, L)) {
+        return -1;
+    }
     const long hlim_u = L[0], wlim_u = L[1], lim_h = L[2], hlim_c = L[3], wlim_c = L[4];
     const long NY = 2 * ny, NX = 2 * nx, N = NY * NX, n = ny * nx;
     const double tmp = M_PI / (lambda * z);
@@ -245,6 +249,137 @@ int olc_arss_prop(const double *srcd, double *dstd, long ny, long nx, double dy,
     free(hb);
     free(U);
     free(a);
+    return 0;
+}
+
+/* ------------------------------------------------------ shifted ASM / split */
+/* band window of shiftedAsmTransferF olprop.h:254-284 for one axis, in double */
+static void shifted_band(double d, double o, double z, double lambda, double *c, double *w)
+{
+    const double s0 = 0.5 / d;
+    const double lm = 1 / sqrt(pow(o - 0.5 / d, -2) * z * z + 1.0) / lambda;
+    const double lp = 1 / sqrt(pow(o + 0.5 / d, -2) * z * z + 1.0) / lambda;
+    if (s0 < o) {
+        *c = 0.5 * (lp + lm);
+        *w = lp - lm;
+    } else if (-s0 <= o && o < s0) {
+        *c = 0.5 * (lp - lm);
+        *w = lp + lm;
+    } else {
+        *c = -0.5 * (lp + lm);
+        *w = lm - lp;
+    }
+}
+
+/* the same with PREC_T = float, each operation rounded as that instantiation
+ * rounds it: float operands, std::pow(float, int) and the sqrt in double,
+ * results stored to float (this file is built with -ffp-contract=off) */
+static void shifted_band_f(float d, float o, float z, float lambda, float *c, float *w)
+{
+    const float s0 = 0.5f / d;
+    volatile float tm = o - 0.5f / d, tp = o + 0.5f / d;
+    const float lm = (float)(1 / sqrt(pow((double)tm, -2) * z * z + 1.0f) / lambda);
+    const float lp = (float)(1 / sqrt(pow((double)tp, -2) * z * z + 1.0f) / lambda);
+    volatile float cc, ww;
+    if (s0 < o) {
+        cc = 0.5f * (lp + lm);
+        ww = lp - lm;
+    } else if (-s0 <= o && o < s0) {
+        cc = 0.5f * (lp - lm);
+        ww = lp + lm;
+    } else {
+        cc = -0.5f * (lp + lm);
+        ww = lm - lp;
+    }
+    *c = cc;
+    *w = ww;
+}
+
+void olc_shifted_asm_prop(const double *srcd, double *dstd, long ny, long nx, double dy, double dx, double lambda,
+                          double z, double oy, double ox, int flags)
+{
+    const long NY = 2 * ny, NX = 2 * nx, N = NY * NX;
+    const double du = 1.0 / (dx * NX), dv = 1.0 / (dy * NY);
+    cplx *U = pad2((const cplx *)srcd, ny, nx);
+    cplx *H = cz(N);
+    double u0 = 0, uw = 0, v0 = 0, vw = 0;
+    float u0f = 0, uwf = 0, v0f = 0, vwf = 0, duf = 0, dvf = 0;
+    const int band = flags & OLC_BANDLIMIT, f32 = flags & OLC_F32_WINDOW;
+    if (band && !f32) {
+        shifted_band(du, ox, z, lambda, &u0, &uw);
+        shifted_band(dv, oy, z, lambda, &v0, &vw);
+    } else if (band) {
+        /* shiftedAsmProp olprop.h:313-314: du = 1 / (dx * width2) in PREC_T */
+        duf = 1 / ((float)dx * (float)NX);
+        dvf = 1 / ((float)dy * (float)NY);
+        shifted_band_f(duf, (float)ox, (float)z, (float)lambda, &u0f, &uwf);
+        shifted_band_f(dvf, (float)oy, (float)z, (float)lambda, &v0f, &vwf);
+    }
+    const double tmp = 1.0 / (lambda * lambda);
+    /* gshiftedAsmTransferF golprop.h:336-358 / shiftedAsmTransferF olprop.h:286-304 */
+#pragma omp parallel for
+    for (long n = 0; n < NY; ++n) {
+        const double v = (double)(n - NY / 2) * dv;
+        for (long m = 0; m < NX; ++m) {
+            const double uu = (double)(m - NX / 2) * du;
+            if (band && !f32 && !(fabs(uu - u0) * 2 < uw && fabs(v - v0) * 2 < vw)) {
+                H[n * NX + m] = 0;
+                continue;
+            }
+            if (band && f32) {
+                const float uf = (float)(m - NX / 2) * duf, vf = (float)(n - NY / 2) * dvf;
+                if (!(fabsf(uf - u0f) * 2 < uwf && fabsf(vf - v0f) * 2 < vwf)) {
+                    H[n * NX + m] = 0;
+                    continue;
+                }
+            }
+            const double w = sqrt(tmp - uu * uu - v * v);
+            const double phase = 2 * M_PI * (w * z + ox * uu + oy * v);
+            H[n * NX + m] = cos(phase) + I * sin(phase);
+        }
+    }
+    fftshift2(H, NY, NX);
+    fft2(U, NY, NX, -1);
+    const double sc = (flags & OLC_NO_NORMALIZE) ? 1.0 : 1.0 / (double)N;
+    const int cj = flags & OLC_CONJ;
+#pragma omp parallel for
+    for (long i = 0; i < N; ++i) U[i] *= (cj ? conj(H[i]) : H[i]) * sc;
+    fft2(U, NY, NX, +1);
+    crop2(U, ny, nx, (cplx *)dstd);
+    free(H);
+    free(U);
+}
+
+int olc_split_prop(const double *srcd, double *dstd, long ny, long nx, double dy, double dx, double lambda, double z,
+                   int mode, int blocks_y, int blocks_x, int flags)
+{
+    if (blocks_y <= 0 || blocks_x <= 0 || (mode != 0 && mode != 1)) return -1;
+    const long bh = ny / blocks_y, bw = nx / blocks_x, nb = bh * bw;
+    const cplx *src = (const cplx *)srcd;
+    cplx *dst = (cplx *)dstd;
+    if (!(flags & OLC_ACCUMULATE)) memset(dst, 0, sizeof(cplx) * (size_t)(ny * nx));
+    cplx *a = cz(nb), *b = cz(nb);
+    for (long gn = 0; gn < blocks_y; ++gn)
+        for (long gm = 0; gm < blocks_x; ++gm) {
+            for (long h = 0; h < bh; ++h)
+                memcpy(a + h * bw, src + (gn * bh + h) * nx + gm * bw, sizeof(cplx) * (size_t)bw);
+            for (long dn = 0; dn < blocks_y; ++dn)
+                for (long dm = 0; dm < blocks_x; ++dm) {
+                    /* golprop.h:795-796: an int times a float pitch, in float */
+                    const double oy = (double)((float)((gn - dn) * bh) * (float)dy);
+                    const double ox = (double)((float)((gm - dm) * bw) * (float)dx);
+                    if (mode == 0)
+                        olc_shifted_asm_prop((const double *)a, (double *)b, bh, bw, dy, dx, lambda, z, oy, ox,
+                                             flags & (OLC_CONJ | OLC_NO_NORMALIZE | OLC_BANDLIMIT | OLC_F32_WINDOW));
+                    else
+                        olc_arss_prop((const double *)a, (double *)b, bh, bw, dy, dx, lambda, z, 1.0, oy, ox,
+                                      (flags & OLC_CONJ) | OLC_NO_WINDOWS);
+                    for (long h = 0; h < bh; ++h)
+                        for (long w = 0; w < bw; ++w) dst[(dn * bh + h) * nx + dm * bw + w] += b[h * bw + w];
+                }
+        }
+    free(a);
+    free(b);
     return 0;
 }
 

@@ -23,6 +23,9 @@ extern "C" {
 #define OLC_CONJ 0x1         /* adjoint: conjugate transfer function / swap+conjugate chirps */
 #define OLC_NO_NORMALIZE 0x2 /* host-pointer overload convention: no 1/Np factors */
 #define OLC_ACCUMULATE 0x4   /* U += result instead of U = result */
+#define OLC_F32_WINDOW 0x10  /* with OLC_BANDLIMIT: decide the window in float, as PREC_T = float does */
+#define OLC_BANDLIMIT 0x40   /* shifted ASM: the host overload's band window (olprop.h:251-305) */
+#define OLC_NO_WINDOWS 0x80  /* olc_arss_prop: no windows -- the shifted Fresnel propagation */
 
 /* Unnormalised 2-D DFT, sign -1 forward / +1 backward (FFTW/cuFFT convention). */
 void olc_fft2d(double *u, long ny, long nx, int sign, int nthreads);
@@ -45,9 +48,28 @@ void olc_fresnel_prop(double *u, long ny, long nx, double dy, double dx, double 
 /* ARSS Fresnel propagation, golprop.h:816-995 (the reference has no CPU ARSS).
  * src and dst are ny x nx and may alias.  Returns 0, or -1 for s in {0, 1}
  * (the reference's window limits divide by s*|s-1| and |1-s|).
- * OLC_CONJ applies the exact adjoint of that linear map. */
+ * OLC_CONJ applies the exact adjoint of that linear map.  OLC_NO_WINDOWS
+ * drops every window (any s): gshiftedFresnelProp golprop.h:606-752. */
 int olc_arss_prop(const double *src, double *dst, long ny, long nx, double dy, double dx,
                   double lambda, double z, double s, double oy, double ox, int flags);
+
+/* Shifted angular spectrum method, gshiftedAsmProp golprop.h:537-575 with
+ * gshiftedAsmTransferF golprop.h:335-420: H = exp(2 pi i (w z + ox u + oy v)),
+ * 1/Np (none with OLC_NO_NORMALIZE).  OLC_BANDLIMIT: H = 0 outside the band
+ * window of shiftedAsmTransferF olprop.h:251-305 (the host overload
+ * shiftedAsmProp olprop.h:307-327 also scales by a further 1/Np, which this
+ * function leaves to the caller).  OLC_CONJ: adjoint.  src, dst ny x nx. */
+void olc_shifted_asm_prop(const double *src, double *dst, long ny, long nx, double dy, double dx, double lambda,
+                          double z, double oy, double ox, int flags);
+
+/* Split propagation, gsplitProp golprop.h:772-813 / splitAsmProp
+ * olprop.h:618-654: dst = sum over (source, destination) block pairs of the
+ * shifted propagation (mode 0 ASM with the given flags, mode 1 shifted
+ * Fresnel with s = 1) of the source block into the destination block, with
+ * offsets (src - dst) * block size * pitch formed in float as the reference
+ * does.  dst must not alias src. */
+int olc_split_prop(const double *src, double *dst, long ny, long nx, double dy, double dx, double lambda, double z,
+                   int mode, int blocks_y, int blocks_x, int flags);
 
 /* ARSS window limits as the reference computes them: lims[0..5] =
  * {hlim_u, wlim_u, lim_h, hlim_cz, wlim_cz, unused}. */

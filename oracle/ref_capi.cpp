@@ -109,6 +109,35 @@ void ref_complex2img(const double *u, uint8_t *img, int ny, int nx, int mode)
     std::memcpy(img, I.get(), (long)ny * nx);
 }
 
+/* ol::shiftedAsmProp<double>, olprop.h:307-327 (band window, 1/Np twice) */
+void ref_shifted_asm_prop(const double *src, double *dst, int ny, int nx, double dy, double dx, double lam, double z,
+                          double oy, double ox)
+{
+    auto S = load(src, (long)ny * nx);
+    auto D = std::make_unique<cd[]>((long)ny * nx);
+    ol::shiftedAsmProp(S, D, (int64_t)ny, (int64_t)nx, dy, dx, lam, z, oy, ox);
+    store(D, dst, (long)ny * nx);
+}
+
+/* ol::shiftedFresnelProp<double>, olprop.h:338-406 (in place; no windows) */
+void ref_shifted_fresnel_prop(double *u, int ny, int nx, double dy, double dx, double lam, double z, double s,
+                              double oy, double ox)
+{
+    auto U = load(u, (long)ny * nx);
+    ol::shiftedFresnelProp(U, (int64_t)ny, (int64_t)nx, dy, dx, lam, z, s, oy, ox);
+    store(U, u, (long)ny * nx);
+}
+
+/* ol::splitAsmProp, olprop.h:618-654 (in place).  It only instantiates with
+ * PREC_T = float (it passes float block offsets to shiftedAsmProp), so the
+ * physical parameters and every phase are single precision there. */
+void ref_split_asm_prop(double *u, int ny, int nx, double dy, double dx, double lam, double z, int by, int bx)
+{
+    auto U = load(u, (long)ny * nx);
+    ol::splitAsmProp<float>(U, (int64_t)ny, (int64_t)nx, (float)dy, (float)dx, (float)lam, (float)z, by, bx);
+    store(U, u, (long)ny * nx);
+}
+
 /* ol::quant8bit, olimg.h:178-198 */
 void ref_quant8bit(double *real, uint8_t *img, int ny, int nx) { ol::quant8bit(real, img, ny, nx); }
 

@@ -4,7 +4,8 @@ The reference (somamake/openol) ships no golden vectors and no assertions, so
 the fixtures are made by running its CPU templates -- ``ol::AsmProp``,
 ``ol::FresnelProp``, ``ol::FresnelPropBandLimit``, ``ol::Prop``,
 ``ol::AsmPropCheck`` / ``ol::FresnelPropCheck``, ``ol::Cgh`` (complex and phase
-outputs), ``ol::complex2img`` and ``ol::quant8bit`` -- compiled unmodified by
+outputs), ``ol::complex2img``, ``ol::quant8bit``, ``ol::shiftedAsmProp``,
+``ol::shiftedFresnelProp`` and ``ol::splitAsmProp`` -- compiled unmodified by
 ``oracle/Makefile`` (``make -C oracle ref``; needs the reference sources) on
 seeded inputs.  Run from the repository root:
 
@@ -109,6 +110,34 @@ def main():
     img = np.zeros((16, 24), np.uint8)
     R.ref_quant8bit(O._ptr(real.copy()), O._ptr(img), 16, 24)
     g["q_quant8bit"] = img
+
+    # shifted / split propagation (a separate generator: the cases above stay as they were)
+    rs = np.random.default_rng(20261204)
+    shifted = [(32, 32, 8e-6, 8e-6, 532e-9, 0.02, 1e-4, -2e-4), (32, 64, 6e-6, 8e-6, 633e-9, 0.05, 3e-4, 5e-4),
+               (64, 32, 4e-6, 4e-6, 532e-9, -0.01, -1e-4, 2e-4), (32, 32, 8e-6, 8e-6, 532e-9, 0.02, 2.56e-4, 0.0)]
+    for i, (ny, nx, dy, dx, lam, z, oy, ox) in enumerate(shifted):
+        u = field(rs, (ny, nx))
+        d = np.zeros_like(u)
+        R.ref_shifted_asm_prop(O._ptr(np.ascontiguousarray(u)), O._ptr(d), ny, nx, dy, dx, lam, z, oy, ox)
+        g[f"shasm{i}_params"] = np.array([ny, nx, dy, dx, lam, z, oy, ox])
+        g[f"shasm{i}_in"] = u
+        g[f"shasm{i}_out"] = d
+    g["n_shasm"] = np.array(len(shifted))
+    shfr = [(32, 32, 8e-6, 8e-6, 532e-9, 0.02, 1.0, 1e-4, -2e-4), (32, 64, 6e-6, 8e-6, 633e-9, 0.05, 0.7, 3e-4, 5e-4),
+            (64, 32, 4e-6, 4e-6, 450e-9, -0.03, 1.3, 0.0, 1e-4)]
+    for i, (ny, nx, dy, dx, lam, z, sc, oy, ox) in enumerate(shfr):
+        u = field(rs, (ny, nx))
+        g[f"shfr{i}_params"] = np.array([ny, nx, dy, dx, lam, z, sc, oy, ox])
+        g[f"shfr{i}_in"] = u
+        g[f"shfr{i}_out"] = refcall(R.ref_shifted_fresnel_prop, u, dy, dx, lam, z, sc, oy, ox)
+    g["n_shfr"] = np.array(len(shfr))
+    split = [(64, 64, 8e-6, 8e-6, 532e-9, 0.01, 2, 2), (64, 128, 8e-6, 8e-6, 532e-9, 0.02, 2, 4)]
+    for i, (ny, nx, dy, dx, lam, z, by, bx) in enumerate(split):
+        u = field(rs, (ny, nx))
+        g[f"split{i}_params"] = np.array([ny, nx, dy, dx, lam, z, by, bx])
+        g[f"split{i}_in"] = u
+        g[f"split{i}_out"] = refcall(R.ref_split_asm_prop, u, dy, dx, lam, z, by, bx)
+    g["n_split"] = np.array(len(split))
 
     np.savez_compressed(OUT, **g)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")

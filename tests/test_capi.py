@@ -93,6 +93,12 @@ def test_argument_validation_without_gpu():
     assert b"s = 1" in L.olg_last_error() or b"s|s-1|" in L.olg_last_error()
     assert L.olg_cgh_fresnel_c64(None, None, None, 5, None, None, 8, 8, 8e-6, 8e-6, 532e-9, 0, None) == -1
     assert L.olg_prop_c64(base, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 7, 0, None, None, 0, None) == -1
+    # shifted / split: bad mode, blocks that do not divide the field, overlapping output
+    assert L.olg_shifted_prop_c64(base, base, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, 0, 2, 0, None, 0, None) == -1
+    assert L.olg_split_prop_c64(base, base + 16, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, 3, 2, 0, None, 0, None) == -1
+    assert L.olg_split_prop_c64(base, base, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, 2, 2, 0, None, 0, None) == -1
+    assert b"overlap" in L.olg_last_error()
+    assert L.olg_split_prop_c64(base, base + 16, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 2, 2, 2, 0, None, 0, None) == -1
 
 
 def test_workspace_size():

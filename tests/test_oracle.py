@@ -150,3 +150,80 @@ def test_arss_windows_and_rejects_s1():
     assert (w[:5] > 0).all()
     with pytest.raises(ValueError):
         O.arss_windows(64, 64, 8e-6, 8e-6, 532e-9, 0.05, 1.0)
+
+
+def _rel_or_zero(a, b):
+    nb = np.linalg.norm(b)
+    return rel_l2(a, b) if nb > 0 else np.abs(a).max()
+
+
+def test_golden_shifted_asm(golden):
+    """ol::shiftedAsmProp<double> (olprop.h:307-327): band window, 1/Np twice."""
+    for i in range(int(golden["n_shasm"])):
+        ny, nx, dy, dx, lam, z, oy, ox = golden[f"shasm{i}_params"]
+        out = O.shifted_asm_prop(golden[f"shasm{i}_in"], dy, dx, lam, z, oy, ox, flags=O.OLC_BANDLIMIT)
+        assert _rel_or_zero(out / (4 * ny * nx), golden[f"shasm{i}_out"]) < 1e-13, i
+
+
+def test_golden_shifted_fresnel(golden):
+    """ol::shiftedFresnelProp<double> (olprop.h:338-406): one more 1/Np than
+    gshiftedFresnelProp, which the oracle follows."""
+    for i in range(int(golden["n_shfr"])):
+        ny, nx, dy, dx, lam, z, s, oy, ox = golden[f"shfr{i}_params"]
+        out = O.shifted_fresnel_prop(golden[f"shfr{i}_in"], dy, dx, lam, z, s, oy, ox)
+        assert rel_l2(out / (4 * ny * nx), golden[f"shfr{i}_out"]) < 1e-13, i
+
+
+def test_golden_split_asm(golden):
+    """ol::splitAsmProp (olprop.h:618-654) only instantiates with PREC_T = float:
+    its phases are single precision (about 1e-2 of relative L2 against FP64;
+    a single-block split shows the same).  The oracle takes the float-rounded
+    parameters and decides the band windows in float like it; adjacent blocks
+    sit exactly on the window's branch boundary, where a double decision would
+    give a different window (about 0.8 relative L2)."""
+    f32 = lambda v: float(np.float32(v))
+    for i in range(int(golden["n_split"])):
+        ny, nx, dy, dx, lam, z, by, bx = golden[f"split{i}_params"]
+        ny, nx, by, bx = int(ny), int(nx), int(by), int(bx)
+        out = O.split_prop(golden[f"split{i}_in"], f32(dy), f32(dx), f32(lam), f32(z), 0, by, bx,
+                           flags=O.OLC_BANDLIMIT | 0x10)
+        out /= 4 * (ny // by) * (nx // bx)
+        assert rel_l2(out, golden[f"split{i}_out"]) < 2e-2, i
+        wrong = O.split_prop(golden[f"split{i}_in"], dy, dx, lam, z, 0, by, bx, flags=O.OLC_BANDLIMIT)
+        assert rel_l2(wrong / (4 * (ny // by) * (nx // bx)), golden[f"split{i}_out"]) > 0.3
+
+
+@pytest.mark.parametrize("kind", ["shifted_asm", "shifted_asm_band", "shifted_fresnel"])
+def test_shifted_adjoint_dot_product(kind):
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((32, 64)) + 1j * rng.standard_normal((32, 64))
+    y = rng.standard_normal((32, 64)) + 1j * rng.standard_normal((32, 64))
+    args = (6e-6, 8e-6, 633e-9, 0.03)
+    if kind == "shifted_fresnel":
+        A = lambda v, f: O.shifted_fresnel_prop(v, *args, 0.8, 2e-4, -1e-4, flags=f)
+    else:
+        band = O.OLC_BANDLIMIT if kind.endswith("band") else 0
+        A = lambda v, f: O.shifted_asm_prop(v, *args, 2e-4, -1e-4, flags=f | band)
+    lhs = np.vdot(y, A(x, 0))
+    rhs = np.vdot(A(y, 0x1), x)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_split_sums_shifted_blocks():
+    """Split propagation == sum of shifted propagations of the blocks."""
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal((32, 64)) + 1j * rng.standard_normal((32, 64))
+    args = (8e-6, 8e-6, 532e-9, 0.01)
+    out = O.split_prop(u, *args, 0, 2, 2)
+    ref = np.zeros_like(u)
+    for gn in range(2):
+        for gm in range(2):
+            blk = np.zeros_like(u)
+            blk[gn * 16:(gn + 1) * 16, gm * 32:(gm + 1) * 32] = u[gn * 16:(gn + 1) * 16, gm * 32:(gm + 1) * 32]
+            for dn in range(2):
+                for dm in range(2):
+                    oy = float(np.float32((gn - dn) * 16) * np.float32(8e-6))
+                    ox = float(np.float32((gm - dm) * 32) * np.float32(8e-6))
+                    s = O.shifted_asm_prop(u[gn * 16:(gn + 1) * 16, gm * 32:(gm + 1) * 32], *args, oy, ox)
+                    ref[dn * 16:(dn + 1) * 16, dm * 32:(dm + 1) * 32] += s
+    assert rel_l2(out, ref) < 1e-14
