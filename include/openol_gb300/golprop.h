@@ -122,6 +122,69 @@ void ARSSFresnelProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &usrc,
     ARSSFresnelProp(usrc, udst, ny, nx, dy, dx, lambda, z, s, (PREC_T)0, (PREC_T)0);
 }
 
+// gshiftedAsmProp, golprop.h:537-575 (no band window, 1/Np)
+template <typename COMPLEX_T, typename PREC_T>
+void gshiftedAsmProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &usrc,
+                     cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &udst, int ny, int nx, PREC_T dy, PREC_T dx,
+                     PREC_T lambda, PREC_T d, PREC_T oy, PREC_T ox)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    if (!udst) udst = cuda::make_unique<thrust::complex<COMPLEX_T>[]>((size_t)ny * nx);
+    olgb::check(olg_shifted_asm_prop_c64(usrc.get(), udst.get(), ny, nx, dy, dx, lambda, d, oy, ox, 0, nullptr, 0,
+                                         nullptr),
+                "gshiftedAsmProp");
+    olgb::sync("gshiftedAsmProp");
+}
+
+// gshiftedFresnelProp, golprop.h:706-752
+template <typename PREC_T = float, typename COMPLEX_T>
+void gshiftedFresnelProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &usrc,
+                         cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &udst, int ny, int nx, PREC_T dy, PREC_T dx,
+                         PREC_T lambda, PREC_T z, PREC_T s, PREC_T oy, PREC_T ox)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    if (!udst) udst = cuda::make_unique<thrust::complex<COMPLEX_T>[]>((size_t)ny * nx);
+    olgb::check(olg_shifted_fresnel_prop_c64(usrc.get(), udst.get(), ny, nx, dy, dx, lambda, z, s, oy, ox, 0, nullptr,
+                                             0, nullptr),
+                "gshiftedFresnelProp");
+    olgb::sync("gshiftedFresnelProp");
+}
+
+// shiftedProp, golprop.h:755-768 (an invalid mode throws where the reference exits)
+template <typename COMPLEX_T, typename PREC_T>
+void shiftedProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &usrc, cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &udst,
+                 int ny, int nx, PREC_T dy, PREC_T dx, PREC_T lambda, PREC_T d, PREC_T oy, PREC_T ox,
+                 PROPMODE propmode)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    if (!udst) udst = cuda::make_unique<thrust::complex<COMPLEX_T>[]>((size_t)ny * nx);
+    const int mode = propmode == PROPMODE::ASM ? OLG_ASM : propmode == PROPMODE::FRESNEL ? OLG_FRESNEL : -1;
+    olgb::check(olg_shifted_prop_c64(usrc.get(), udst.get(), ny, nx, dy, dx, lambda, d, oy, ox, mode, 0, nullptr, 0,
+                                     nullptr),
+                "shiftedProp");
+    olgb::sync("shiftedProp");
+}
+
+// gsplitProp, golprop.h:772-813: a host field; every block pair runs on the GPU
+template <typename PREC_T = float, typename COMPLEX_T>
+void gsplitProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int64_t height, int64_t width, PREC_T dy, PREC_T dx,
+                PREC_T lambda, PREC_T z, PROPMODE propmode, int blocknum_y = 2, int blocknum_x = 2)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    const int mode = propmode == PROPMODE::ASM ? OLG_ASM : propmode == PROPMODE::FRESNEL ? OLG_FRESNEL : -1;
+    const size_t bytes = sizeof(std::complex<float>) * (size_t)height * width;
+    void *a = nullptr, *b = nullptr;
+    CHECK_CUDA_ERROR(cudaMalloc(&a, bytes));
+    CHECK_CUDA_ERROR(cudaMalloc(&b, bytes));
+    CHECK_CUDA_ERROR(cudaMemcpy(a, u.get(), bytes, cudaMemcpyHostToDevice));
+    const int rc = olg_split_prop_c64(a, b, (int)height, (int)width, dy, dx, lambda, z, mode, blocknum_y, blocknum_x, 0,
+                                      nullptr, 0, nullptr);
+    if (rc == OLG_OK) CHECK_CUDA_ERROR(cudaMemcpy(u.get(), b, bytes, cudaMemcpyDeviceToHost));
+    CHECK_CUDA_ERROR(cudaFree(a));
+    CHECK_CUDA_ERROR(cudaFree(b));
+    olgb::check(rc, "gsplitProp");
+}
+
 // golprop.h:578-604 (prints the chosen method, as the reference does)
 template <typename COMPLEX_T, typename PREC_T>
 void Prop(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx, PREC_T lambda,

@@ -50,6 +50,17 @@ int main(int argc, char **argv)
     ol::ARSSFresnelProp(d_u, d_v, H, W, p / 0.5f, p / 0.5f, lambda, d, 0.5f);
     dump(out + "/arss.bin", d_v, H * W);
     ol::cpu2cuda(u, d_u, H * W);
+    ol::gshiftedAsmProp(d_u, d_v, H, W, p, p, lambda, d, 2e-4f, -1e-4f);
+    dump(out + "/shifted_asm.bin", d_v, H * W);
+    {
+        auto hs = std::make_unique<std::complex<PREC_T>[]>(H * W);
+        for (int i = 0; i < H * W; ++i) hs[i] = u[i];
+        ol::gsplitProp(hs, H, W, p, p, lambda, d, ol::PROPMODE::ASM, 2, 2);
+        FILE *f = fopen((out + "/split_asm.bin").c_str(), "wb");
+        fwrite(hs.get(), sizeof(std::complex<PREC_T>), H * W, f);
+        fclose(f);
+    }
+    ol::cpu2cuda(u, d_u, H * W);
     ol::Prop(d_u, H, W, p, p, lambda, d, ol::PROPMODE::AUTO);
     dump(out + "/prop_auto.bin", d_u, H * W);
     // host-pointer overload (no 1/Np)

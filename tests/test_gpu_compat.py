@@ -42,6 +42,9 @@ def test_compat_propagation(demo_out):
     assert rel_l2(load(out, "prop_auto"), O.prop(u, p, p, lam, d)) < 1e-5
     assert "AsmProp" in stdout
     assert rel_l2(load(out, "asm_host"), O.asm_prop(u, p, p, lam, d, flags=2)) < 1e-5
+    f = lambda v: float(np.float32(v))
+    assert rel_l2(load(out, "shifted_asm"), O.shifted_asm_prop(u, p, p, lam, d, f(2e-4), f(-1e-4))) < 1e-5
+    assert rel_l2(load(out, "split_asm"), O.split_prop(u, p, p, lam, d, 0, 2, 2)) < 1e-5
 
 
 def test_compat_cgh(demo_out):
