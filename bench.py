@@ -619,12 +619,19 @@ def run_ours(args):
         def step_serial():
             plan.execute_serial()
 
+        from openol_gb300.plain import plain_prop
+
+        def step_plain():
+            for f in fields:
+                plain_prop(f)
+
         with ClockSampler(local) as clk:
             l0 = og.launch_count()
             ms_direct = timed(torch, plan.execute, K, W, flush, stream, barrier)
             launches = (og.launch_count() - l0) // (K + W) * K
             ms = timed(torch, step, K, W, flush, stream, barrier)
             ms_serial = timed(torch, step_serial, K, W, flush, stream, barrier)
+            ms_plain = timed(torch, step_plain, K, W, flush, stream, barrier)
         clocks = clk.summary()
         plan.check()
         t_step = max_over_ranks(statistics.mean(ms))
@@ -636,6 +643,7 @@ def run_ours(args):
         splan = og.BatchPlan(small)
         ms_small = timed(torch, splan.execute, K, W, None, stream, barrier)
         ms_small_serial = timed(torch, splan.execute_serial, K, W, None, stream, barrier)
+        ms_small_plain = timed(torch, lambda: [plain_prop(f) for f in small], K, W, None, stream, barrier)
         splan.check()
         splan.close()
         hin = [f["u_in"].cpu().pin_memory() for f in fields]
@@ -668,10 +676,15 @@ def run_ours(args):
                       "persistent_direct": {"ms": statistics.mean(ms_direct)},
                       "serial_per_field": {"props/s": nprop * 1e3 / statistics.mean(ms_serial),
                                            "ms": statistics.mean(ms_serial)},
+                      "serial_plain_cufft": {"props/s": nprop * 1e3 / statistics.mean(ms_plain),
+                                             "ms": statistics.mean(ms_plain),
+                                             "note": "each field through the reference-structured cuFFT chain"},
                       "small_256sq_persistent": {"props/s": 96e3 / statistics.mean(ms_small),
                                                  "ms": statistics.mean(ms_small)},
                       "small_256sq_serial": {"props/s": 96e3 / statistics.mean(ms_small_serial),
-                                             "ms": statistics.mean(ms_small_serial)}},
+                                             "ms": statistics.mean(ms_small_serial)},
+                      "small_256sq_plain_cufft": {"props/s": 96e3 / statistics.mean(ms_small_plain),
+                                                  "ms": statistics.mean(ms_small_plain)}},
             "clocks": clocks,
         }
         plan.close()

@@ -16,6 +16,18 @@ extern "C" {
 int olg_plain_asm_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
                            double z, olg_stream_t stream);
 
+/* Fresnel the way golprop.h:167-198 chains it: pad, cuFFT forward, 1/Np,
+ * FP32 sampled response (golprop.h:9-30), fftshift, cuFFT forward, 1/Np,
+ * multiply, cuFFT inverse, crop.  Same cached plan and buffers. */
+int olg_plain_fresnel_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                               double z, olg_stream_t stream);
+
+/* ARSS the way golprop.h:941-988 chains it: FP32 windowed pre-chirp into
+ * u_dst, pad, FFT, 1/Np, windowed chirp, fftshift, FFT, 1/Np, multiply,
+ * IFFT, crop, FP32 windowed post-chirp.  u_src != u_dst. */
+int olg_plain_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx, double lambda,
+                            double z, double s, double oy, double ox, olg_stream_t stream);
+
 /* Fresnel-form CGH the way gCghShared (golcgh.h:47-88) computes it: one
  * thread per pixel, points staged in shared memory, FP32 phase with
  * full-precision sin/cos.  Unit amplitudes. */

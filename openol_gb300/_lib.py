@@ -73,6 +73,8 @@ SIGNATURES = {
     "olg_wrp_step1_c64": (_i, [_p, _i, _p, _i, _i, _f, _f, _f, _f, _i, _p]),
     "olg_wrp_method_c64": (_i, [_p, _i, _p, _i, _i, _f, _f, _f, _f, _f, _i, _i, _i, C.POINTER(_f), _p]),
     "olg_plain_asm_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _p]),
+    "olg_plain_fresnel_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _p]),
+    "olg_plain_arss_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _d, _p]),
     "olg_plain_cgh_fresnel_c64": (_i, [_p, _i, _p, _i, _i, _d, _d, _p]),
     "olg_complex2img_u8": (_i, [_p, _p, _i, _i, _i, _p]),
     "olg_binarize_u8": (_i, [_p, _p, _i, _i, _p]),

@@ -6,6 +6,10 @@
 //    1/Np scale, transfer function in FP32 (golprop.h:307-322), fftshift,
 //    multiply, cuFFT inverse, crop -- one kernel per step (cuFFT plan and
 //    buffers cached per size rather than created per call).
+//  * Fresnel as golprop.h:167-198: pad, FFT, 1/Np, the sampled response
+//    (FP32, golprop.h:9-30), fftshift, FFT, 1/Np, multiply, IFFT, crop.
+//  * ARSS as golprop.h:941-988: windowed pre-chirp, pad, FFT, 1/Np, windowed
+//    chirp, fftshift, FFT, 1/Np, multiply, IFFT, crop, windowed post-chirp.
 //  * Fresnel-form CGH as gCghShared (golcgh.h:47-88): one thread per pixel,
 //    points staged through shared memory, FP32 phase, full-precision sin/cos.
 // Not used by any product path.
@@ -72,6 +76,41 @@ __global__ void k_crop(const float2 *in, float2 *out, int ny, int nx)
     out[(size_t)h * nx + w] = in[(size_t)(h + ny / 2) * (2 * nx) + (w + nx / 2)];
 }
 
+__global__ void k_fresnel_h(float2 *h, int NY, int NX, float dy, float dx, float lambda, float z, float s, int lim)
+{
+    const int w = blockIdx.x * blockDim.x + threadIdx.x, hh = blockIdx.y * blockDim.y + threadIdx.y;
+    if (w >= NX || hh >= NY) return;
+    const int cy = NY / 2, cx = NX / 2;
+    float2 v = make_float2(0.f, 0.f);
+    if (lim < 0 || (abs(w - cx) < lim && abs(hh - cy) < lim)) {
+        const float y = (hh - cy) * dy, x = (w - cx) * dx;
+        const float ph = 3.14159265358979f / (lambda * z) * s * (x * x + y * y);
+        v = make_float2(cosf(ph), sinf(ph));
+    }
+    h[(size_t)hh * NX + w] = v;
+}
+
+// ARSS pre-chirp (mode 0: zero outside its window) and post-chirp (mode 1:
+// identity outside its window), in FP32 like golprop.h:817-843 / 901-922
+__global__ void k_arss_chirp(const float2 *in, float2 *out, int ny, int nx, float dy, float dx, float lambda, float z,
+                             float s, float oy, float ox, int hlim, int wlim, int mode)
+{
+    const int w = blockIdx.x * blockDim.x + threadIdx.x, h = blockIdx.y * blockDim.y + threadIdx.y;
+    if (w >= nx || h >= ny) return;
+    const size_t i = (size_t)h * nx + w;
+    const bool inside = abs(w - nx / 2) < wlim && abs(h - ny / 2) < hlim;
+    if (!inside) {
+        out[i] = mode == 0 ? make_float2(0.f, 0.f) : in[i];
+        return;
+    }
+    const float tmp = 3.14159265358979f / (lambda * z);
+    const float y = (h - ny / 2) * dy, x = (w - nx / 2) * dx;
+    float ph = mode == 0 ? (s * s - s) * (x * x + y * y) - 2 * s * (ox * x + oy * y)
+                         : (1 - s) * (x * x + y * y) + 2 * (ox * x + oy * y) + ox * ox + oy * oy;
+    ph *= tmp;
+    out[i] = cmul(in[i], make_float2(cosf(ph), sinf(ph)));
+}
+
 __global__ void k_cgh_shared(const float *pts, int n, float2 *U, int ny, int nx, float p, float lambda)
 {
     const int w = blockIdx.x * blockDim.x + threadIdx.x, h = blockIdx.y * blockDim.y + threadIdx.y;
@@ -122,6 +161,59 @@ int get_plan(int ny, int nx, Plan **out)
     return OLG_OK;
 }
 
+// plain Fresnel / ARSS: the convolution form with the response's spectrum
+// formed per call, as golprop.h:167-198 and 941-988 do
+static int plain_conv(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda, double z,
+                      bool arss, double s, double oy, double ox, cudaStream_t st)
+{
+    Plan *P = nullptr;
+    if (int rc = get_plan(ny, nx, &P)) return rc;
+    if (cufftSetStream(P->h, st) != CUFFT_SUCCESS) return fail(OLG_ERR_CUDA, "cufftSetStream");
+    const int NY = 2 * ny, NX = 2 * nx;
+    const long Np = (long)NY * NX;
+    dim3 blk(16, 16), g2((NX + 15) / 16, (NY + 15) / 16), g1((nx + 15) / 16, (ny + 15) / 16),
+        gs((NX / 2 + 15) / 16, (NY / 2 + 15) / 16);
+    const int lin = (int)((Np + 255) / 256);
+    const float inv = (float)(1.0 / (double)Np);
+    const float *src = (const float *)u_in;
+    int launches = 0;
+    int hlim_u = 0, wlim_u = 0, lim_h = -1, hlim_c = 0, wlim_c = 0;
+    if (arss) {
+        hlim_u = (int)std::floor(lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dy) / dy);
+        wlim_u = (int)std::floor(lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dx) / dx);
+        lim_h = (int)std::floor(std::fabs(lambda * z * 0.5 / (dx * s)) / dx);
+        hlim_c = (int)std::floor(lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dy) / dy);
+        wlim_c = (int)std::floor(lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dx) / dx);
+        // the pre-chirp goes to the output field first (udst in the reference)
+        k_arss_chirp<<<g1, blk, 0, st>>>((const float2 *)u_in, (float2 *)u_out, ny, nx, (float)dy, (float)dx,
+                                         (float)lambda, (float)z, (float)s, (float)oy, (float)ox, hlim_u, wlim_u, 0);
+        ++launches;
+        src = (const float *)u_out;
+    }
+    k_pad<<<g2, blk, 0, st>>>((const float2 *)src, P->b1, ny, nx);
+    if (cufftExecC2C(P->h, (cufftComplex *)P->b1, (cufftComplex *)P->b1, CUFFT_FORWARD) != CUFFT_SUCCESS)
+        return fail(OLG_ERR_CUDA, "cufftExecC2C");
+    k_scale<<<lin, 256, 0, st>>>(P->b1, Np, inv);
+    k_fresnel_h<<<g2, blk, 0, st>>>(P->b2, NY, NX, (float)dy, (float)dx, (float)lambda, (float)z,
+                                    arss ? (float)s : 1.0f, lim_h);
+    k_fftshift<<<gs, blk, 0, st>>>(P->b2, NY, NX);
+    if (cufftExecC2C(P->h, (cufftComplex *)P->b2, (cufftComplex *)P->b2, CUFFT_FORWARD) != CUFFT_SUCCESS)
+        return fail(OLG_ERR_CUDA, "cufftExecC2C");
+    k_scale<<<lin, 256, 0, st>>>(P->b2, Np, inv);
+    k_mult<<<lin, 256, 0, st>>>(P->b1, P->b2, Np);
+    if (cufftExecC2C(P->h, (cufftComplex *)P->b1, (cufftComplex *)P->b1, CUFFT_INVERSE) != CUFFT_SUCCESS)
+        return fail(OLG_ERR_CUDA, "cufftExecC2C");
+    k_crop<<<g1, blk, 0, st>>>(P->b1, (float2 *)u_out, ny, nx);
+    launches += 7;
+    if (arss) {
+        k_arss_chirp<<<g1, blk, 0, st>>>((const float2 *)u_out, (float2 *)u_out, ny, nx, (float)dy, (float)dx,
+                                         (float)lambda, (float)z, (float)s, (float)oy, (float)ox, hlim_c, wlim_c, 1);
+        ++launches;
+    }
+    count_launch(launches);
+    return check_launch("plain convolution propagation");
+}
+
 } // namespace plain
 } // namespace olg
 
@@ -164,4 +256,19 @@ extern "C" int olg_plain_cgh_fresnel_c64(const float *points, int n_points, void
     k_cgh_shared<<<g, blk, 0, (cudaStream_t)stream>>>(points, n_points, (float2 *)U, ny, nx, (float)p, (float)lambda);
     count_launch();
     return check_launch("plain cgh");
+}
+
+extern "C" int olg_plain_fresnel_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx,
+                                          double lambda, double z, olg_stream_t stream)
+{
+    if (!u_in || !u_out || ny <= 0 || nx <= 0) return fail(OLG_ERR_INVALID_ARG, "bad arguments");
+    return plain_conv(u_in, u_out, ny, nx, dy, dx, lambda, z, false, 1.0, 0.0, 0.0, (cudaStream_t)stream);
+}
+
+extern "C" int olg_plain_arss_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double dy, double dx,
+                                       double lambda, double z, double s, double oy, double ox, olg_stream_t stream)
+{
+    if (!u_src || !u_dst || ny <= 0 || nx <= 0 || s == 0.0 || s == 1.0) return fail(OLG_ERR_INVALID_ARG, "bad arguments");
+    if (u_src == u_dst) return fail(OLG_ERR_INVALID_ARG, "plain ARSS writes its pre-chirp into u_dst: u_src != u_dst");
+    return plain_conv(u_src, u_dst, ny, nx, dy, dx, lambda, z, true, s, oy, ox, (cudaStream_t)stream);
 }

@@ -1754,10 +1754,12 @@ namespace olg {
 
 constexpr int BATCH_NT = 512;
 constexpr int BATCH_CTAS_PER_SM = 1;
-// rows per row unit and columns per column tile: 8192 elements per unit
-__host__ __device__ constexpr int brow_nseq(int N) { return FFT_MAX / N; }
-__host__ __device__ constexpr int bcol_c(int N) { return FFT_MAX / N; }
-constexpr int BATCH_SMEM = padded_len(FFT_MAX) * 8; // 8192 elements: the largest pass tile
+// rows per row unit and columns per column tile: 16384 elements per unit
+// (two 8192-point columns, as the fastest single-call column shape)
+constexpr int BATCH_TILE = 2 * FFT_MAX;
+__host__ __device__ constexpr int brow_nseq(int N) { return BATCH_TILE / N; }
+__host__ __device__ constexpr int bcol_c(int N) { return BATCH_TILE / N; }
+constexpr int BATCH_SMEM = padded_len(FFT_MAX) * 2 * 8; // the largest pass tile
 constexpr long long BATCH_WAIT = 4000000000LL;           // ~2 s of SM clock
 
 enum : int { BK_CHIRP = 0, BK_FWD = 1, BK_COLS = 2, BK_INV = 3 };
@@ -1766,7 +1768,7 @@ struct BatchItem {
     int field, kind, unit, n; // n: FFT length that selects the instantiation
     int count;                // consecutive units processed by this item
 };
-constexpr int BATCH_UNITS_PER_ITEM = 16; // 16 x 8192 elements per item
+constexpr int BATCH_UNITS_PER_ITEM = 8; // 8 x 16384 elements per item
 
 struct BatchDev {
     const PropParams *P;

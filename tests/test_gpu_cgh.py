@@ -144,6 +144,11 @@ def test_plain_forms_run_and_are_close():
     src = torch.from_numpy(u0).cuda()
     out = plain_asm_prop(src, torch.empty_like(src), dy=8e-6, dx=8e-6, lam=532e-9, z=0.05)
     assert rel_l2(host(out), O.asm_prop(u0.astype(np.complex128), 8e-6, 8e-6, 532e-9, 0.05)) < 0.1
+    from openol_gb300.plain import plain_arss_prop, plain_fresnel_prop
+    out = plain_fresnel_prop(src, torch.empty_like(src), dy=8e-6, dx=8e-6, lam=532e-9, z=0.05)
+    assert rel_l2(host(out), O.fresnel_prop(u0.astype(np.complex128), 8e-6, 8e-6, 532e-9, 0.05)) < 1e-2
+    out = plain_arss_prop(src, torch.empty_like(src), dy=8e-6, dx=8e-6, lam=532e-9, z=0.05, s=0.5)
+    assert rel_l2(host(out), O.arss_prop(u0.astype(np.complex128), 8e-6, 8e-6, 532e-9, 0.05, 0.5)) < 1e-2
     pts = np.stack([rng.random(200) * 64 * 8e-6, rng.random(200) * 48 * 8e-6, 0.05 + rng.random(200) * 0.01], 1)
     U = torch.zeros((48, 64), dtype=torch.complex64, device="cuda")
     plain_cgh_fresnel(og.gObject(pts), U, ny=48, nx=64, p=8e-6, lam=532e-9)
