@@ -22,8 +22,10 @@
  *    pool (cudaMallocAsync / cudaFreeAsync on `stream`).
  *  - In-place operation is allowed wherever an input and an output pointer
  *    have the same shape (u_in == u_out).
- *  - Sizes: the FFT engine handles ny, nx powers of two in [16, 4096]
- *    (padded grid 32 .. 8192); other sizes return OLG_ERR_UNSUPPORTED_SIZE.
+ *  - Sizes: each axis n (ny or nx) is a power of two in [16, 4096] (tuned
+ *    passes, padded 32 .. 8192), or has a padded length 2n = 2^a 3^b 5^c up
+ *    to 7680 with n >= 8 (mixed-radix passes; e.g. 3840 x 2160).  Other
+ *    sizes return OLG_ERR_UNSUPPORTED_SIZE.
  */
 #ifndef OLGB300_H
 #define OLGB300_H

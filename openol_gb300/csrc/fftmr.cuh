@@ -1,0 +1,139 @@
+// fftmr.cuh -- mixed-radix in-shared-memory Stockham FFT with a run-time
+// stage plan (sm_103a).
+//
+// Lengths N = 2^a 3^b 5^c that are not powers of two run through here: the
+// reference's default field 3840 x 2160 pads to 7680 x 4320.  The plan is a
+// list of radices from {16, 8, 4, 2, 5, 3} (powers of two first); every
+// stage is the same in-place Stockham step as fft.cuh (read all R inputs
+// into registers, barrier, write the R outputs), with twiddles
+// exp(-2 pi i m / N) from a per-length table.  Layouts as fft.cuh: rows
+// (q * ss + pidx(i)) or column tiles (pidx(i) * nseq + q).
+#pragma once
+#include "fft.cuh"
+#include "propdev.cuh"
+
+namespace olg {
+
+// X[k] = sum_n x[n] w^(n k), w = exp(DIR 2 pi i / 3): natural output order
+template <int DIR>
+__device__ __forceinline__ void dft3(float2 (&v)[3])
+{
+    constexpr float S3 = 0.86602540378443865f; // sin(2 pi / 3)
+    const float2 s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+    const float2 a = v[0];
+    const float2 t = make_float2(a.x - 0.5f * s.x, a.y - 0.5f * s.y);
+    // (DIR i) sin(2 pi / 3) d
+    const float2 id = DIR < 0 ? make_float2(S3 * d.y, -S3 * d.x) : make_float2(-S3 * d.y, S3 * d.x);
+    v[0] = cadd(a, s);
+    v[1] = cadd(t, id);
+    v[2] = csub(t, id);
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft5(float2 (&v)[5])
+{
+    constexpr float C1 = 0.30901699437494742f, C2 = -0.80901699437494742f; // cos(2 pi / 5), cos(4 pi / 5)
+    constexpr float S1 = 0.95105651629515357f, S2 = 0.58778525229247313f;  // sin(2 pi / 5), sin(4 pi / 5)
+    const float2 a = v[0];
+    const float2 s1 = cadd(v[1], v[4]), d1 = csub(v[1], v[4]), s2 = cadd(v[2], v[3]), d2 = csub(v[2], v[3]);
+    const float2 r1 = make_float2(a.x + C1 * s1.x + C2 * s2.x, a.y + C1 * s1.y + C2 * s2.y);
+    const float2 r2 = make_float2(a.x + C2 * s1.x + C1 * s2.x, a.y + C2 * s1.y + C1 * s2.y);
+    const float2 q1 = make_float2(S1 * d1.x + S2 * d2.x, S1 * d1.y + S2 * d2.y);
+    const float2 q2 = make_float2(S2 * d1.x - S1 * d2.x, S2 * d1.y - S1 * d2.y);
+    // (DIR i) q
+    const float2 i1 = DIR < 0 ? make_float2(q1.y, -q1.x) : make_float2(-q1.y, q1.x);
+    const float2 i2 = DIR < 0 ? make_float2(q2.y, -q2.x) : make_float2(-q2.y, q2.x);
+    v[0] = cadd(a, cadd(s1, s2));
+    v[1] = cadd(r1, i1);
+    v[4] = csub(r1, i1);
+    v[2] = cadd(r2, i2);
+    v[3] = csub(r2, i2);
+}
+
+template <int R, int DIR>
+__device__ __forceinline__ void mr_dft(float2 (&v)[R])
+{
+    if constexpr (R == 3) dft3<DIR>(v);
+    else if constexpr (R == 5) dft5<DIR>(v);
+    else dft<R, DIR>(v);
+}
+
+// twiddle m of the per-length table (forward), conjugated for DIR > 0
+template <int DIR>
+__device__ __forceinline__ float2 mr_twid(const float2 *__restrict__ tw, int m)
+{
+    const float2 w = __ldg(tw + m);
+    return DIR < 0 ? w : make_float2(w.x, -w.y);
+}
+
+// complex values a thread holds in one stage; a radix-R stage covers at most
+// NT * (MR_VALS / R) butterflies, and the host sizes nseq (mr_nseq) so that
+// every stage of the plan stays within that.
+constexpr int MR_VALS = 16;
+
+// One radix-R stage over nseq sequences of length N (NS = radices already
+// applied).
+template <int R, int DIR, int NT, bool COLS>
+__device__ __forceinline__ void mr_stage(float2 *s, int ss, int nseq, int N, int NS, const float2 *__restrict__ tw,
+                                         int tid)
+{
+    constexpr int BMAX = MR_VALS / R;
+    const int B = N / R, BT = nseq * B, L = NS * R, step = N / L;
+    float2 v[BMAX][R];
+#pragma unroll
+    for (int t = 0; t < BMAX; ++t) {
+        const int b = tid + t * NT;
+        if (b >= BT) continue;
+        const int q = COLS ? b % nseq : b / B;
+        const int j = COLS ? b / nseq : b % B;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int i = j + r * B;
+            v[t][r] = s[COLS ? pidx(i) * nseq + q : q * ss + pidx(i)];
+        }
+        if (NS > 1) {
+            const int k = j % NS;
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[t][r] = cmul(v[t][r], mr_twid<DIR>(tw, r * k * step));
+        }
+        mr_dft<R, DIR>(v[t]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < BMAX; ++t) {
+        const int b = tid + t * NT;
+        if (b >= BT) continue;
+        const int q = COLS ? b % nseq : b / B;
+        const int j = COLS ? b / nseq : b % B;
+        const int k = j % NS, base = (j / NS) * L + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int i = base + r * NS;
+            s[COLS ? pidx(i) * nseq + q : q * ss + pidx(i)] = v[t][outpos<R>(r)];
+        }
+    }
+    __syncthreads();
+}
+
+// The whole transform of nseq sequences in place (unnormalised); all NT
+// threads of the CTA call it after a barrier that follows the loads.
+template <int DIR, int NT, bool COLS>
+__device__ __forceinline__ void mr_fft(float2 *s, int ss, int nseq, const MrPlan &pl, const float2 *__restrict__ tw,
+                                       int tid)
+{
+    int NS = 1;
+    for (int i = 0; i < pl.nst; ++i) {
+        const int R = (int)((pl.radices >> (5 * i)) & 31);
+        switch (R) {
+        case 16: mr_stage<16, DIR, NT, COLS>(s, ss, nseq, pl.n, NS, tw, tid); break;
+        case 8: mr_stage<8, DIR, NT, COLS>(s, ss, nseq, pl.n, NS, tw, tid); break;
+        case 4: mr_stage<4, DIR, NT, COLS>(s, ss, nseq, pl.n, NS, tw, tid); break;
+        case 2: mr_stage<2, DIR, NT, COLS>(s, ss, nseq, pl.n, NS, tw, tid); break;
+        case 5: mr_stage<5, DIR, NT, COLS>(s, ss, nseq, pl.n, NS, tw, tid); break;
+        default: mr_stage<3, DIR, NT, COLS>(s, ss, nseq, pl.n, NS, tw, tid); break;
+        }
+        NS *= R;
+    }
+}
+
+} // namespace olg

@@ -33,65 +33,14 @@
 #include "fft.cuh"
 #include "fft2.cuh"
 #include "fftp.cuh"
+#include "propdev.cuh"
+#include "propmr.cuh"
 
 namespace olg {
-
-// Programmatic dependent launch: a pass lets the next one launch as soon as all
-// of its CTAs are running, and waits for the previous grid's completion (and
-// memory) before touching any field data.  Both are no-ops when the launch
-// carries no programmatic-serialisation attribute.
-__device__ __forceinline__ void pdl_enter()
-{
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-}
 
 static __device__ float2 g_tw[FFT_MAX];
 // the same table as (c, c, s, s) for the paired-sequence passes
 static __device__ float4 g_tw4[FFT_MAX];
-
-enum : int { M_ASM = 0, M_CHIRP = 1 };
-// pre/post operation modes
-enum : int { OP_NONE = 0, OP_TABLE = 1, OP_TABLE_IN_WINDOW = 2, OP_SEED = 3 };
-
-struct PropParams {
-    int ny, nx, NY, NX;
-    int method;     // M_ASM: T computed in registers; M_CHIRP: T = Hx[kx] * Hy[ky]
-    int conj;       // conjugate T (adjoint)
-    float scale;    // folded into T
-    // ASM transfer function constants (cycles)
-    float c0;               // frac(z / lambda)
-    float ax_hi, ax_lo;     // z lambda du^2 / 2
-    float ay_hi, ay_lo;     // z lambda dv^2 / 2
-    float tx, ty;           // lambda^2 du^2, lambda^2 dv^2
-    float zl;               // z / lambda
-    // chirp spectra (M_CHIRP)
-    const float2 *Hx, *Hy;
-    // pass-1 and pass-3 elementwise operations
-    int pre_mode, post_mode;
-    const float2 *prex, *prey, *postx, *posty;
-    int pre_hlim, pre_wlim, post_hlim, post_wlim;
-    int accumulate;
-    const float2 *in;
-    float2 *out;
-    float2 *S;
-    // phase-only input (pass 1 reads phi and forms exp(i phi)) when non-null
-    const float *in_phase;
-    // OP_SEED (pass 3): out = seed_scale (|v|^2 - target) v, loss += sum (|v|^2 - target)^2
-    const float *target;
-    float seed_scale;
-    double *loss;
-    // tables written earlier in the same launch (batched persistent kernel):
-    // read them through L2 (ld.global.cg), never the non-coherent path
-    int coherent;
-    // row strides (elements) of in / in_phase and of out (sub-blocks of a larger field)
-    long in_ld, out_ld;
-    // shifted ASM: extra phase ox u + oy v = lx fx + ly fy cycles; optional band
-    // window fx in [fx_lo, fx_hi], fy in [fy_lo, fy_hi] (T = 0 outside)
-    int shift, band;
-    float lx_hi, lx_lo, ly_hi, ly_lo;
-    int fx_lo, fx_hi, fy_lo, fy_hi;
-};
 
 // ---------------------------------------------------------------- launch shapes
 template <int N>
@@ -107,28 +56,6 @@ struct ColCfg {
     static constexpr int NT = E / 16;                  // 1 radix-16 butterfly per thread per stage
     static constexpr int SMEM = padded_len(N) * C * 8;
 };
-
-__device__ __forceinline__ float2 apply_op(float2 v, int mode, const float2 *tx, const float2 *ty, int h, int w,
-                                           int ny, int nx, int hlim, int wlim)
-{
-    if (mode == OP_NONE) return v;
-    if (mode == OP_TABLE_IN_WINDOW) {
-        if (!(abs(w - nx / 2) < wlim && abs(h - ny / 2) < hlim)) return v;
-    }
-    return cmul(v, cmul(__ldg(tx + w), __ldg(ty + h)));
-}
-
-__device__ __forceinline__ float2 ld_tab(const float2 *p, int coherent) { return coherent ? __ldcg(p) : __ldg(p); }
-
-__device__ __forceinline__ float2 apply_op_c(float2 v, int mode, const float2 *tx, const float2 *ty, int h, int w,
-                                             int ny, int nx, int hlim, int wlim, int coherent)
-{
-    if (mode == OP_NONE) return v;
-    if (mode == OP_TABLE_IN_WINDOW) {
-        if (!(abs(w - nx / 2) < wlim && abs(h - ny / 2) < hlim)) return v;
-    }
-    return cmul(v, cmul(ld_tab(tx + w, coherent), ld_tab(ty + h, coherent)));
-}
 
 // ------------------------------------------------------------------- pass 1
 template <int N>
@@ -238,29 +165,6 @@ __global__ void __launch_bounds__(RowCfg<N>::NT) k_rows_inv(PropParams P)
     }
 }
 
-// ASM transfer function exp(2 pi i z w) at (fx, fy), cycles evaluated as
-//   frac(z/lambda) - ax fx^2 - ay fy^2 - (z/lambda) t^2 / (2 (1 + sqrt(1-t))^2)
-// with t = lambda^2 (u^2 + v^2): the exact expansion of z sqrt(1/lambda^2 - u^2 - v^2).
-// The two quadratic terms are reduced exactly (frac_mul); the remainder is
-// a few cycles at most, so FP32 keeps ~1e-6 rad of phase.  t > 1 gives NaN,
-// as sqrt of a negative argument does in the reference (golprop.h:318).
-__device__ __forceinline__ float2 asm_tf(const PropParams &P, int fx, int fy)
-{
-    const float fx2 = (float)(fx * fx), fy2 = (float)(fy * fy);
-    const float t = P.tx * fx2 + P.ty * fy2;
-    const float s = sqrtf(1.0f - t);
-    const float q = t / (1.0f + s);
-    const float g = 0.5f * q * q;
-    float cyc = P.c0 - frac_mul(P.ax_hi, P.ax_lo, fx2) - frac_mul(P.ay_hi, P.ay_lo, fy2) - P.zl * g;
-    if (P.shift) {
-        if (P.band && (fx < P.fx_lo || fx > P.fx_hi || fy < P.fy_lo || fy > P.fy_hi)) return make_float2(0.f, 0.f);
-        cyc += frac_mul(P.lx_hi, P.lx_lo, (float)fx) + frac_mul(P.ly_hi, P.ly_lo, (float)fy);
-    }
-    cyc = wrap_cycles(cyc);
-    if (P.conj) cyc = -cyc;
-    return cscale(cis_cycles(cyc), P.scale);
-}
-
 // ------------------------------------------------------------------- pass 2
 template <int N>
 __global__ void __launch_bounds__(ColCfg<N>::NT) k_cols(PropParams P)
@@ -317,18 +221,6 @@ __global__ void __launch_bounds__(ColCfg<N>::NT) k_cols(PropParams P)
 
 // =========================================================== v2 passes
 // N >= 256: register-resident first / last radix-16 stages (fft2.cuh).
-__device__ __forceinline__ float2 load_in(const PropParams &P, int h, int w)
-{
-    float2 x;
-    if (P.in_phase) {
-        const float ph = __ldg(P.in_phase + (size_t)h * P.in_ld + w);
-        sincosf(ph, &x.y, &x.x);
-    } else {
-        x = __ldg(P.in + (size_t)h * P.in_ld + w);
-    }
-    return apply_op_c(x, P.pre_mode, P.prex, P.prey, h, w, P.ny, P.nx, P.pre_hlim, P.pre_wlim, P.coherent);
-}
-
 template <int N, int NT, int NSEQ>
 __device__ __forceinline__ void rows_fwd_body(const PropParams &P, int r0, float2 *sm, int tid)
 {
@@ -360,24 +252,6 @@ __device__ __forceinline__ void rows_fwd_body(const PropParams &P, int r0, float
             for (int k = 0; k < 16; ++k) __stcg(P.S + (size_t)h * N + j + k * B, v[outpos<16>(k)]);
         }
     }
-}
-
-__device__ __forceinline__ void store_out(const PropParams &P, int h, int w, float2 a, float &lsum)
-{
-    const size_t o = (size_t)h * P.out_ld + w;
-    if (P.post_mode == OP_SEED) {
-        const float r2 = a.x * a.x + a.y * a.y - __ldg(P.target + (size_t)h * P.nx + w);
-        lsum = fmaf(r2, r2, lsum);
-        a = cscale(a, P.seed_scale * r2);
-    } else {
-        a = apply_op_c(a, P.post_mode, P.postx, P.posty, h, w, P.ny, P.nx, P.post_hlim, P.post_wlim, P.coherent);
-    }
-    if (P.accumulate) {
-        const float2 v = P.out[o];
-        a.x += v.x;
-        a.y += v.y;
-    }
-    P.out[o] = a;
 }
 
 template <int N, int NT, int NSEQ>
@@ -414,17 +288,6 @@ __device__ __forceinline__ void rows_inv_body(const PropParams &P, int r0, float
             store_out(P, h, w, a, lsum);
         }
     }
-}
-
-__device__ __forceinline__ float2 tf_at(const PropParams &P, int ky, int kx, int NY)
-{
-    if (P.method == M_ASM) {
-        const int fx = kx < P.NX / 2 ? kx : kx - P.NX;
-        const int fy = ky < NY / 2 ? ky : ky - NY;
-        return asm_tf(P, fx, fy);
-    }
-    float2 T = cmul(ld_tab(P.Hx + kx, P.coherent), ld_tab(P.Hy + ky, P.coherent));
-    return P.conj ? cconj(T) : T;
 }
 
 template <int N, int NT, int C>
@@ -652,19 +515,6 @@ __device__ __forceinline__ void cols_body_p(const PropParams &P, int c0, float4 
 }
 
 
-__device__ __forceinline__ void loss_reduce(float lsum, double *loss, int tid, int nt)
-{
-    __shared__ float red[32];
-    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-    if ((tid & 31) == 0) red[tid >> 5] = lsum;
-    __syncthreads();
-    if (tid < 32) {
-        float v = tid < nt / 32 ? red[tid] : 0.f;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (tid == 0) atomicAdd(loss, (double)v);
-    }
-}
-
 // Launch-shape variants of the v2 passes (threads, elements per CTA, minimum
 // resident CTAs); olg_autotune_prop times them on the device and keeps the
 // fastest per FFT length.
@@ -788,19 +638,6 @@ __global__ void __launch_bounds__(V::NT, V::MINB) k_cols3(PropParams P)
 // c(m) = exp(2 pi i kap m^2) and c = 0 for |m| >= lim (lim < 0: no window).
 // blockIdx.x == 1: the pass-1 / pass-3 tables along this axis:
 //   a[m] = [|m'| < alim] exp(2 pi i (a2 m'^2 + a1 m' + a0))  (m' = m - n/2), and b[] likewise.
-struct ChirpAxis {
-    int L, n;                  // padded length, field length along this axis
-    float kap_hi, kap_lo;      // chirp cycles per index^2
-    int lim;                   // chirp window (< 0: none)
-    float scale;               // applied to the spectrum
-    int conj_spec;             // conjugate the spectrum
-    float2 *H;                 // out: L
-    // elementwise tables (nullable)
-    float2 *ta, *tb;           // out: n each
-    float a2_hi, a2_lo, a1_hi, a1_lo, a0; int alim; int aconj;
-    float b2_hi, b2_lo, b1_hi, b1_lo, b0; int blim; int bconj;
-};
-
 template <int N>
 struct ChirpCfg {
     static constexpr int NT = N / 16 < 256 ? N / 16 : 256;
@@ -824,28 +661,7 @@ __device__ __forceinline__ void chirp_body(const ChirpAxis &A, int part, float2 
             A.H[j] = A.conj_spec ? cconj(v) : v;
         }
     } else {
-        for (int m = tid; m < A.n; m += NT) {
-            const int mp = m - A.n / 2;
-            const float fm = (float)mp, fm2 = (float)(mp * mp);
-            if (A.ta) {
-                float2 v = make_float2(0.f, 0.f);
-                if (A.alim < 0 || abs(mp) < A.alim) {
-                    const float cyc = frac_mul(A.a2_hi, A.a2_lo, fm2) + frac_mul(A.a1_hi, A.a1_lo, fm) + A.a0;
-                    v = cis_cycles(wrap_cycles(cyc));
-                    if (A.aconj) v = cconj(v);
-                }
-                A.ta[m] = v;
-            }
-            if (A.tb) {
-                float2 v = make_float2(0.f, 0.f);
-                if (A.blim < 0 || abs(mp) < A.blim) {
-                    const float cyc = frac_mul(A.b2_hi, A.b2_lo, fm2) + frac_mul(A.b1_hi, A.b1_lo, fm) + A.b0;
-                    v = cis_cycles(wrap_cycles(cyc));
-                    if (A.bconj) v = cconj(v);
-                }
-                A.tb[m] = v;
-            }
-        }
+        chirp_tables(A, tid, NT);
     }
 }
 
@@ -1065,9 +881,22 @@ int launch_chirp(const ChirpAxis &A, cudaStream_t st)
     default: return fail(OLG_ERR_UNSUPPORTED_SIZE, "FFT length not supported");                                \
     }
 
-int rows_pass(const PropParams &P, bool inverse, cudaStream_t st) { OLG_SIZE_SWITCH(P.NX, launch_rows, P, inverse, st) }
-int cols_pass(const PropParams &P, cudaStream_t st) { OLG_SIZE_SWITCH(P.NY, launch_cols, P, st) }
-int chirp_axis(const ChirpAxis &A, cudaStream_t st) { OLG_SIZE_SWITCH(A.L, launch_chirp, A, st) }
+// lengths that are not powers of two take the mixed-radix passes (propmr.cu)
+int rows_pass(const PropParams &P, bool inverse, cudaStream_t st)
+{
+    if (!is_pow2(P.NX)) return mr_rows_pass(P, inverse, st);
+    OLG_SIZE_SWITCH(P.NX, launch_rows, P, inverse, st)
+}
+int cols_pass(const PropParams &P, cudaStream_t st)
+{
+    if (!is_pow2(P.NY)) return mr_cols_pass(P, st);
+    OLG_SIZE_SWITCH(P.NY, launch_cols, P, st)
+}
+int chirp_axis(const ChirpAxis &A, cudaStream_t st)
+{
+    if (!is_pow2(A.L)) return mr_chirp_axis(A, st);
+    OLG_SIZE_SWITCH(A.L, launch_chirp, A, st)
+}
 
 struct Layout {
     float2 *S, *Hx, *Hy, *tax, *tay, *tbx, *tby;
@@ -1093,12 +922,18 @@ size_t layout_bytes(int ny, int nx, Layout *L, char *base)
     return off;
 }
 
+// A field axis n is supported when the padded length 2n is a power of two in
+// [32, 8192] (the tuned passes) or 2^a 3^b 5^c with n >= 8 that one CTA holds
+// (mixed radix, up to 7680).
+bool axis_ok(int n) { return is_pow2(n) ? (n >= 16 && 2 * n <= FFT_MAX) : (n >= 8 && mr_length_ok(2 * n)); }
+
 int validate(const void *a, const void *b, int ny, int nx)
 {
     if (!a || !b) return fail(OLG_ERR_INVALID_ARG, "null field pointer");
     if (((uintptr_t)a & 15) || ((uintptr_t)b & 15)) return fail(OLG_ERR_INVALID_ARG, "field pointers must be 16-byte aligned");
-    if (!is_pow2(nx) || !is_pow2(ny) || nx < 16 || ny < 16 || 2 * nx > FFT_MAX || 2 * ny > FFT_MAX)
-        return fail(OLG_ERR_UNSUPPORTED_SIZE, "ny, nx must be powers of two in [16, 4096]");
+    if (!axis_ok(ny) || !axis_ok(nx))
+        return fail(OLG_ERR_UNSUPPORTED_SIZE,
+                    "ny, nx must be powers of two in [16, 4096] or have 2n = 2^a 3^b 5^c <= 7680 (n >= 8)");
     return OLG_OK;
 }
 
@@ -1190,6 +1025,7 @@ int setup_asm(const void *in, void *out, int ny, int nx, double dy, double dx, d
 {
     if (int rc = check_phys(dy, dx, lambda, z, false)) return rc;
     PropParams P = base_params(in, out, ny, nx, L);
+    if (int rc = mr_prepare(P)) return rc;
     const double NX = 2.0 * nx, NY = 2.0 * ny;
     const double du = 1.0 / (dx * NX), dv = 1.0 / (dy * NY);
     const double zl = z / lambda;
@@ -1280,6 +1116,7 @@ int setup_fresnel(const void *in, void *out, int ny, int nx, double dy, double d
     if (int rc = check_phys(dy, dx, lambda, z, true)) return rc;
     if (bandlimit < 0 || bandlimit > 2) return fail(OLG_ERR_INVALID_ARG, "bandlimit must be 0, 1 or 2");
     PropParams P = base_params(in, out, ny, nx, L);
+    if (int rc = mr_prepare(P)) return rc;
     const int NX = 2 * nx, NY = 2 * ny;
     const double np = (double)NX * (double)NY;
     const double sc1 = (flags & OLG_NO_NORMALIZE) ? 1.0 : 1.0 / np;
@@ -1311,6 +1148,7 @@ int setup_arss(const void *u_src, void *u_dst, int ny, int nx, double dy, double
     if (windows && (s == 0.0 || s == 1.0))
         return fail(OLG_ERR_INVALID_ARG, "ARSS is undefined for s = 0 or s = 1 (window limits divide by s|s-1|)");
     PropParams P = base_params(u_src, u_dst, ny, nx, L);
+    if (int rc = mr_prepare(P)) return rc;
     const int NX = 2 * nx, NY = 2 * ny;
     const double np = (double)NX * (double)NY;
     // windows, golprop.h:849-852, 891-892, 928-931 (-1: none)
@@ -2287,6 +2125,9 @@ extern "C" int olg_asm_prop_noalloc_c64(const void *u_in, void *u_out, int ny, i
     if ((long)ny * (long)nx > NOALLOC_MAX_PIXELS || layout_bytes(ny, nx, nullptr, nullptr) > NOALLOC_SCRATCH_BYTES)
         return fail(OLG_ERR_WORKSPACE, "olg_asm_prop_noalloc_c64: ny * nx must be <= 1048576 (its static scratch is "
                                        "17 MiB); use olg_asm_prop_c64 with a workspace for larger fields");
+    // mixed-radix lengths allocate their twiddle table on first use
+    if (!is_pow2(ny) || !is_pow2(nx))
+        return fail(OLG_ERR_UNSUPPORTED_SIZE, "olg_asm_prop_noalloc_c64 takes power-of-two ny, nx");
     if (int rc = validate(u_in, u_out, ny, nx)) return rc;
     void *scratch = nullptr;
     if (int rc = noalloc_scratch(&scratch)) return rc;

@@ -86,7 +86,7 @@ def test_argument_validation_without_gpu():
     assert L.olg_asm_prop_c64(None, None, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, None, 0, None) == -1
     buf = (C.c_char * 64)()
     base = (C.addressof(buf) + 15) // 16 * 16
-    assert L.olg_asm_prop_c64(base, base, 48, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, None, 0, None) == -2
+    assert L.olg_asm_prop_c64(base, base, 14, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, None, 0, None) == -2  # 28 = 4 * 7
     assert L.olg_asm_prop_c64(base, base, 64, 8192, 8e-6, 8e-6, 532e-9, 0.05, 0, None, 0, None) == -2
     assert L.olg_asm_prop_c64(base + 8, base, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, None, 0, None) == -1
     assert L.olg_arss_prop_c64(base, base, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 1.0, 0, 0, 0, None, 0, None) == -1

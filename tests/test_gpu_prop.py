@@ -166,7 +166,7 @@ def test_linearity_and_adjoint_identity_full_size():
 
 
 def test_errors_raise():
-    u = torch.zeros((48, 64), dtype=torch.complex64, device="cuda")
+    u = torch.zeros((14, 64), dtype=torch.complex64, device="cuda")  # 2 * 14 = 4 * 7: no plan
     with pytest.raises(og.OlgError):
         og.asm_prop(u, dy=8e-6, dx=8e-6, lam=532e-9, z=0.05)
     v = torch.zeros((64, 64), dtype=torch.complex64, device="cuda")
