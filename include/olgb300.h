@@ -67,6 +67,10 @@ extern "C" {
 #define OLG_WINDOW_CIRCLE 0 /* WRPStep1   golcgh.h:291-378 */
 #define OLG_WINDOW_SQUARE 1 /* WRPStep1_D golcgh.h:392-491 */
 
+/* objset modes, ol::OBJSET_MODE (olobject.h:192-194) */
+#define OLG_OBJSET_ZMIN 0
+#define OLG_OBJSET_ZMIDDLE 1
+
 typedef void *olg_stream_t;
 
 /* ---------------------------------------------------------------- library */
@@ -131,7 +135,7 @@ int olg_shifted_prop_c64(const void *u_src, void *u_dst, int ny, int nx, double 
 
 /* Split propagation.  Replaces ol::gsplitProp (golprop.h:772-813) and
  * ol::splitAsmProp (olprop.h:618-654) on device fields: the ny x nx field
- * is cut into blocks_y x blocks_x blocks (powers of two, >= 16), and every
+ * is cut into blocks_y x blocks_x blocks (each block side a supported size), and every
  * (source, destination) block pair adds olg_shifted_prop_c64 of the source
  * block, offset by the blocks' distance, into the destination block.  u_out
  * must not overlap u_in; it is zeroed first unless OLG_ACCUMULATE.  Flags
@@ -298,6 +302,46 @@ int olg_wrp_method_c64(const float *points, int n_points, void *U, int ny, int n
 int olg_complex2img_u8(const void *u, uint8_t *img, int ny, int nx, int mode, olg_stream_t stream);
 /* Binarised 8-bit hologram (project rule): 255 where Re(U) >= 0, else 0. */
 int olg_binarize_u8(const void *u, uint8_t *img, int ny, int nx, olg_stream_t stream);
+
+/* ------------------------------------------- point clouds and image files */
+/* Device point clouds are n records of float (x, y, z), as ol::gObject<float>. */
+
+/* ol::objinfo (olobject.h:163-174) on the device: minmax_out (host, 6 floats)
+ * = {xmin, ymin, zmin, xmax, ymax, zmax}.  Synchronises `stream`. */
+int olg_obj_minmax_f32(const float *points, int n, float *minmax_out, olg_stream_t stream);
+
+/* ol::objset on the device, in place.  y_range < 0: the one-range form
+ * (olobject.h:196-230): scale = x_range / max(x extent, y extent); otherwise
+ * the two-range form (olobject.h:232-264): the smaller of x_range / x extent
+ * and y_range / y extent.  Then offset (host, 3 floats) minus the scaled
+ * centre in x, y and the scaled zmin (OLG_OBJSET_ZMIN) or z centre
+ * (OLG_OBJSET_ZMIDDLE), and p = p * scale + offset, rounded as the
+ * reference's float code rounds it.  OLG_VERBOSE prints the extents as the
+ * one-range form does.  Reads the extents back (synchronises `stream`). */
+int olg_objset_f32(float *points, int n, float x_range, float y_range, const float *offset, int mode, int flags,
+                   olg_stream_t stream);
+
+/* ol::objsort (olobject.h:176-181) on the device, in place: records ordered
+ * by z, largest first; equal z keep their order (the reference's std::sort
+ * leaves it unspecified).  Scratch: olg_objsort_workspace_bytes(n). */
+size_t olg_objsort_workspace_bytes(int n);
+int olg_objsort_f32(float *points, int n, void *work, size_t work_bytes, olg_stream_t stream);
+
+/* ol::objread (olobject.h:9-91), host: a .3d (int32 records) or .3df (float
+ * records) file of a 4-byte count and n (x, y, z) records into `points`
+ * (host, 3 * capacity floats).  points == NULL: only *n_out is set. */
+int olg_objread(const char *path, float *points, int capacity, int *n_out);
+/* ol::objread(path, offset, scale) (olobject.h:93-161), host: int32 records,
+ * p = xint * scale + offset in float. */
+int olg_objread_scaled(const char *path, const float *offset, float scale, float *points, int capacity,
+                       int *n_out);
+
+/* ol::bmpwrite (olimg.h:136-165) and ol::bmpread (olimg.h:55-99), host: an
+ * 8-bit grey BMP (256-entry palette), rows in memory order, each followed by
+ * nx % 4 zero bytes as the reference writes them (a standard row padding only
+ * when nx % 4 is 0 or 2). */
+int olg_bmpwrite_u8(const char *fname, const uint8_t *img, int ny, int nx);
+int olg_bmpread_u8(const char *fname, uint8_t *img, int ny, int nx);
 
 #ifdef __cplusplus
 }

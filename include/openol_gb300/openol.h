@@ -7,4 +7,5 @@
 #include "golclass.h"
 #include "golprop.h"
 #include "golcgh.h"
+#include "olobject.h"
 #endif

@@ -72,6 +72,14 @@ SIGNATURES = {
     "olg_wrp_plane_z": (_f, [_i, _i, _i, _f, _f, _f, _f, _f]),
     "olg_wrp_step1_c64": (_i, [_p, _i, _p, _i, _i, _f, _f, _f, _f, _i, _p]),
     "olg_wrp_method_c64": (_i, [_p, _i, _p, _i, _i, _f, _f, _f, _f, _f, _i, _i, _i, C.POINTER(_f), _p]),
+    "olg_obj_minmax_f32": (_i, [_p, _i, _p, _p]),
+    "olg_objset_f32": (_i, [_p, _i, _f, _f, _p, _i, _i, _p]),
+    "olg_objsort_workspace_bytes": (_sz, [_i]),
+    "olg_objsort_f32": (_i, [_p, _i, _p, _sz, _p]),
+    "olg_objread": (_i, [C.c_char_p, _p, _i, C.POINTER(_i)]),
+    "olg_objread_scaled": (_i, [C.c_char_p, _p, _f, _p, _i, C.POINTER(_i)]),
+    "olg_bmpwrite_u8": (_i, [C.c_char_p, _p, _i, _i]),
+    "olg_bmpread_u8": (_i, [C.c_char_p, _p, _i, _i]),
     "olg_plain_asm_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _p]),
     "olg_plain_fresnel_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _p]),
     "olg_plain_arss_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _d, _p]),

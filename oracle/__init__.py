@@ -100,6 +100,13 @@ def ref():
         lib.ref_shifted_asm_prop.argtypes = [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d]
         lib.ref_shifted_fresnel_prop.argtypes = [_p, _i, _i, _d, _d, _d, _d, _d, _d, _d]
         lib.ref_split_asm_prop.argtypes = [_p, _i, _i, _d, _d, _d, _d, _i, _i]
+        lib.ref_objread.argtypes = [C.c_char_p, _p, _i]
+        lib.ref_objread.restype = _i
+        lib.ref_objread_scaled.argtypes = [C.c_char_p, _f, _f, _f, _f, _p, _i]
+        lib.ref_objread_scaled.restype = _i
+        lib.ref_objset.argtypes = [_p, _i, _f, _f, _f, _f, _f, _i]
+        lib.ref_objsort.argtypes = [_p, _i]
+        lib.ref_bmpwrite.argtypes = [C.c_char_p, _p, _i, _i]
         _REF = lib
     return _REF
 

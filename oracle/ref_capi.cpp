@@ -6,6 +6,7 @@
  * (olcpu.c) and to generate the golden fixtures under tests/golden/.  Output
  * goes to oracle/_ref/ (git-ignored).
  */
+#include <algorithm>
 #include <complex>
 #include <cstdint>
 #include <cstring>
@@ -13,6 +14,8 @@
 
 #include "olprop.h"
 #include "olcgh.h"
+#include "olimg.h"
+#include "olobject.h"
 
 using cd = std::complex<double>;
 
@@ -137,6 +140,66 @@ void ref_split_asm_prop(double *u, int ny, int nx, double dy, double dx, double 
     ol::splitAsmProp<float>(U, (int64_t)ny, (int64_t)nx, (float)dy, (float)dx, (float)lam, (float)z, by, bx);
     store(U, u, (long)ny * nx);
 }
+
+/* ol::objread<float>, olobject.h:79-91 (.3d / .3df); returns n, fills up to cap records */
+int ref_objread(const char *path, float *out, int cap)
+{
+    auto obj = ol::objread<float>(path);
+    for (int j = 0; j < obj.size && j < cap; ++j) {
+        out[3 * j] = obj[j].x;
+        out[3 * j + 1] = obj[j].y;
+        out[3 * j + 2] = obj[j].z;
+    }
+    return obj.size;
+}
+
+/* ol::objread<float>(path, Vect3<float> offset, float scale), olobject.h:128-161 */
+int ref_objread_scaled(const char *path, float ox, float oy, float oz, float scale, float *out, int cap)
+{
+    auto obj = ol::objread<float>(path, ol::Vect3<float>(ox, oy, oz), scale);
+    for (int j = 0; j < obj.size && j < cap; ++j) {
+        out[3 * j] = obj[j].x;
+        out[3 * j + 1] = obj[j].y;
+        out[3 * j + 2] = obj[j].z;
+    }
+    return obj.size;
+}
+
+static ol::Object<float> mkobjf(const float *p, int n)
+{
+    ol::Object<float> obj(n);
+    for (int j = 0; j < n; ++j) obj[j] = ol::Vect3<float>(p[3 * j], p[3 * j + 1], p[3 * j + 2]);
+    return obj;
+}
+static void storef(ol::Object<float> &obj, float *p)
+{
+    for (int j = 0; j < obj.size; ++j) {
+        p[3 * j] = obj[j].x;
+        p[3 * j + 1] = obj[j].y;
+        p[3 * j + 2] = obj[j].z;
+    }
+}
+
+/* ol::objset<float>: y_range < 0 -> one-range form olobject.h:196-230, else
+ * the two-range form olobject.h:232-264; mode = ol::OBJSET_MODE; in place */
+void ref_objset(float *p, int n, float x_range, float y_range, float ox, float oy, float oz, int mode)
+{
+    auto obj = mkobjf(p, n);
+    if (y_range < 0) ol::objset(obj, x_range, ol::Vect3<float>(ox, oy, oz), (ol::OBJSET_MODE)mode);
+    else ol::objset(obj, x_range, y_range, ol::Vect3<float>(ox, oy, oz), (ol::OBJSET_MODE)mode);
+    storef(obj, p);
+}
+
+/* ol::objsort<float>, olobject.h:176-181, in place */
+void ref_objsort(float *p, int n)
+{
+    auto obj = mkobjf(p, n);
+    ol::objsort(obj);
+    storef(obj, p);
+}
+
+/* ol::bmpwrite, olimg.h:136-160 */
+void ref_bmpwrite(const char *fname, uint8_t *img, int ny, int nx) { ol::bmpwrite(fname, img, ny, nx); }
 
 /* ol::quant8bit, olimg.h:178-198 */
 void ref_quant8bit(double *real, uint8_t *img, int ny, int nx) { ol::quant8bit(real, img, ny, nx); }

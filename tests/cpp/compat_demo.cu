@@ -89,6 +89,28 @@ int main(int argc, char **argv)
     auto d_ph = cuda::make_unique<float[]>(H * W);
     ol::gCgh(gobj, d_ph, H, W, p, p, lambda);
     dump(out + "/cgh_phase.bin", d_ph, H * W);
+    // point file -> objset -> objsort (host Object, through the GPU), and a BMP
+    {
+        const int M = 300;
+        FILE *f = fopen((out + "/cloud.3d").c_str(), "wb");
+        const int32_t m = M;
+        fwrite(&m, 4, 1, f);
+        std::uniform_int_distribution<int> I(-100, 100);
+        for (int j = 0; j < 3 * M; ++j) {
+            const int32_t v = I(rng);
+            fwrite(&v, 4, 1, f);
+        }
+        fclose(f);
+        auto cloud = ol::objread<PREC_T>((out + "/cloud.3d").c_str());
+        ol::objset(cloud, 2e-3f, ol::Vect3<PREC_T>(W / 2 * p, H / 2 * p, 0.03f), ol::ZMIN);
+        ol::objsort(cloud);
+        FILE *g = fopen((out + "/cloud_set_sorted.bin").c_str(), "wb");
+        fwrite(cloud.points.get(), sizeof(ol::Vect3<PREC_T>), cloud.size, g);
+        fclose(g);
+        auto img = std::make_unique<uint8_t[]>(H * W);
+        for (int i = 0; i < H * W; ++i) img[i] = (uint8_t)(i * 7);
+        ol::bmpwrite((out + "/img.bmp").c_str(), img, H, W);
+    }
     printf("compat_demo ok\n");
     return 0;
 }

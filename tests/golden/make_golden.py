@@ -5,7 +5,8 @@ the fixtures are made by running its CPU templates -- ``ol::AsmProp``,
 ``ol::FresnelProp``, ``ol::FresnelPropBandLimit``, ``ol::Prop``,
 ``ol::AsmPropCheck`` / ``ol::FresnelPropCheck``, ``ol::Cgh`` (complex and phase
 outputs), ``ol::complex2img``, ``ol::quant8bit``, ``ol::shiftedAsmProp``,
-``ol::shiftedFresnelProp`` and ``ol::splitAsmProp`` -- compiled unmodified by
+``ol::shiftedFresnelProp``, ``ol::splitAsmProp``, ``ol::objread``,
+``ol::objset``, ``ol::objsort`` and ``ol::bmpwrite`` -- compiled unmodified by
 ``oracle/Makefile`` (``make -C oracle ref``; needs the reference sources) on
 seeded inputs.  Run from the repository root:
 
@@ -138,6 +139,47 @@ def main():
         g[f"split{i}_in"] = u
         g[f"split{i}_out"] = refcall(R.ref_split_asm_prop, u, dy, dx, lam, z, by, bx)
     g["n_split"] = np.array(len(split))
+
+    # point files, objset / objsort and BMP files (their own generator)
+    import tempfile
+    ro = np.random.default_rng(20261205)
+    pts = np.stack([ro.integers(-200, 201, 500), ro.integers(-150, 151, 500), ro.integers(0, 40, 500)], 1)
+    with tempfile.TemporaryDirectory() as td:
+        f3d = os.path.join(td, "obj.3d")
+        with open(f3d, "wb") as f:
+            f.write(np.int32(len(pts)).tobytes() + pts.astype(np.int32).tobytes())
+        g["obj_3d_bytes"] = np.frombuffer(open(f3d, "rb").read(), np.uint8)
+        out = np.zeros((len(pts), 3), np.float32)
+        assert R.ref_objread(f3d.encode(), O._ptr(out), len(pts)) == len(pts)
+        g["obj_read"] = out.copy()
+        sc = np.zeros_like(out)
+        R.ref_objread_scaled(f3d.encode(), 1e-3, -2e-3, 0.1, 1.7e-5, O._ptr(sc), len(pts))
+        g["obj_read_scaled"] = sc
+        f3df = os.path.join(td, "obj.3df")
+        fl = (ro.random((64, 3)) * 0.01 - 0.005).astype(np.float32)
+        with open(f3df, "wb") as f:
+            f.write(np.int32(len(fl)).tobytes() + fl.tobytes())
+        g["obj_3df_bytes"] = np.frombuffer(open(f3df, "rb").read(), np.uint8)
+        o2 = np.zeros((64, 3), np.float32)
+        R.ref_objread(f3df.encode(), O._ptr(o2), 64)
+        g["obj_read_3df"] = o2
+        cases = [(5e-3, -1.0, 0), (5e-3, -1.0, 1), (6e-3, 4e-3, 0), (3e-3, 7e-3, 1)]
+        for i, (xr, yr, mode) in enumerate(cases):
+            q = out.copy()
+            R.ref_objset(O._ptr(q), len(q), xr, yr, 7.68e-3, 4.32e-3, 0.1, mode)
+            g[f"objset{i}_params"] = np.array([xr, yr, 7.68e-3, 4.32e-3, 0.1, mode], np.float64)
+            g[f"objset{i}_out"] = q
+        g["n_objset"] = np.array(len(cases))
+        q = out.copy()
+        R.ref_objsort(O._ptr(q), len(q))
+        g["objsort_out"] = q
+        for i, (ny, nx) in enumerate([(5, 8), (4, 9), (3, 10), (6, 11)]):
+            img = ro.integers(0, 256, (ny, nx)).astype(np.uint8)
+            fb = os.path.join(td, f"img{i}.bmp")
+            R.ref_bmpwrite(fb.encode(), O._ptr(img), ny, nx)
+            g[f"bmp{i}_img"] = img
+            g[f"bmp{i}_bytes"] = np.frombuffer(open(fb, "rb").read(), np.uint8)
+        g["n_bmp"] = np.array(4)
 
     np.savez_compressed(OUT, **g)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+import openol_gb300 as og
 from conftest import ROOT, rel_l2
 from openol_gb300 import build as B
 
@@ -55,3 +56,17 @@ def test_compat_cgh(demo_out):
     assert rel_l2(load(out, "cgh"), U) < 1e-3          # tensor-core path (>= 1024 points)
     g = load(out, "cgh_phase", np.float32)
     assert np.abs(np.angle(np.exp(1j * (g - ph)))).max() < 1e-3
+
+
+def test_compat_objects(demo_out):
+    """ol::objread / objset / objsort / bmpwrite through the drop-in headers."""
+    out, _ = demo_out
+    cloud = og.objread(out / "cloud.3d")
+    g = og.gObject(cloud)
+    p = float(np.float32(8e-6))
+    og.objset(g, np.float32(2e-3), (np.float32(256 / 2 * p), np.float32(128 / 2 * p), np.float32(0.03)), og.ZMIN)
+    og.objsort(g)
+    got = np.fromfile(out / "cloud_set_sorted.bin", dtype=np.float32).reshape(-1, 3)
+    assert np.array_equal(got, g.points.cpu().numpy())
+    img = (np.arange(128 * 256) * 7 % 256).astype(np.uint8).reshape(128, 256)
+    assert np.array_equal(og.bmpread(out / "img.bmp", 128, 256), img)
