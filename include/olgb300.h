@@ -67,6 +67,10 @@ extern "C" {
 #define OLG_WINDOW_CIRCLE 0 /* WRPStep1   golcgh.h:291-378 */
 #define OLG_WINDOW_SQUARE 1 /* WRPStep1_D golcgh.h:392-491 */
 
+/* tilted propagation interpolation, ol::INTERPOLATION (olprop.h:408-410) */
+#define OLG_BILINEAR 0
+#define OLG_BICUBIC 1
+
 /* objset modes, ol::OBJSET_MODE (olobject.h:192-194) */
 #define OLG_OBJSET_ZMIN 0
 #define OLG_OBJSET_ZMIDDLE 1
@@ -147,6 +151,21 @@ size_t olg_split_prop_workspace_bytes(int ny, int nx, int blocks_y, int blocks_x
 int olg_split_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda, double z,
                        int propmode, int blocks_y, int blocks_x, int flags, void *work, size_t work_bytes,
                        olg_stream_t stream);
+
+/* Tilted-plane propagation.  Replaces ol::TiltedSourceProp (olprop.h:414-521,
+ * reference == 0: the destination plane is rotated by `angle` radians about
+ * the y axis as seen from the source) and ol::TiltedReferenceProp
+ * (olprop.h:523-600, reference != 0: propagate, then resample for a plane
+ * rotated by `angle`).  interp OLG_BILINEAR / OLG_BICUBIC (radial kernel,
+ * a = -1), propmode OLG_ASM / OLG_FRESNEL.  Normalisation as the reference
+ * (1/Np after the forward and after the inverse FFT; the Fresnel spectrum
+ * carries one more).  Every frequency of the 2x padded grid must propagate
+ * (no evanescent sample), else OLG_ERR_INVALID_ARG.  u_out may equal u_in.
+ * Scratch: olg_tilted_workspace_bytes (two padded spectra). */
+size_t olg_tilted_workspace_bytes(int ny, int nx);
+int olg_tilted_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                        double z, double angle, int interp, int propmode, int reference, void *work,
+                        size_t work_bytes, olg_stream_t stream);
 
 /* Angular spectrum method that allocates nothing -- no counterpart in the
  * reference.  Same computation and flags as olg_asm_prop_c64, but its scratch

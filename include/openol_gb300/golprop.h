@@ -185,6 +185,64 @@ void gsplitProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int64_t height, i
     olgb::check(rc, "gsplitProp");
 }
 
+// TiltedSourceProp olprop.h:414-521 / TiltedReferenceProp olprop.h:523-600:
+// the reference's CPU templates, here on the GPU for a host field (copied in
+// and out) or a device field (in place)
+namespace olgb {
+inline int tilt_mode(PROPMODE propmode)
+{
+    return propmode == PROPMODE::ASM ? OLG_ASM : propmode == PROPMODE::FRESNEL ? OLG_FRESNEL : -1;
+}
+} // namespace olgb
+
+template <typename PREC_T = float, typename COMPLEX_T>
+void TiltedSourceProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx,
+                      PREC_T lambda, PREC_T z, PREC_T angle_src2dst, INTERPOLATION inp = BILINEAR,
+                      PROPMODE propmode = ASM)
+{
+    olgb::host_roundtrip(u, ny, nx, [&](void *d) {
+        olgb::check(olg_tilted_prop_c64(d, d, ny, nx, dy, dx, lambda, z, angle_src2dst, (int)inp,
+                                        olgb::tilt_mode(propmode), 0, nullptr, 0, nullptr),
+                    "TiltedSourceProp");
+    });
+}
+
+template <typename PREC_T = float, typename COMPLEX_T>
+void TiltedReferenceProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int64_t ny, int64_t nx, PREC_T dy, PREC_T dx,
+                         PREC_T lambda, PREC_T z, PREC_T rotate, INTERPOLATION inp = BILINEAR,
+                         PROPMODE propmode = ASM)
+{
+    olgb::host_roundtrip(u, (int)ny, (int)nx, [&](void *d) {
+        olgb::check(olg_tilted_prop_c64(d, d, (int)ny, (int)nx, dy, dx, lambda, z, rotate, (int)inp,
+                                        olgb::tilt_mode(propmode), 1, nullptr, 0, nullptr),
+                    "TiltedReferenceProp");
+    });
+}
+
+template <typename PREC_T = float, typename COMPLEX_T>
+void TiltedSourceProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx,
+                      PREC_T lambda, PREC_T z, PREC_T angle_src2dst, INTERPOLATION inp = BILINEAR,
+                      PROPMODE propmode = ASM)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    olgb::check(olg_tilted_prop_c64(u.get(), u.get(), ny, nx, dy, dx, lambda, z, angle_src2dst, (int)inp,
+                                    olgb::tilt_mode(propmode), 0, nullptr, 0, nullptr),
+                "TiltedSourceProp");
+    olgb::sync("TiltedSourceProp");
+}
+
+template <typename PREC_T = float, typename COMPLEX_T>
+void TiltedReferenceProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &u, int64_t ny, int64_t nx, PREC_T dy,
+                         PREC_T dx, PREC_T lambda, PREC_T z, PREC_T rotate, INTERPOLATION inp = BILINEAR,
+                         PROPMODE propmode = ASM)
+{
+    olgb::complex64_only<COMPLEX_T>();
+    olgb::check(olg_tilted_prop_c64(u.get(), u.get(), (int)ny, (int)nx, dy, dx, lambda, z, rotate, (int)inp,
+                                    olgb::tilt_mode(propmode), 1, nullptr, 0, nullptr),
+                "TiltedReferenceProp");
+    olgb::sync("TiltedReferenceProp");
+}
+
 // golprop.h:578-604 (prints the chosen method, as the reference does)
 template <typename COMPLEX_T, typename PREC_T>
 void Prop(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx, PREC_T lambda,

@@ -17,6 +17,8 @@ from .prop import (ASM, AUTO, FRESNEL, PROPMODE, ARSSFresnelProp, AsmPropCheck, 
                    Prop, arss_prop, asm_prop, fresnel_prop, gAsmProp, gFresnelProp, gFresnelPropBandLimit,
                    autotune, get_variant, set_variant, variant_count, workspace, workspace_bytes,
                    gshiftedAsmProp, gshiftedFresnelProp, gsplitProp, shiftedAsmProp, shiftedFresnelProp, shiftedProp,
-                   shifted_asm_prop, shifted_fresnel_prop, split_prop, split_workspace, splitAsmProp)
+                   shifted_asm_prop, shifted_fresnel_prop, split_prop, split_workspace, splitAsmProp,
+                   BICUBIC, BILINEAR, INTERPOLATION, TiltedReferenceProp, TiltedSourceProp, tilted_prop,
+                   tilted_workspace)
 
 __version__ = "0.1.0"

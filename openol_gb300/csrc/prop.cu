@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(V::NT, V::MINB) k_cols3(PropParams P)
 // ------------------------------------------------------------- chirp tables
 // Per axis (blockIdx.x == 0): the 1-D spectrum H[k] = sum_j c(j') e^{-2 pi i j k / L},
 // j' = j for j < L/2 else j - L (the fftshift'ed centred response), with
-// c(m) = exp(2 pi i kap m^2) and c = 0 for |m| >= lim (lim < 0: no window).
+// c(m) = exp(2 pi i (kap m^2 + lin m)) and c = 0 for |m| >= lim (lim < 0: no window).
 // blockIdx.x == 1: the pass-1 / pass-3 tables along this axis:
 //   a[m] = [|m'| < alim] exp(2 pi i (a2 m'^2 + a1 m' + a0))  (m' = m - n/2), and b[] likewise.
 template <int N>
@@ -650,9 +650,7 @@ __device__ __forceinline__ void chirp_body(const ChirpAxis &A, int part, float2 
     if (part == 0) {
         for (int j = tid; j < N; j += NT) {
             const int m = j < N / 2 ? j : j - N;
-            float2 c = make_float2(0.f, 0.f);
-            if (A.lim < 0 || abs(m) < A.lim) c = cis_cycles(frac_mul(A.kap_hi, A.kap_lo, (float)(m * m)));
-            sm[pidx(j)] = c;
+            sm[pidx(j)] = chirp_sample(A, m);
         }
         __syncthreads();
         smem_fft<N, -1, NT, false, 1>(sm, padded_len(N), g_tw, tid);
@@ -1388,6 +1386,129 @@ extern "C" int olg_split_prop_c64(const void *u_in, void *u_out, int ny, int nx,
                 }
         }
     return OLG_OK;
+}
+
+// ------------------------------------------------------------- tilted
+namespace olg {
+namespace {
+
+struct TiltLayout {
+    float2 *C, *D, *Hx, *Hy;
+};
+
+size_t tilt_layout(int ny, int nx, TiltLayout *L, char *base)
+{
+    size_t off = 0;
+    auto take = [&](size_t elems) {
+        char *p = base ? base + off : nullptr;
+        off += align_up(elems * sizeof(float2), 256);
+        return (float2 *)p;
+    };
+    const size_t full = (size_t)4 * ny * nx;
+    TiltLayout l;
+    l.C = take(full);
+    l.D = take(full);
+    l.Hx = take(2 * (size_t)nx);
+    l.Hy = take(2 * (size_t)ny);
+    if (L) *L = l;
+    return off;
+}
+
+} // namespace
+} // namespace olg
+
+extern "C" size_t olg_tilted_workspace_bytes(int ny, int nx)
+{
+    if (ny <= 0 || nx <= 0) return 0;
+    return tilt_layout(ny, nx, nullptr, nullptr);
+}
+
+// Tilted-plane propagation (olprop.h:414-600).  reference == 0:
+// TiltedSourceProp, the destination plane rotated by `angle` about the y axis
+// as seen from the source; the spectrum is resampled on the rotated grid and
+// then propagated.  reference != 0: TiltedReferenceProp, propagated first and
+// then resampled for a plane rotated by `angle`.  Every frequency of the 2x
+// padded grid must propagate (no evanescent sample), as the reference's
+// square roots require.  u_out may equal u_in.
+extern "C" int olg_tilted_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
+                                   double z, double angle, int interp, int propmode, int reference, void *work,
+                                   size_t work_bytes, olg_stream_t stream)
+{
+    if (int rc = validate(u_in, u_out, ny, nx)) return rc;
+    if (propmode != OLG_ASM && propmode != OLG_FRESNEL)
+        return fail(OLG_ERR_INVALID_ARG, "tilted propagation takes OLG_ASM or OLG_FRESNEL");
+    if (interp != OLG_BILINEAR && interp != OLG_BICUBIC)
+        return fail(OLG_ERR_INVALID_ARG, "interp must be OLG_BILINEAR or OLG_BICUBIC");
+    if (int rc = check_phys(dy, dx, lambda, z, propmode == OLG_FRESNEL)) return rc;
+    if (!std::isfinite(angle)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    const int NY = 2 * ny, NX = 2 * nx;
+    const double N = (double)NY * (double)NX;
+    const double du = 1 / (dx * NX), dv = 1 / (dy * NY);
+    const double fsqr = 1 / (lambda * lambda), f0 = 1 / lambda;
+    const double ang = reference ? angle : -angle;
+    const double a11 = std::cos(ang), a13 = -std::sin(ang);
+    const double a13f0 = reference ? 0.0 : a13 * f0;
+    // the largest |fpx|, |fpy| (and |fpx + a13 f0| for the shifted ASM) sit on the grid's corners
+    for (int cm = 0; cm < 2; ++cm)
+        for (int cn = 0; cn < 2; ++cn) {
+            const double fpx = (double)((cm ? NX - 1 : 0) - NX / 2) * du, fpy = (double)((cn ? NY - 1 : 0) - NY / 2) * dv;
+            const double uu = fpx + a13f0;
+            if (!(fsqr - fpx * fpx - fpy * fpy > 0) ||
+                (!reference && propmode == OLG_ASM && !(fsqr - uu * uu - fpy * fpy >= 0)))
+                return fail(OLG_ERR_INVALID_ARG, "tilted propagation: the padded grid reaches evanescent frequencies");
+        }
+    if (int rc = ensure_twiddles()) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, tilt_layout(ny, nx, nullptr, nullptr), st)) return rc;
+    TiltLayout TL;
+    tilt_layout(ny, nx, &TL, (char *)sc.ptr);
+    Layout L{};
+    L.S = TL.D;
+    PropParams P = base_params(u_in, u_out, ny, nx, L);
+    if (int rc = mr_prepare(P)) return rc;
+
+    TiltArgs T{};
+    T.ny = ny; T.nx = nx; T.NY = NY; T.NX = NX;
+    T.reference = reference ? 1 : 0;
+    T.interp = interp;
+    T.fresnel = propmode == OLG_FRESNEL ? 1 : 0;
+    T.du = du; T.dv = dv; T.fsqr = fsqr; T.a11 = a11; T.a13 = a13; T.a13f0 = a13f0; T.z = z;
+    T.J0 = (float)a11;
+    T.Jb = (float)(-a13);
+    T.invN = (float)(1.0 / N);
+    T.Hx = TL.Hx; T.Hy = TL.Hy;
+    T.C = TL.C; T.D = TL.D;
+    PropParams &tf = T.tf;
+    tf.ny = ny; tf.nx = nx; tf.NY = NY; tf.NX = NX;
+    tf.scale = 1.0f;
+    if (propmode == OLG_FRESNEL) {
+        tf.method = M_CHIRP;
+        tf.Hx = TL.Hx;
+        tf.Hy = TL.Hy;
+    } else {
+        const double zl = z / lambda;
+        tf.method = M_ASM;
+        tf.c0 = frac_host(zl);
+        set_quad(tf.ax_hi, tf.ax_lo, z * lambda * du * du / 2.0);
+        set_quad(tf.ay_hi, tf.ay_lo, z * lambda * dv * dv / 2.0);
+        tf.tx = (float)(lambda * lambda * du * du);
+        tf.ty = (float)(lambda * lambda * dv * dv);
+        tf.zl = (float)zl;
+    }
+
+    if (int rc = rows_pass(P, false, st)) return rc;
+    if (propmode == OLG_FRESNEL) {
+        // the Fresnel response's spectrum, fftshift'ed, 1/N (on x), with the
+        // source form's linear phase exp(-2 pi i x a13 f0) along x
+        ChirpAxis ax = chirp_axis_params(NX, nx, dx, lambda, z, 1.0, -1, 1.0 / N, TL.Hx);
+        if (!reference) set_quad(ax.lin_hi, ax.lin_lo, -a13 * f0 * dx);
+        ChirpAxis ay = chirp_axis_params(NY, ny, dy, lambda, z, 1.0, -1, 1.0, TL.Hy);
+        if (int rc = chirp_axis(ax, st)) return rc;
+        if (int rc = chirp_axis(ay, st)) return rc;
+    }
+    if (int rc = tilt_middle(T, st)) return rc;
+    return rows_pass(P, true, st);
 }
 
 // ------------------------------------------------------------- autotuner

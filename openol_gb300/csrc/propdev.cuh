@@ -184,7 +184,17 @@ struct ChirpAxis {
     float2 *ta, *tb;           // out: n each
     float a2_hi, a2_lo, a1_hi, a1_lo, a0; int alim; int aconj;
     float b2_hi, b2_lo, b1_hi, b1_lo, b0; int blim; int bconj;
+    float lin_hi, lin_lo;      // linear chirp term, cycles per index (0: none)
 };
+
+// One sample of the chirp: exp(2 pi i (kap m^2 + lin m)), 0 outside the window.
+__device__ __forceinline__ float2 chirp_sample(const ChirpAxis &A, int m)
+{
+    if (A.lim >= 0 && abs(m) >= A.lim) return make_float2(0.f, 0.f);
+    const float q = frac_mul(A.kap_hi, A.kap_lo, (float)m * (float)m);
+    if (A.lin_hi == 0.f && A.lin_lo == 0.f) return cis_cycles(q);
+    return cis_cycles(wrap_cycles(q + frac_mul(A.lin_hi, A.lin_lo, (float)m)));
+}
 
 
 // The ARSS pre/post tables of one axis (no FFT): ta, tb of length n.

@@ -101,9 +101,7 @@ __global__ void __launch_bounds__(MR_NT, 1) k_chirp_mr(ChirpAxis A, MrPlan pl, c
     if (blockIdx.x == 0) {
         for (int j = tid; j < N; j += MR_NT) {
             const int m = j < N / 2 ? j : j - N;
-            float2 c = make_float2(0.f, 0.f);
-            if (A.lim < 0 || abs(m) < A.lim) c = cis_cycles(frac_mul(A.kap_hi, A.kap_lo, (float)m * (float)m));
-            sm[pidx(j)] = c;
+            sm[pidx(j)] = chirp_sample(A, m);
         }
         __syncthreads();
         mr_fft<-1, MR_NT, false>(sm, padded_len(N), 1, pl, tw, tid);
@@ -113,6 +111,133 @@ __global__ void __launch_bounds__(MR_NT, 1) k_chirp_mr(ChirpAxis A, MrPlan pl, c
         }
     } else {
         chirp_tables(A, tid, MR_NT);
+    }
+}
+
+// ------------------------------------------------------------------ tilted
+// Column FFTs of the ny stored row spectra (D rows 0..ny-1, centred zero
+// padding to NY) and the centred spectrum C[(ky + NY/2) % NY][(kx + NX/2) % NX]
+// = F[ky][kx] / N (x the unrotated transfer function, reference form).
+__global__ void __launch_bounds__(MR_NT, 1) k_tilt_cols_fwd(TiltArgs T, MrPlan pl, const float2 *tw, int C)
+{
+    extern __shared__ float2 sm[];
+    const int N = T.NY, NX = T.NX, tid = threadIdx.x;
+    const int c0 = blockIdx.x * C, off = (N - T.ny) / 2;
+    for (int e = tid; e < N * C; e += MR_NT) {
+        const int i = e / C, c = e % C, kx = c0 + c, h = i - off;
+        float2 v = make_float2(0.f, 0.f);
+        if (kx < NX && h >= 0 && h < T.ny) v = T.D[(size_t)h * NX + kx];
+        sm[pidx(i) * C + c] = v;
+    }
+    __syncthreads();
+    mr_fft<-1, MR_NT, true>(sm, 0, C, pl, tw, tid);
+    for (int e = tid; e < N * C; e += MR_NT) {
+        const int ky = e / C, c = e % C, kx = c0 + c;
+        if (kx >= NX) continue;
+        float2 v = cscale(sm[pidx(ky) * C + c], T.invN);
+        if (T.reference) v = cmul(v, tf_at(T.tf, ky, kx, N));
+        const int n = ky < N / 2 ? ky + N / 2 : ky - N / 2, m = kx < NX / 2 ? kx + NX / 2 : kx - NX / 2;
+        T.C[(size_t)n * NX + m] = v;
+    }
+}
+
+// radial bicubic kernel, a = -1 (olutils.h:290-321)
+__device__ __forceinline__ float tilt_cubic(float d)
+{
+    constexpr float a = -1.f;
+    if (d < 1.f) return 1.f - (a + 3.f) * d * d + (a + 2.f) * d * d * d;
+    if (d < 2.f) return -4.f * a + 8.f * a * d - 5.f * a * d * d + a * d * d * d;
+    return 0.f;
+}
+
+// One resampled sample per thread: output frequency (n, m) of the centred
+// grid, stored at its natural-order position in D.  The sampling position
+// (x, y) is formed in FP64 operation by operation as the reference forms it
+// (each rounding explicit, so that the cell and boundary decisions agree);
+// weights, Jacobian and products are FP32.
+__global__ void __launch_bounds__(256) k_tilt_resample(TiltArgs T)
+{
+    const int NX = T.NX, NY = T.NY;
+    const int n = blockIdx.y, m = blockIdx.x * 256 + threadIdx.x;
+    if (m >= NX) return;
+    const double fpy = __dmul_rn((double)(n - NY / 2), T.dv);
+    const double fpx = __dmul_rn((double)(m - NX / 2), T.du);
+    const double fpz = __dsqrt_rn(__dsub_rn(__dsub_rn(T.fsqr, __dmul_rn(fpx, fpx)), __dmul_rn(fpy, fpy)));
+    double fsx = __dadd_rn(__dmul_rn(T.a11, fpx), __dmul_rn(T.a13, fpz));
+    if (!T.reference) fsx = __dsub_rn(fsx, T.a13f0);
+    const double x = __dadd_rn(__ddiv_rn(fsx, T.du), (double)(NX / 2));
+    const double y = __dadd_rn(__ddiv_rn(fpy, T.dv), (double)(NY / 2));
+    const double xf = floor(x), yf = floor(y);
+    const float2 *C = T.C;
+    float2 v = make_float2(0.f, 0.f);
+    if (T.interp == 0) {
+        if (xf >= 0.0 && xf < (double)(NX - 1) && yf >= 0.0 && yf < (double)(NY - 1)) {
+            const int ms = (int)xf, ns = (int)yf;
+            const float s = (float)(x - xf), t = (float)(y - yf);
+            const float2 *p = C + (size_t)ns * NX + ms;
+            const float2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + NX), d = __ldg(p + NX + 1);
+            const float2 u1 = make_float2((1.f - s) * a.x + s * b.x, (1.f - s) * a.y + s * b.y);
+            const float2 u2 = make_float2((1.f - s) * c.x + s * d.x, (1.f - s) * c.y + s * d.y);
+            v = make_float2((1.f - t) * u1.x + t * u2.x, (1.f - t) * u1.y + t * u2.y);
+        } else if (xf >= 0.0 && xf < (double)NX && yf >= 0.0 && yf < (double)NY) {
+            v = __ldg(C + (size_t)(int)yf * NX + (int)xf);
+        }
+    } else if (xf >= 0.0 && xf < (double)NX && yf >= 0.0 && yf < (double)NY) {
+        const int ms = (int)xf, ns = (int)yf;
+        const float s = (float)(x - xf), t = (float)(y - yf);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int nn = ns - 1 + j;
+            if (nn < 0 || nn >= NY) continue;
+            const float dyv = (float)(j - 1) - t;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int mm = ms - 1 + i;
+                if (mm < 0 || mm >= NX) continue;
+                const float dxv = (float)(i - 1) - s;
+                const float k = tilt_cubic(sqrtf(dxv * dxv + dyv * dyv));
+                const float2 q = __ldg(C + (size_t)nn * NX + mm);
+                v.x = fmaf(k, q.x, v.x);
+                v.y = fmaf(k, q.y, v.y);
+            }
+        }
+    }
+    const float J = T.J0 + T.Jb * (float)fpx / (float)fpz;
+    v = cscale(v, J);
+    const int ky = n < NY / 2 ? n + NY / 2 : n - NY / 2, kx = m < NX / 2 ? m + NX / 2 : m - NX / 2;
+    if (!T.reference) {
+        float2 H;
+        if (T.fresnel) {
+            H = cmul(__ldg(T.Hx + kx), __ldg(T.Hy + ky));
+        } else {
+            // exp(2 pi i z w), w = sqrt(fsqr - (fpx + a13 f0)^2 - fpy^2), in cycles
+            const double uu = __dadd_rn(fpx, T.a13f0);
+            const double w = __dsqrt_rn(__dsub_rn(__dsub_rn(T.fsqr, __dmul_rn(uu, uu)), __dmul_rn(fpy, fpy)));
+            const double cyc = w * T.z;
+            H = cis_cycles((float)(cyc - rint(cyc)));
+        }
+        v = cmul(v, H);
+    }
+    T.D[(size_t)ky * NX + kx] = v;
+}
+
+// Inverse column FFTs of the resampled spectrum; the central ny rows, x 1/N,
+// go to D's first ny rows (the scratch the inverse row pass reads).  A CTA
+// reads its whole column tile before writing back into the same columns.
+__global__ void __launch_bounds__(MR_NT, 1) k_tilt_cols_inv(TiltArgs T, MrPlan pl, const float2 *tw, int C)
+{
+    extern __shared__ float2 sm[];
+    const int N = T.NY, NX = T.NX, tid = threadIdx.x;
+    const int c0 = blockIdx.x * C, off = (N - T.ny) / 2;
+    for (int e = tid; e < N * C; e += MR_NT) {
+        const int i = e / C, c = e % C, kx = c0 + c;
+        sm[pidx(i) * C + c] = kx < NX ? T.D[(size_t)i * NX + kx] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    mr_fft<+1, MR_NT, true>(sm, 0, C, pl, tw, tid);
+    for (int e = tid; e < T.ny * C; e += MR_NT) {
+        const int h = e / C, c = e % C, kx = c0 + c;
+        if (kx < NX) T.D[(size_t)h * NX + kx] = cscale(sm[pidx(h + off) * C + c], T.invN);
     }
 }
 
@@ -262,6 +387,29 @@ int mr_chirp_axis(const ChirpAxis &A, cudaStream_t st)
     k_chirp_mr<<<(A.ta || A.tb) ? 2 : 1, MR_NT, smem, st>>>(A, pl, tw);
     count_launch();
     return check_launch("k_chirp_mr");
+}
+
+int tilt_middle(const TiltArgs &T, cudaStream_t st)
+{
+    MrPlan pl;
+    if (!mr_plan(T.NY, &pl) || mr_nseq(pl) < 1)
+        return fail(OLG_ERR_UNSUPPORTED_SIZE, "height: 2 ny must be a power of two or 2^a 3^b 5^c <= 7680");
+    const float2 *tw = nullptr;
+    if (int rc = mr_table(T.NY, &tw)) return rc;
+    const int C = mr_nseq(pl);
+    const int smem = C * padded_len(T.NY) * (int)sizeof(float2);
+    if (int rc = mr_smem(k_tilt_cols_fwd, smem)) return rc;
+    if (int rc = mr_smem(k_tilt_cols_inv, smem)) return rc;
+    const int gc = (T.NX + C - 1) / C;
+    k_tilt_cols_fwd<<<gc, MR_NT, smem, st>>>(T, pl, tw, C);
+    count_launch();
+    if (int rc = check_launch("k_tilt_cols_fwd")) return rc;
+    k_tilt_resample<<<dim3((T.NX + 255) / 256, T.NY), 256, 0, st>>>(T);
+    count_launch();
+    if (int rc = check_launch("k_tilt_resample")) return rc;
+    k_tilt_cols_inv<<<gc, MR_NT, smem, st>>>(T, pl, tw, C);
+    count_launch();
+    return check_launch("k_tilt_cols_inv");
 }
 
 } // namespace olg

@@ -16,4 +16,26 @@ int mr_rows_pass(const PropParams &P, bool inverse, cudaStream_t st);
 int mr_cols_pass(const PropParams &P, cudaStream_t st);
 int mr_chirp_axis(const ChirpAxis &A, cudaStream_t st);
 
+// Tilted-plane propagation, the part between the row passes (propmr.cu).
+// Frequencies (fpx, fpy) = ((m - NX/2) du, (n - NY/2) dv) on the centred grid;
+// the source frequency sampled for output frequency (n, m) is
+//   fsx = a11 fpx + a13 fpz - a13f0,  fsy = fpy,  fpz = sqrt(fsqr - fpx^2 - fpy^2)
+// (a13f0 = 0 for the reference form), weighted by J = J0 + Jb fpx / fpz.
+struct TiltArgs {
+    int ny, nx, NY, NX;
+    int reference;               // 1: transfer function before resampling; 0: after
+    int interp;                  // 0 bilinear, 1 bicubic (a = -1)
+    int fresnel;                 // transfer function Hx[kx] Hy[ky] (else ASM)
+    double du, dv, fsqr, a11, a13, a13f0, z;
+    float J0, Jb, invN;
+    PropParams tf;               // reference form: tf_at() of the unrotated grid
+    const float2 *Hx, *Hy;       // Fresnel spectra, natural order (Hx carries 1/N)
+    float2 *C;                   // centred spectrum, NY x NX
+    float2 *D;                   // resampled spectrum, natural order, NY x NX; its
+                                 // first ny rows are the row-pass scratch (ny x NX)
+};
+// column FFTs of the row spectra (D) -> C, resampling C -> D, inverse column
+// FFTs D -> D's first ny rows (x 1/N)
+int tilt_middle(const TiltArgs &T, cudaStream_t st);
+
 } // namespace olg

@@ -292,6 +292,61 @@ def gsplitProp(u, height, width, dy, dx, lam, z, propmode, blocknum_y=2, blocknu
     return _write_host(u, o)
 
 
+# ------------------------------------------------------------------ tilted
+class INTERPOLATION(IntEnum):
+    """ol::INTERPOLATION (olprop.h:408-410)."""
+
+    BILINEAR = 0
+    BICUBIC = 1
+
+
+BILINEAR, BICUBIC = INTERPOLATION.BILINEAR, INTERPOLATION.BICUBIC
+
+
+def tilted_workspace(ny, nx, device="cuda"):
+    n = int(lib().olg_tilted_workspace_bytes(ny, nx))
+    return torch.empty(n, dtype=torch.uint8, device=device)
+
+
+def tilted_prop(u_in, u_out=None, *, dy, dx, lam, z, angle, interp=INTERPOLATION.BILINEAR, propmode=PROPMODE.ASM,
+                reference=False, stream=None, work=None):
+    """Tilted-plane propagation (olg_tilted_prop_c64) on device fields.
+
+    ``reference=False`` is TiltedSourceProp (the destination plane rotated by
+    ``angle`` about y as seen from the source); ``reference=True`` is
+    TiltedReferenceProp (propagate, then resample for a plane rotated by
+    ``angle``).  ``interp`` BILINEAR / BICUBIC, ``propmode`` ASM / FRESNEL."""
+    ny, nx = u_in.shape
+    _dev_field(u_in, ny, nx, "u_in")
+    u_out = u_in if u_out is None else _dev_field(u_out, ny, nx, "u_out")
+    if int(propmode) not in (PROPMODE.ASM, PROPMODE.FRESNEL):
+        raise ValueError("tilted propagation takes PROPMODE.ASM or PROPMODE.FRESNEL")
+    wp, wb = _work(work)
+    call("olg_tilted_prop_c64", u_in.data_ptr(), u_out.data_ptr(), ny, nx, float(dy), float(dx), float(lam),
+         float(z), float(angle), int(interp), int(propmode), 1 if reference else 0, wp, wb, _stream(stream))
+    return u_out
+
+
+def _tilted_mirror(u, ny, nx, dy, dx, lam, z, angle, inp, propmode, reference):
+    if _is_host(u):
+        d = _host_c64(u, ny, nx)
+        tilted_prop(d, dy=dy, dx=dx, lam=lam, z=z, angle=angle, interp=inp, propmode=propmode, reference=reference)
+        return _write_host(u, d)
+    d = _dev_field(u, ny, nx).view(ny, nx)
+    tilted_prop(d, dy=dy, dx=dx, lam=lam, z=z, angle=angle, interp=inp, propmode=propmode, reference=reference)
+    return u
+
+
+def TiltedSourceProp(u, ny, nx, dy, dx, lam, z, angle_src2dst, inp=INTERPOLATION.BILINEAR, propmode=PROPMODE.ASM):
+    """ol::TiltedSourceProp, olprop.h:414-521, in place (host array or device tensor)."""
+    return _tilted_mirror(u, ny, nx, dy, dx, lam, z, angle_src2dst, inp, propmode, False)
+
+
+def TiltedReferenceProp(u, ny, nx, dy, dx, lam, z, rotate, inp=INTERPOLATION.BILINEAR, propmode=PROPMODE.ASM):
+    """ol::TiltedReferenceProp, olprop.h:523-600, in place (host array or device tensor)."""
+    return _tilted_mirror(u, ny, nx, dy, dx, lam, z, rotate, inp, propmode, True)
+
+
 # ------------------------------------------------------------------ autotuner
 def autotune(ny, nx, reps=5, stream=None):
     """Time every launch variant of the three passes for an ny x nx field and keep

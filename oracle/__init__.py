@@ -73,6 +73,7 @@ def cpu():
         lib.olc_quant8bit.argtypes = [_p, _p, _l, _l]
         lib.olc_binarize.argtypes = [_p, _p, _l, _l]
         lib.olc_fft2d.argtypes = [_p, _l, _l, _i, _i]
+        lib.olc_tilted_prop.argtypes = [_p, _l, _l, _d, _d, _d, _d, _d, _i, _i, _i]
         _CPU = lib
     return _CPU
 
@@ -107,6 +108,7 @@ def ref():
         lib.ref_objset.argtypes = [_p, _i, _f, _f, _f, _f, _f, _i]
         lib.ref_objsort.argtypes = [_p, _i]
         lib.ref_bmpwrite.argtypes = [C.c_char_p, _p, _i, _i]
+        lib.ref_tilted_prop.argtypes = [_p, _i, _i, _d, _d, _d, _d, _d, _i, _i, _i]
         _REF = lib
     return _REF
 
@@ -162,6 +164,17 @@ def split_prop(u, dy, dx, lam, z, mode, blocks_y=2, blocks_x=2, flags=0):
                             flags) != 0:
         raise ValueError("bad split arguments")
     return out
+
+
+def tilted_prop(u, dy, dx, lam, z, angle, interp=0, mode=0, reference=False, use_ref=False):
+    """Tilted-plane propagation: TiltedSourceProp (olprop.h:414-521) or, with
+    ``reference``, TiltedReferenceProp (olprop.h:523-600); interp 0 bilinear /
+    1 bicubic, mode 0 ASM / 1 Fresnel.  ``use_ref`` runs the reference's own
+    build instead of the restatement."""
+    u = _c128(u).copy()
+    fn = ref().ref_tilted_prop if use_ref else cpu().olc_tilted_prop
+    fn(_ptr(u), u.shape[0], u.shape[1], dy, dx, lam, z, angle, interp, mode, int(bool(reference)))
+    return u
 
 
 def arss_windows(ny, nx, dy, dx, lam, z, s):

@@ -9,6 +9,7 @@
 
 #include <complex.h>
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -381,6 +382,145 @@ int olc_split_prop(const double *srcd, double *dstd, long ny, long nx, double dy
     free(a);
     free(b);
     return 0;
+}
+
+/* -------------------------------------------------------------- tilted */
+/* bilinear olutils.h:213-233: the four neighbours when the cell is inside,
+ * the nearest sample on the last row / column, 0 outside. */
+static cplx tilt_bilinear(const cplx *src, double dsty, double dstx, long ny, long nx)
+{
+    const int64_t ms = (int64_t)floor(dstx), ns = (int64_t)floor(dsty);
+    if (0 <= ms && ms < nx - 1 && 0 <= ns && ns < ny - 1) {
+        const double s = dstx - ms, t = dsty - ns;
+        const cplx u1 = (1 - s) * src[ms + ns * nx] + s * src[(ms + 1) + ns * nx];
+        const cplx u2 = (1 - s) * src[ms + (ns + 1) * nx] + s * src[(ms + 1) + (ns + 1) * nx];
+        return (1 - t) * u1 + t * u2;
+    }
+    if (0 <= ms && ms < nx && 0 <= ns && ns < ny) return src[ms + ns * nx];
+    return 0;
+}
+
+/* bicubic olutils.h:290-321: 4 x 4 window, kernel of the radial distance,
+ * a = -1, taps outside the grid dropped, 0 when (floor x, floor y) is outside. */
+static cplx tilt_bicubic(const cplx *src, double dsty, double dstx, long ny, long nx)
+{
+    const double a = -1;
+    const int64_t ms = (int64_t)floor(dstx), ns = (int64_t)floor(dsty);
+    if (!(0 <= ms && ms < nx && 0 <= ns && ns < ny)) return 0;
+    cplx avg = 0;
+    for (int64_t j = 0; j < 4; j++)
+        for (int64_t i = 0; i < 4; i++) {
+            const int64_t m = ms - 1 + i, n = ns - 1 + j;
+            if (!(0 <= m && m < nx && 0 <= n && n < ny)) continue;
+            const double d = sqrt((m - dstx) * (m - dstx) + (n - dsty) * (n - dsty));
+            double k;
+            if (0 <= d && d < 1) k = 1 - (a + 3) * d * d + (a + 2) * d * d * d;
+            else if (1 <= d && d < 2) k = -4 * a + 8 * a * d - 5 * a * d * d + a * d * d * d;
+            else k = 0;
+            avg += k * src[m + n * nx];
+        }
+    return avg;
+}
+
+/* Fresnel response with an optional linear phase exp(-2 pi i x c), fftshift,
+ * FFT, 1/N, fftshift: the spectrum TiltedSourceProp (olprop.h:481-494,
+ * c = a13 f0) and TiltedReferenceProp (olprop.h:546-552, none) use. */
+static void tilt_fresnel_spectrum(cplx *H, long NY, long NX, double dy, double dx, double lambda, double z, double a13,
+                                  double f0)
+{
+    const double tmp = 1 / (lambda * z);
+    const long hh = NY / 2, hw = NX / 2, N = NY * NX;
+#pragma omp parallel for
+    for (long n = 0; n < NY; ++n) {
+        const double y = (double)(n - hh) * dy;
+        for (long m = 0; m < NX; ++m) {
+            const double x = (double)(m - hw) * dx;
+            const double phase = M_PI * (x * x + y * y) * tmp;
+            cplx h = cos(phase) + I * sin(phase);
+            if (f0 != 0) {
+                const double w = (double)(m - NX / 2) * dx;
+                const double p2 = -2 * M_PI * w * a13 * f0;
+                h *= cos(p2) + I * sin(p2);
+            }
+            H[n * NX + m] = h;
+        }
+    }
+    fftshift2(H, NY, NX);
+    fft2(H, NY, NX, -1);
+    for (long i = 0; i < N; ++i) H[i] *= 1.0 / (double)N;
+    fftshift2(H, NY, NX);
+}
+
+/* TiltedSourceProp olprop.h:414-521 (reference == 0) and TiltedReferenceProp
+ * olprop.h:523-600 (reference != 0), with PREC_T = double, in place on u
+ * (ny x nx).  Centred spectrum of the 2x padded field (1/N), then for every
+ * output frequency (fpx, fpy, fpz) the rotated source frequency
+ * fsx = a11 fpx + a13 fpz [- a13 f0], fsy = fpy, sampled by bilinear or bicubic
+ * interpolation and weighted by the Jacobian a11 - a13 fpx / fpz; the
+ * transfer function (ASM, or the FFT of the Fresnel response) multiplies the
+ * resampled spectrum (source form) or the spectrum before resampling
+ * (reference form); fftshift, inverse FFT, crop, 1/N. */
+void olc_tilted_prop(double *ud, long ny, long nx, double dy, double dx, double lambda, double z, double angle,
+                     int interp, int mode, int reference)
+{
+    cplx *u = (cplx *)ud;
+    const long NY = 2 * ny, NX = 2 * nx, N = NY * NX;
+    const double du = 1 / (dx * NX), dv = 1 / (dy * NY);
+    const double fsqr = 1 / (lambda * lambda);
+    cplx *U = pad2(u, ny, nx);
+    fft2(U, NY, NX, -1);
+    fftshift2(U, NY, NX);
+    for (long i = 0; i < N; ++i) U[i] *= 1.0 / (double)N;
+    const double ang = reference ? angle : -angle;
+    const double a11 = cos(ang), a12 = 0, a13 = -sin(ang);
+    const double a21 = 0, a22 = 1, a23 = 0;
+    const double f0 = 1 / lambda;
+    cplx *H = cz(N);
+    if (mode == 0) {
+        const double tmp = 1 / (lambda * lambda);
+        /* reference form: AsmTransferF olprop.h:173-189; source form: its
+         * frequency shifted by a13 f0 (olprop.h:468-479) */
+#pragma omp parallel for
+        for (long n = 0; n < NY; ++n) {
+            const double v = (double)(n - NY / 2) * dv;
+            for (long m = 0; m < NX; ++m) {
+                const double uu = reference ? (double)(m - NX / 2) * du : (double)(m - NX / 2) * du + a13 * f0;
+                const double w = sqrt(tmp - uu * uu - v * v);
+                const double phase = 2 * M_PI * w * z;
+                H[n * NX + m] = cos(phase) + I * sin(phase);
+            }
+        }
+    } else {
+        tilt_fresnel_spectrum(H, NY, NX, dy, dx, lambda, z, a13, reference ? 0.0 : f0);
+    }
+    if (reference)
+        for (long i = 0; i < N; ++i) U[i] = U[i] * H[i];
+    cplx *Up = cz(N);
+#pragma omp parallel for
+    for (long n = 0; n < NY; ++n)
+        for (long m = 0; m < NX; ++m) {
+            const double fpx = (m - NX / 2) * du;
+            const double fpy = (n - NY / 2) * dv;
+            const double fpz = sqrt(fsqr - fpx * fpx - fpy * fpy);
+            const double fsx = reference ? a11 * fpx + a12 * fpy + a13 * fpz
+                                         : a11 * fpx + a12 * fpy + a13 * fpz - a13 * f0;
+            const double fsy = a21 * fpx + a22 * fpy + a23 * fpz;
+            const double y = fsy / dv + NY / 2, x = fsx / du + NX / 2;
+            cplx v = interp == 1 ? tilt_bicubic(U, y, x, NY, NX) : tilt_bilinear(U, y, x, NY, NX);
+            const double J = (a11 * a22 - a12 * a21) + (a12 * a23 - a13 * a22) * fpx / fpz +
+                             (a13 * a21 - a11 * a23) * fpy / fpz;
+            v *= J;
+            Up[m + n * NX] = v;
+        }
+    if (!reference)
+        for (long i = 0; i < N; ++i) Up[i] = Up[i] * H[i];
+    fftshift2(Up, NY, NX);
+    fft2(Up, NY, NX, +1);
+    crop2(Up, ny, nx, u);
+    for (long i = 0; i < ny * nx; ++i) u[i] *= 1.0 / (double)N;
+    free(Up);
+    free(H);
+    free(U);
 }
 
 /* ------------------------------------------------------------- AUTO checks */

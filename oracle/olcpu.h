@@ -71,6 +71,14 @@ void olc_shifted_asm_prop(const double *src, double *dst, long ny, long nx, doub
 int olc_split_prop(const double *src, double *dst, long ny, long nx, double dy, double dx, double lambda, double z,
                    int mode, int blocks_y, int blocks_x, int flags);
 
+/* Tilted-plane propagation, TiltedSourceProp olprop.h:414-521 (reference == 0:
+ * the destination plane is rotated by `angle` about y as seen from the source)
+ * and TiltedReferenceProp olprop.h:523-600 (reference != 0: rotation `angle`),
+ * in PREC_T = double.  interp 0 bilinear, 1 bicubic (a = -1); mode 0 ASM,
+ * 1 Fresnel.  In place on u (ny x nx). */
+void olc_tilted_prop(double *u, long ny, long nx, double dy, double dx, double lambda, double z, double angle,
+                     int interp, int mode, int reference);
+
 /* ARSS window limits as the reference computes them: lims[0..5] =
  * {hlim_u, wlim_u, lim_h, hlim_cz, wlim_cz, unused}. */
 int olc_arss_windows(long ny, long nx, double dy, double dx, double lambda, double z, double s, int64_t *lims);

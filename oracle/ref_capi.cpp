@@ -141,6 +141,20 @@ void ref_split_asm_prop(double *u, int ny, int nx, double dy, double dx, double 
     store(U, u, (long)ny * nx);
 }
 
+/* ol::TiltedSourceProp<double> olprop.h:414-521 (reference == 0) and
+ * ol::TiltedReferenceProp<double> olprop.h:523-600 (reference != 0), in place;
+ * interp 0 BILINEAR / 1 BICUBIC, mode 0 ASM / 1 FRESNEL */
+void ref_tilted_prop(double *u, int ny, int nx, double dy, double dx, double lam, double z, double angle, int interp,
+                     int mode, int reference)
+{
+    auto U = load(u, (long)ny * nx);
+    const ol::INTERPOLATION ip = interp == 1 ? ol::BICUBIC : ol::BILINEAR;
+    const ol::PROPMODE pm = mode == 1 ? ol::FRESNEL : ol::ASM;
+    if (reference) ol::TiltedReferenceProp<double>(U, (int64_t)ny, (int64_t)nx, dy, dx, lam, z, angle, ip, pm);
+    else ol::TiltedSourceProp<double>(U, ny, nx, dy, dx, lam, z, angle, ip, pm);
+    store(U, u, (long)ny * nx);
+}
+
 /* ol::objread<float>, olobject.h:79-91 (.3d / .3df); returns n, fills up to cap records */
 int ref_objread(const char *path, float *out, int cap)
 {

@@ -60,6 +60,18 @@ int main(int argc, char **argv)
         fwrite(hs.get(), sizeof(std::complex<PREC_T>), H * W, f);
         fclose(f);
     }
+    {
+        // tilted planes: the CPU templates of olprop.h, here on the GPU
+        auto ht = std::make_unique<std::complex<PREC_T>[]>(H * W);
+        for (int i = 0; i < H * W; ++i) ht[i] = u[i];
+        ol::TiltedSourceProp<PREC_T>(ht, H, W, p, p, lambda, d, 0.1f, ol::BICUBIC, ol::PROPMODE::ASM);
+        FILE *f = fopen((out + "/tilted_source.bin").c_str(), "wb");
+        fwrite(ht.get(), sizeof(std::complex<PREC_T>), H * W, f);
+        fclose(f);
+    }
+    ol::cpu2cuda(u, d_u, H * W);
+    ol::TiltedReferenceProp<PREC_T>(d_u, H, W, p, p, lambda, d, 2e-3f, ol::BILINEAR, ol::PROPMODE::FRESNEL);
+    dump(out + "/tilted_reference.bin", d_u, H * W);
     ol::cpu2cuda(u, d_u, H * W);
     ol::Prop(d_u, H, W, p, p, lambda, d, ol::PROPMODE::AUTO);
     dump(out + "/prop_auto.bin", d_u, H * W);

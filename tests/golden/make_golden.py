@@ -6,7 +6,8 @@ the fixtures are made by running its CPU templates -- ``ol::AsmProp``,
 ``ol::AsmPropCheck`` / ``ol::FresnelPropCheck``, ``ol::Cgh`` (complex and phase
 outputs), ``ol::complex2img``, ``ol::quant8bit``, ``ol::shiftedAsmProp``,
 ``ol::shiftedFresnelProp``, ``ol::splitAsmProp``, ``ol::objread``,
-``ol::objset``, ``ol::objsort`` and ``ol::bmpwrite`` -- compiled unmodified by
+``ol::objset``, ``ol::objsort``, ``ol::bmpwrite``, ``ol::TiltedSourceProp`` and
+``ol::TiltedReferenceProp`` -- compiled unmodified by
 ``oracle/Makefile`` (``make -C oracle ref``; needs the reference sources) on
 seeded inputs.  Run from the repository root:
 
@@ -139,6 +140,27 @@ def main():
         g[f"split{i}_in"] = u
         g[f"split{i}_out"] = refcall(R.ref_split_asm_prop, u, dy, dx, lam, z, by, bx)
     g["n_split"] = np.array(len(split))
+
+    # tilted-plane propagation (its own generator): ol::TiltedSourceProp /
+    # ol::TiltedReferenceProp in PREC_T = double
+    rt = np.random.default_rng(20261206)
+    tilt = [
+        # ny, nx, dy, dx, lam, z, angle, interp, mode, reference
+        (32, 32, 8e-6, 8e-6, 532e-9, 0.02, 0.1, 0, 0, 0),
+        (32, 48, 8e-6, 6e-6, 633e-9, 0.01, -0.2, 1, 0, 0),
+        (32, 32, 8e-6, 8e-6, 532e-9, 0.02, 0.15, 0, 1, 0),
+        (24, 40, 8e-6, 8e-6, 532e-9, 0.03, 0.05, 1, 1, 0),
+        (32, 32, 8e-6, 8e-6, 532e-9, 0.02, 2e-3, 0, 0, 1),
+        (32, 32, 8e-6, 8e-6, 532e-9, -0.02, -4e-3, 1, 0, 1),
+        (32, 64, 8e-6, 8e-6, 532e-9, 0.02, 3e-3, 0, 1, 1),
+        (40, 24, 6e-6, 8e-6, 633e-9, 0.03, -2e-3, 1, 1, 1),
+    ]
+    for i, (ny, nx, dy, dx, lam, z, ang, ip, mode, refm) in enumerate(tilt):
+        u = field(rt, (ny, nx))
+        g[f"tilt{i}_params"] = np.array([ny, nx, dy, dx, lam, z, ang, ip, mode, refm], np.float64)
+        g[f"tilt{i}_in"] = u
+        g[f"tilt{i}_out"] = refcall(R.ref_tilted_prop, u, dy, dx, lam, z, ang, ip, mode, refm)
+    g["n_tilt"] = np.array(len(tilt))
 
     # point files, objset / objsort and BMP files (their own generator)
     import tempfile

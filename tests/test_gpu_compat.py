@@ -46,6 +46,8 @@ def test_compat_propagation(demo_out):
     f = lambda v: float(np.float32(v))
     assert rel_l2(load(out, "shifted_asm"), O.shifted_asm_prop(u, p, p, lam, d, f(2e-4), f(-1e-4))) < 1e-5
     assert rel_l2(load(out, "split_asm"), O.split_prop(u, p, p, lam, d, 0, 2, 2)) < 1e-5
+    assert rel_l2(load(out, "tilted_source"), O.tilted_prop(u, p, p, lam, d, f(0.1), 1, 0, False)) < 1e-5
+    assert rel_l2(load(out, "tilted_reference"), O.tilted_prop(u, p, p, lam, d, f(2e-3), 0, 1, True)) < 1e-5
 
 
 def test_compat_cgh(demo_out):

@@ -227,3 +227,23 @@ def test_split_sums_shifted_blocks():
                     s = O.shifted_asm_prop(u[gn * 16:(gn + 1) * 16, gm * 32:(gm + 1) * 32], *args, oy, ox)
                     ref[dn * 16:(dn + 1) * 16, dm * 32:(dm + 1) * 32] += s
     assert rel_l2(out, ref) < 1e-14
+
+
+def test_golden_tilted(golden):
+    """ol::TiltedSourceProp / ol::TiltedReferenceProp (PREC_T = double) outputs."""
+    for i in range(int(golden["n_tilt"])):
+        ny, nx, dy, dx, lam, z, ang, ip, mode, refm = golden[f"tilt{i}_params"]
+        out = O.tilted_prop(golden[f"tilt{i}_in"], dy, dx, lam, z, ang, int(ip), int(mode), bool(refm))
+        assert rel_l2(out, golden[f"tilt{i}_out"]) < 1e-13, i
+
+
+def test_tilted_zero_angle_is_plain_propagation():
+    """At angle 0 both tilted forms resample on the unrotated grid (J = 1); the
+    source form with ASM is then the ASM propagation with one more 1/N."""
+    rng = np.random.default_rng(3)
+    u = (rng.random((32, 48)) < 0.5) * np.exp(2j * np.pi * rng.random((32, 48)))
+    n = 4 * u.size
+    ref = O.asm_prop(u, 8e-6, 8e-6, 532e-9, 0.02) / n
+    for refm in (False, True):
+        out = O.tilted_prop(u, 8e-6, 8e-6, 532e-9, 0.02, 0.0, 0, 0, refm)
+        assert rel_l2(out, ref) < 1e-12
