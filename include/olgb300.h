@@ -288,6 +288,12 @@ size_t olg_cgh_gemm_workspace_bytes(int n_points, int ny, int nx);
 int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, const float *phase0, int n_points, void *U,
                              int ny, int nx, double py, double px, double lambda, int flags, void *work,
                              size_t work_bytes, olg_stream_t stream);
+/* Tuning hook of the GEMM's work split (no counterpart in the reference):
+ * when a hologram has fewer 128 x 256 output tiles than the GPU has SMs, the
+ * spare SMs take the last part of every tile's K range, and w is the cost of
+ * one of their K blocks relative to a tile CTA's (default 1.2; 0 turns the
+ * split off).  Sets w when 0 <= w <= 16 and returns the previous value. */
+double olg_cgh_gemm_tail_weight(double w);
 /* Synchronises the device and reports (OLG_ERR_CUDA) whether any tensor-core
  * kernel of this library gave up on a bounded wait; clear != 0 resets the flag. */
 int olg_device_fault_check(int clear);

@@ -17,16 +17,18 @@
 // k_cgh_gemm_prep  per point, FP64: expansion coefficients of the x / y phases
 // k_cgh_gemm_ops   builds A_hi/A_lo/B_hi/B_lo (f16, K-contiguous, zero padded),
 //                  phases range-reduced exactly (frac_mul), MUFU sin/cos
-// k_cgh_gemm       warp-specialised tcgen05 GEMM: warp 0 issues TMA loads into a
+// k_cgh_gemm       warp-specialised tcgen05 GEMM, one CTA per tile plus CTAs on
+//                  the spare SMs that take the tiles' K tails: warp 0 issues TMA loads into a
 //                  4-stage ring (128 x 64 A and 256 x 64 B f16 tiles, 128-byte
 //                  swizzle), warp 1 owns TMEM (two 256-column f32 accumulators)
 //                  and issues the 128 x 256 x 16 MMAs chunk by chunk, warps 2-9
-//                  add each finished chunk into f32 registers and finally write
-//                  complex64.
+//                  add each finished chunk into f32 registers and add every
+//                  finished piece of a tile into the complex64 output.
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -144,16 +146,46 @@ __global__ void k_cgh_gemm_ops(GemmOps G)
 
 struct GemmParams {
     int m2, n, kblocks; // rows of D (2 ny), columns (nx), K blocks of 64 per segment
-    float2 *U;
-    int accumulate;
+    int tiles_n;        // 256-column tiles across D
+    int tiles;          // 128 x 256 tiles of D
+    int split;          // K blocks (of 3 kblocks) a tile's own CTA does
+    int extra;          // CTAs beyond `tiles` that do the rest [split, 3 kblocks)
+    float2 *U;          // added to with float2 atomics (zeroed first unless accumulating)
     int *err;
 };
 
-// Accumulation: the MMA warp writes chunks of GB_CHUNK K-blocks alternately
-// into two 256-column TMEM accumulators; the 8 epilogue warps add every
-// finished chunk into f32 registers (rounded adds) while the next chunk
-// runs, so the tensor pipe's own accumulation never spans more than
-// GB_CHUNK x 64 x 3 products.
+// Work split.  CTA c < tiles does tile c over K blocks [0, split); when there
+// are fewer tiles than SMs (1920 x 1080: 136 tiles, 152 SMs) the `extra` CTAs
+// do the remaining [split, total) of tiles e, e + extra, e + 2 extra, ... so
+// that every SM gets about the same tensor work.  The tile CTAs walk K in
+// lockstep (their A / B blocks are shared through L2), and the extra CTAs'
+// K range is a small slice of the operands that L2 holds.  Each piece (tile,
+// K range) is one accumulation, added into U with float2 atomics when it ends;
+// a tile's two pieces add in either order.
+__device__ __forceinline__ int gemm_pieces(const GemmParams &P)
+{
+    if ((int)blockIdx.x < P.tiles) return 1;
+    const int e = blockIdx.x - P.tiles;
+    return e < P.tiles ? (P.tiles - e + P.extra - 1) / P.extra : 0;
+}
+__device__ __forceinline__ void gemm_piece(const GemmParams &P, int p, int total, int &t, int &k0, int &k1)
+{
+    if ((int)blockIdx.x < P.tiles) {
+        t = blockIdx.x;
+        k0 = 0;
+        k1 = P.split;
+    } else {
+        t = (int)blockIdx.x - P.tiles + p * P.extra;
+        k0 = P.split;
+        k1 = total;
+    }
+}
+
+// Accumulation within a piece: the MMA warp writes chunks of GB_CHUNK
+// K-blocks alternately into two 256-column TMEM accumulators; the 8 epilogue
+// warps add every finished chunk into f32 registers (rounded adds) while the
+// next chunk runs, so the tensor pipe's own accumulation never spans more
+// than GB_CHUNK x 64 x 3 products.
 constexpr int GB_CHUNK = 8;
 constexpr int GB_EPI_WARPS = 8;
 constexpr int GB_THREADS = 64 + 32 * GB_EPI_WARPS;
@@ -174,9 +206,8 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
     volatile int *fault = (volatile int *)(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
-    const int total = 3 * P.kblocks;
-    const int nchunks = (total + GB_CHUNK - 1) / GB_CHUNK;
+    const int total = 3 * P.kblocks; // K blocks per tile
+    const int np = gemm_pieces(P);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < GB_STAGES; ++s) {
@@ -201,106 +232,132 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            int issued = 0;
-            for (int kb = 0; kb < total && !*fault; ++kb) {
-                const int s = kb % GB_STAGES;
-                const uint32_t ph = (uint32_t)(kb / GB_STAGES) & 1u;
-                if (!mbar_wait(smem_u32(empty + s), ph ^ 1u, GB_WAIT)) {
-                    *fault = 1;
-                    break;
+            int i = 0, issued = 0;
+            for (int p = 0; p < np && !*fault; ++p) {
+                int t, k0, k1;
+                gemm_piece(P, p, total, t, k0, k1);
+                const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * GB_N;
+                for (int kb = k0; kb < k1 && !*fault; ++kb, ++i) {
+                    const int s = i % GB_STAGES;
+                    const uint32_t ph = (uint32_t)(i / GB_STAGES) & 1u;
+                    if (!mbar_wait(smem_u32(empty + s), ph ^ 1u, GB_WAIT)) {
+                        *fault = 1;
+                        break;
+                    }
+                    const int seg = kb / P.kblocks, kk = (kb % P.kblocks) * GB_K;
+                    const CUtensorMap *ma = seg < 2 ? &tAh : &tAl;
+                    const CUtensorMap *mb = seg == 1 ? &tBl : &tBh;
+                    mbar_expect_tx(smem_u32(full + s), GB_A_BYTES + GB_B_BYTES);
+                    tma_load_2d(smem_u32(sA + s * GB_A_BYTES), ma, smem_u32(full + s), kk, m0);
+                    tma_load_2d(smem_u32(sB + s * GB_B_BYTES), mb, smem_u32(full + s), kk, n0);
+                    issued = i + 1;
                 }
-                const int seg = kb / P.kblocks, kk = (kb % P.kblocks) * GB_K;
-                const CUtensorMap *ma = seg < 2 ? &tAh : &tAl;
-                const CUtensorMap *mb = seg == 1 ? &tBl : &tBh;
-                mbar_expect_tx(smem_u32(full + s), GB_A_BYTES + GB_B_BYTES);
-                tma_load_2d(smem_u32(sA + s * GB_A_BYTES), ma, smem_u32(full + s), kk, m0);
-                tma_load_2d(smem_u32(sB + s * GB_B_BYTES), mb, smem_u32(full + s), kk, n0);
-                issued = kb + 1;
             }
             // never leave with copies in flight
-            for (int kb = issued > GB_STAGES ? issued - GB_STAGES : 0; kb < issued; ++kb)
-                mbar_wait(smem_u32(full + kb % GB_STAGES), (uint32_t)(kb / GB_STAGES) & 1u, GB_WAIT);
+            for (int j = issued > GB_STAGES ? issued - GB_STAGES : 0; j < issued; ++j)
+                mbar_wait(smem_u32(full + j % GB_STAGES), (uint32_t)(j / GB_STAGES) & 1u, GB_WAIT);
         }
     } else if (warp == 1) {
         if (lane == 0) {
             constexpr uint32_t idesc = idesc_f16_f32(GB_M, GB_N);
-            for (int c = 0; c < nchunks && !*fault; ++c) {
-                const int b = c & 1;
-                if (c >= 2 && !mbar_wait(smem_u32(tfree + b), (uint32_t)((c >> 1) - 1) & 1u, GB_WAIT)) {
-                    *fault = 1;
-                    break;
-                }
-                tc_fence_after();
-                const uint32_t d = tmem + (uint32_t)(b * GB_N);
-                const int kb0 = c * GB_CHUNK, kb1 = min(total, kb0 + GB_CHUNK);
-                for (int kb = kb0; kb < kb1; ++kb) {
-                    const int s = kb % GB_STAGES;
-                    if (!mbar_wait(smem_u32(full + s), (uint32_t)(kb / GB_STAGES) & 1u, GB_WAIT)) {
+            int c = 0, i = 0; // chunk and stage counters over all pieces
+            for (int p = 0; p < np && !*fault; ++p) {
+                int t, k0, k1;
+                gemm_piece(P, p, total, t, k0, k1);
+                for (int kb = k0; kb < k1 && !*fault; ++c) {
+                    const int b = c & 1;
+                    if (c >= 2 && !mbar_wait(smem_u32(tfree + b), (uint32_t)((c >> 1) - 1) & 1u, GB_WAIT)) {
                         *fault = 1;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * GB_B_BYTES);
+                    const uint32_t d = tmem + (uint32_t)(b * GB_N);
+                    const int kend = min(k1, kb + GB_CHUNK);
+                    for (int kc = kb; kc < kend; ++kc, ++i) {
+                        const int s = i % GB_STAGES;
+                        if (!mbar_wait(smem_u32(full + s), (uint32_t)(i / GB_STAGES) & 1u, GB_WAIT)) {
+                            *fault = 1;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * GB_B_BYTES);
 #pragma unroll
-                    for (int k = 0; k < GB_K / 16; ++k)
-                        umma_f16(d, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), idesc,
-                                 (kb > kb0 || k > 0) ? 1u : 0u);
-                    umma_commit(smem_u32(empty + s));
+                        for (int k = 0; k < GB_K / 16; ++k)
+                            umma_f16(d, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), idesc,
+                                     (kc > kb || k > 0) ? 1u : 0u);
+                        umma_commit(smem_u32(empty + s));
+                    }
+                    umma_commit(smem_u32(tfull + b));
+                    kb = kend;
                 }
-                umma_commit(smem_u32(tfull + b));
             }
         }
     } else {
         // epilogue: warp w drains TMEM lanes [32 (w % 4), +32), columns [128 half, +128)
         const int q = warp & 3, half = (warp - 2) >> 2;
-        float acc[128];
-#pragma unroll
-        for (int i = 0; i < 128; ++i) acc[i] = 0.f;
         bool ok = true;
-        for (int c = 0; c < nchunks; ++c) {
-            const int b = c & 1;
-            if (ok && !mbar_wait(smem_u32(tfull + b), (uint32_t)(c >> 1) & 1u, GB_WAIT)) {
-                *fault = 1;
-                ok = false;
+        int c = 0;
+        for (int p = 0; p < np && ok; ++p) {
+            int t, k0, k1;
+            gemm_piece(P, p, total, t, k0, k1);
+            float acc[128];
+#pragma unroll
+            for (int i = 0; i < 128; ++i) acc[i] = 0.f;
+            for (int kb = k0; kb < k1; ++c) {
+                const int b = c & 1;
+                if (!mbar_wait(smem_u32(tfull + b), (uint32_t)(c >> 1) & 1u, GB_WAIT)) {
+                    *fault = 1;
+                    ok = false;
+                }
+                if (!ok || *fault) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * GB_N + 128 * half);
+#pragma unroll
+                for (int cc = 0; cc < 8; ++cc) {
+                    float v[16];
+                    tmem_ld16(base + 16 * cc, v);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) acc[16 * cc + i] += v[i];
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tfree + b)) : "memory");
+                kb = min(k1, kb + GB_CHUNK);
             }
-            if (!ok || *fault) break;
-            tc_fence_after();
-            const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * GB_N + 128 * half);
+            const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * GB_N;
+            const int row = m0 + 32 * q + lane; // row of D
+            const int h = row >> 1;
+            const bool odd = row & 1;
+            const bool store = ok && row < P.m2;
 #pragma unroll
             for (int cc = 0; cc < 8; ++cc) {
-                float v[16];
-                tmem_ld16(base + 16 * cc, v);
+                float o[16];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) acc[16 * cc + i] += v[i];
-            }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tfree + b)) : "memory");
-        }
-        const int row = m0 + 32 * q + lane; // row of D
-        const int h = row >> 1;
-        const bool odd = row & 1;
-        const bool store = ok && !*fault && row < P.m2;
+                for (int i = 0; i < 16; ++i) o[i] = __shfl_xor_sync(0xffffffffu, acc[16 * cc + i], 1);
+                if (!store) continue;
+                // even lane holds Re of row h, odd lane Im: even adds columns +0..7, odd +8..15
+                const int cb = n0 + 128 * half + 16 * cc + (odd ? 8 : 0);
+                float2 *dst = P.U + (size_t)h * P.n + cb;
+                if ((P.n & 1) == 0 && cb + 8 <= P.n) {
+                    // two complex values per 16-byte atomic (cb and n even: aligned)
 #pragma unroll
-        for (int cc = 0; cc < 8; ++cc) {
-            float o[16];
-#pragma unroll
-            for (int i = 0; i < 16; ++i) o[i] = __shfl_xor_sync(0xffffffffu, acc[16 * cc + i], 1);
-            if (!store) continue;
-            // even lane holds Re of row h, odd lane Im: even writes columns +0..7, odd +8..15
-            const int cb = n0 + 128 * half + 16 * cc + (odd ? 8 : 0);
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int col = cb + i;
-                if (col >= P.n) break;
-                const float re = odd ? o[8 + i] : acc[16 * cc + i];
-                const float im = odd ? acc[16 * cc + 8 + i] : o[i];
-                float2 *dst = P.U + (size_t)h * P.n + col;
-                if (P.accumulate) {
-                    const float2 prev = *dst;
-                    *dst = make_float2(prev.x + re, prev.y + im);
+                    for (int i = 0; i < 8; i += 2) {
+                        const float4 v = odd ? make_float4(o[8 + i], acc[16 * cc + 8 + i], o[9 + i], acc[16 * cc + 9 + i])
+                                             : make_float4(acc[16 * cc + i], o[i], acc[16 * cc + i + 1], o[i + 1]);
+                        atomicAdd(reinterpret_cast<float4 *>(dst + i), v);
+                    }
                 } else {
-                    *dst = make_float2(re, im);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        if (cb + i >= P.n) break;
+                        const float re = odd ? o[8 + i] : acc[16 * cc + i];
+                        const float im = odd ? acc[16 * cc + 8 + i] : o[i];
+                        atomicAdd(dst + i, make_float2(re, im));
+                    }
                 }
             }
         }
@@ -315,6 +372,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
 namespace {
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+double g_tail_weight = 1.2;
 std::mutex g_encode_mu;
 int *g_err_flag[64] = {};
 
@@ -429,21 +487,55 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
     P.m2 = 2 * ny;
     P.n = nx;
     P.kblocks = kp / GB_K;
+    P.tiles_n = (nx + GB_N - 1) / GB_N;
+    const long long tiles = (long long)P.tiles_n * ((2 * ny + GB_M - 1) / GB_M);
+    P.tiles = (int)tiles;
     P.U = (float2 *)U;
-    P.accumulate = (flags & OLG_ACCUMULATE) ? 1 : 0;
     P.err = err;
     static bool attr_done[64] = {};
+    static int sm_count[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
     if (!attr_done[dev]) {
         cudaError_t e = cudaFuncSetAttribute(k_cgh_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM);
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm)");
+        e = cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(SM count)");
         attr_done[dev] = true;
     }
-    dim3 grid((nx + GB_N - 1) / GB_N, (2 * ny + GB_M - 1) / GB_M);
+    // SMs left over after one CTA per tile (one CTA per SM: ~197 KB of shared
+    // memory) take the K tails: with e extra CTAs each holds `per` tails.  A
+    // tail K block costs g_tail_weight tile K blocks (its operands are not
+    // shared in L2 with other CTAs at the time), so split = total per w /
+    // (per w + 1) evens the two kinds of CTA; w <= 0 turns the split off.
+    const int total = 3 * P.kblocks;
+    P.split = total;
+    P.extra = 0;
+    if (tiles < sm_count[dev] && g_tail_weight > 0.0) {
+        const int e = sm_count[dev] - (int)tiles;
+        const int per = ((int)tiles + e - 1) / e;
+        const double pw = per * g_tail_weight;
+        const int split = (int)((double)total * pw / (pw + 1.0));
+        if (split > 0 && split < total) {
+            P.split = split;
+            P.extra = std::min(e, (int)tiles);
+        }
+    }
+    if (!(flags & OLG_ACCUMULATE)) {
+        const cudaError_t e = cudaMemsetAsync(U, 0, sizeof(float2) * (size_t)ny * nx, st);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    }
+    const int grid = (int)tiles + P.extra;
     k_cgh_gemm<<<grid, GB_THREADS, GB_SMEM, st>>>(mAh, mAl, mBh, mBl, P);
     count_launch();
     return check_launch("k_cgh_gemm");
+}
+
+extern "C" double olg_cgh_gemm_tail_weight(double w)
+{
+    const double old = g_tail_weight;
+    if (w >= 0.0 && w <= 16.0) g_tail_weight = w;
+    return old;
 }
 
 extern "C" int olg_device_fault_check(int clear)

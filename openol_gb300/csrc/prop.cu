@@ -350,6 +350,108 @@ __device__ __forceinline__ void cols_body(const PropParams &P, int c0, float2 *s
     }
 }
 
+// ======================================================= persistent row passes
+// The same row transforms as rows_fwd_body / rows_inv_body, but each CTA loops
+// over row groups g = blockIdx.x, + gridDim.x, ... and issues the global loads
+// of its next group into registers before it runs the current group through
+// shared memory, so that the loads' latency overlaps the butterflies.
+template <int N, int NT, int NSEQ>
+__device__ __forceinline__ void rows_fwd_body_persist(const PropParams &P, float2 *sm, int tid)
+{
+    constexpr int SS = padded_len(N), B = N / 16;
+    constexpr int BPT = NSEQ * B / NT;
+    const int groups = (P.ny + NSEQ - 1) / NSEQ;
+    float2 nv[BPT][8];
+    auto fetch = [&](int g) {
+#pragma unroll
+        for (int t = 0; t < BPT; ++t) {
+            const int b = tid + t * NT, q = b / B, j = b % B, h = g * NSEQ + q;
+            const bool live = g < groups && h < P.ny;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) nv[t][r] = live ? load_in(P, h, j + r * B) : make_float2(0.f, 0.f);
+        }
+    };
+    fetch(blockIdx.x);
+    for (int g = blockIdx.x; g < groups; g += gridDim.x) {
+#pragma unroll
+        for (int t = 0; t < BPT; ++t) {
+            const int b = tid + t * NT, q = b / B, j = b % B;
+            float2 v[16];
+#pragma unroll
+            for (int r = 4; r < 12; ++r) v[r] = nv[t][r - 4];
+            dft16_in_mid<-1>(v);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+        }
+        fetch(g + gridDim.x);
+        __syncthreads();
+        mid_stages<N, -1, NT, false, NSEQ>(sm, SS, g_tw, tid);
+#pragma unroll
+        for (int t = 0; t < BPT; ++t) {
+            const int b = tid + t * NT, q = b / B, j = b % B, h = g * NSEQ + q;
+            float2 v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+            last_twiddle<N, -1>(v, j, g_tw);
+            dft<16, -1>(v);
+            if (h < P.ny) {
+#pragma unroll
+                for (int k = 0; k < 16; ++k) __stcg(P.S + (size_t)h * N + j + k * B, v[outpos<16>(k)]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int N, int NT, int NSEQ>
+__device__ __forceinline__ void rows_inv_body_persist(const PropParams &P, float2 *sm, int tid, float &lsum)
+{
+    constexpr int SS = padded_len(N), B = N / 16;
+    constexpr int BPT = NSEQ * B / NT;
+    const int groups = (P.ny + NSEQ - 1) / NSEQ;
+    float2 nv[BPT][16];
+    auto fetch = [&](int g) {
+#pragma unroll
+        for (int t = 0; t < BPT; ++t) {
+            const int b = tid + t * NT, q = b / B, j = b % B, h = g * NSEQ + q;
+            const bool live = g < groups && h < P.ny;
+#pragma unroll
+            for (int r = 0; r < 16; ++r)
+                nv[t][r] = live ? __ldcg(P.S + (size_t)h * N + j + r * B) : make_float2(0.f, 0.f);
+        }
+    };
+    fetch(blockIdx.x);
+    for (int g = blockIdx.x; g < groups; g += gridDim.x) {
+#pragma unroll
+        for (int t = 0; t < BPT; ++t) {
+            const int b = tid + t * NT, q = b / B, j = b % B;
+            float2 v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = nv[t][r];
+            dft<16, +1>(v);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+        }
+        fetch(g + gridDim.x);
+        __syncthreads();
+        mid_stages<N, +1, NT, false, NSEQ>(sm, SS, g_tw, tid);
+#pragma unroll
+        for (int t = 0; t < BPT; ++t) {
+            const int b = tid + t * NT, q = b / B, j = b % B, h = g * NSEQ + q;
+            float2 v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+            last_twiddle<N, +1>(v, j, g_tw);
+            dft16_out_mid<+1>(v);
+            if (h < P.ny) {
+#pragma unroll
+                for (int k = 4; k < 12; ++k) store_out(P, h, j + (k - 4) * B, v[outpos<16>(k)], lsum);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ======================================================= paired passes
 // Two rows (passes 1 and 3) or two adjacent columns (pass 2) per butterfly,
 // in planar pairs on the paired FP32 pipe (fftp.cuh).  Same stages, pruning
@@ -518,10 +620,10 @@ __device__ __forceinline__ void cols_body_p(const PropParams &P, int c0, float4 
 // Launch-shape variants of the v2 passes (threads, elements per CTA, minimum
 // resident CTAs); olg_autotune_prop times them on the device and keeps the
 // fastest per FFT length.
-template <int NT_, int E_, int MINB_, bool PAIRED_ = false>
+template <int NT_, int E_, int MINB_, bool PAIRED_ = false, bool PERSIST_ = false>
 struct Shape {
     static constexpr int NT = NT_, E = E_, MINB = MINB_;
-    static constexpr bool PAIRED = PAIRED_;
+    static constexpr bool PAIRED = PAIRED_, PERSIST = PERSIST_;
 };
 // rows: E = row elements per CTA (NSEQ = E / N rows, at least one; paired
 // variants: NSEQ = E / 2N row pairs, at least one)
@@ -534,7 +636,10 @@ template <> struct RowVar<4> : Shape<128, 4096, 4, true> {};
 template <> struct RowVar<5> : Shape<256, 8192, 2, true> {};
 template <> struct RowVar<6> : Shape<512, 16384, 1, true> {};
 template <> struct RowVar<7> : Shape<64, 2048, 8, true> {};
-constexpr int N_ROW_VARIANTS = 8;
+// persistent: one grid of SMs x MINB CTAs looping over row groups
+template <> struct RowVar<8> : Shape<128, 2048, 4, false, true> {};
+template <> struct RowVar<9> : Shape<256, 4096, 2, false, true> {};
+constexpr int N_ROW_VARIANTS = 10;
 // columns: E = elements per CTA (C = E / N adjacent columns; paired variants:
 // C = E / 2N adjacent column pairs)
 template <int I> struct ColVar;
@@ -551,7 +656,8 @@ constexpr int N_COL_VARIANTS = 8;
 template <int N, class V>
 struct RowShape {
     static constexpr int NT = V::NT;
-    static constexpr bool PAIRED = V::PAIRED;
+    static constexpr bool PAIRED = V::PAIRED, PERSIST = V::PERSIST;
+    static constexpr int MINB = V::MINB;
     static constexpr int NSEQ = PAIRED ? (V::E >= 2 * N ? V::E / (2 * N) : 1) : (V::E >= N ? V::E / N : 1);
     static constexpr int ROWS = PAIRED ? 2 * NSEQ : NSEQ; // field rows per CTA
     static constexpr int SMEM = NSEQ * padded_len(N) * (PAIRED ? 16 : 8);
@@ -576,7 +682,8 @@ __global__ void __launch_bounds__(V::NT, V::MINB) k_rows_fwd2(PropParams P)
     pdl_enter();
     extern __shared__ float2 sm[];
     using S = RowShape<N, V>;
-    if constexpr (S::valid) rows_fwd_body<N, S::NT, S::NSEQ>(P, blockIdx.x * S::NSEQ, sm, threadIdx.x);
+    if constexpr (S::valid && S::PERSIST) rows_fwd_body_persist<N, S::NT, S::NSEQ>(P, sm, threadIdx.x);
+    else if constexpr (S::valid) rows_fwd_body<N, S::NT, S::NSEQ>(P, blockIdx.x * S::NSEQ, sm, threadIdx.x);
 }
 
 template <int N, class V>
@@ -587,7 +694,8 @@ __global__ void __launch_bounds__(V::NT, V::MINB) k_rows_inv2(PropParams P)
     using S = RowShape<N, V>;
     if constexpr (S::valid) {
         float lsum = 0.f;
-        rows_inv_body<N, S::NT, S::NSEQ>(P, blockIdx.x * S::NSEQ, sm, threadIdx.x, lsum);
+        if constexpr (S::PERSIST) rows_inv_body_persist<N, S::NT, S::NSEQ>(P, sm, threadIdx.x, lsum);
+        else rows_inv_body<N, S::NT, S::NSEQ>(P, blockIdx.x * S::NSEQ, sm, threadIdx.x, lsum);
         if (P.post_mode == OP_SEED) loss_reduce(lsum, P.loss, threadIdx.x, S::NT);
     }
 }
@@ -731,6 +839,20 @@ int launch_pdl(void (*kern)(Arg), int grid, int block, int smem, cudaStream_t st
 // selected variant per FFT length (index log2 N) and pass kind (0 rows fwd, 1 cols, 2 rows inv)
 int g_variant[3][14] = {};
 
+// SMs of the current device (cached per device; 152 on GB300)
+int sm_count()
+{
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
 template <int N, int I>
 int launch_rows_v(const PropParams &P, bool inverse, cudaStream_t st)
 {
@@ -746,7 +868,8 @@ int launch_rows_v(const PropParams &P, bool inverse, cudaStream_t st)
         if (int rc = prep_smem(k_rows_inv3<N, RowVar<I>>, S::SMEM)) return rc;
         return launch_pdl(k_rows_inv3<N, RowVar<I>>, grid, S::NT, S::SMEM, st, P, "k_rows_inv3");
     } else {
-        const int grid = (P.ny + S::ROWS - 1) / S::ROWS;
+        int grid = (P.ny + S::ROWS - 1) / S::ROWS;
+        if constexpr (S::PERSIST) grid = std::min(grid, sm_count() * S::MINB);
         if (!inverse) {
             if (int rc = prep_smem(k_rows_fwd2<N, RowVar<I>>, S::SMEM)) return rc;
             return launch_pdl(k_rows_fwd2<N, RowVar<I>>, grid, S::NT, S::SMEM, st, P, "k_rows_fwd2");
@@ -785,6 +908,8 @@ bool row_variant_valid(int i)
     case 5: return RowShape<N, RowVar<5>>::valid;
     case 6: return RowShape<N, RowVar<6>>::valid;
     case 7: return RowShape<N, RowVar<7>>::valid;
+    case 8: return RowShape<N, RowVar<8>>::valid;
+    case 9: return RowShape<N, RowVar<9>>::valid;
     default: return false;
     }
 }
@@ -818,6 +943,8 @@ int launch_rows(const PropParams &P, bool inverse, cudaStream_t st)
         case 5: return launch_rows_v<N, 5>(P, inverse, st);
         case 6: return launch_rows_v<N, 6>(P, inverse, st);
         case 7: return launch_rows_v<N, 7>(P, inverse, st);
+        case 8: return launch_rows_v<N, 8>(P, inverse, st);
+        case 9: return launch_rows_v<N, 9>(P, inverse, st);
         default: return launch_rows_v<N, 0>(P, inverse, st);
         }
     } else {

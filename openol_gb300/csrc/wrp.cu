@@ -11,8 +11,9 @@
 //   k_wrp_scan   exclusive scan of the counts (one CTA)
 //   k_wrp_fill   per point: append its index to each covered tile's list
 //   k_wrp_tile   per tile: sort the list (deterministic order), then for each
-//                pixel x listed point: window test in float32 exactly as the
-//                reference evaluates it (each operation rounded), and the
+//                listed point a warp-uniform cull of the warp's 16 x 8 strip, and
+//                for each pixel x kept point: window test in float32 exactly as
+//                the reference evaluates it (each operation rounded), and the
 //                term exp(i pi rho^2 / (lambda dz)) / |dz| with the phase anchored
 //                at the tile centre in double-float arithmetic.
 // Step 2 is the fused propagation in prop.cu.
@@ -76,15 +77,23 @@ __global__ void k_wrp_prep(WrpParams P)
     P.bbox[j] = bb;
 }
 
-// exclusive scan of count[0..T) into offset[0..T], one CTA of 1024 threads
+// exclusive scan of count[0..T) into offset[0..T], and the largest count into
+// offset[T + 1]; one CTA of 1024 threads
 __global__ void __launch_bounds__(1024) k_wrp_scan(const int *count, int *offset, int *cursor, int T)
 {
     __shared__ int part[1024];
+    __shared__ int cmax;
     const int tid = threadIdx.x;
     const int per = (T + 1023) / 1024;
     const int b = tid * per, e = min(b + per, T);
-    int s = 0;
-    for (int i = b; i < e; ++i) s += count[i];
+    if (tid == 0) cmax = 0;
+    __syncthreads();
+    int s = 0, mx = 0;
+    for (int i = b; i < e; ++i) {
+        s += count[i];
+        mx = max(mx, count[i]);
+    }
+    atomicMax(&cmax, mx);
     part[tid] = s;
     __syncthreads();
     for (int off = 1; off < 1024; off <<= 1) {
@@ -100,6 +109,7 @@ __global__ void __launch_bounds__(1024) k_wrp_scan(const int *count, int *offset
         run += count[i];
     }
     if (tid == 1023) offset[T] = part[1023];
+    if (tid == 0) offset[T + 1] = cmax;
 }
 
 __global__ void k_wrp_fill(WrpParams P)
@@ -130,30 +140,59 @@ __device__ __forceinline__ void bitonic_sort(int *a, int n, int tid, int nt)
         }
 }
 
-__global__ void __launch_bounds__(256) k_wrp_tile(WrpParams P)
+// One CTA of two warps per 16 x 16 tile.  Warp w covers the 8-row strip
+// [8 w, 8 w + 8); lane l owns column l % 16 and rows r0, r0 + 2, r0 + 4, r0 + 6
+// (r0 = 8 w + l / 16), taken as two row pairs on the paired FP32 pipe, so each
+// point's constants are read once per 4 pixels.  Before the per-pixel tests a
+// warp skips, uniformly, every point whose window cannot reach its strip (a
+// conservative test with a 1e-4 relative margin; the exact float test decides
+// every pixel it keeps), and every row pair with no pixel inside.  Pixels
+// outside the window get weight 0 instead of a branch.  ids: the tile's point
+// list, sorted (dynamic shared memory, `sort_cap` entries).
+constexpr int WNT = 64; // threads per tile
+constexpr int WNB = 64; // points per batch
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
+template <int WIN>
+__global__ void __launch_bounds__(WNT) k_wrp_tile(WrpParams P, int sort_cap)
 {
-    __shared__ int ids[WLIST_MAX];
-    __shared__ float4 cst[256][2]; // {c0, ax, ay, b} {x, y, Rtest, A}
-    const int tid = threadIdx.x;
+    extern __shared__ int ids[];
+    __shared__ float4 cst[WNB][2]; // {c0, ax, ay, b} {x, y, Rtest, A}
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int t = blockIdx.x;
     const int tx_t = t % P.tiles_x, ty_t = t / P.tiles_x;
-    const int w = tx_t * WT + (tid & 15), h = ty_t * WT + (tid >> 4);
-    const float dw = (float)(tid & 15) - 7.5f, dh = (float)(tid >> 4) - 7.5f;
-    const float q2 = dw * dw + dh * dh;
+    const int col = lane & 15, r0 = warp * 8 + (lane >> 4);
+    const int w = tx_t * WT + col;
+    const float dw = (float)col - 7.5f;
     const float wc = (float)(tx_t * WT) + 7.5f, hc = (float)(ty_t * WT) + 7.5f;
-    // per-pixel window-test operands, rounded as the reference's float code
-    const float pw = __fmul_rn(P.p, (float)w), ph = __fmul_rn(P.p, (float)h);
+    // per-pixel window-test operands, rounded as the reference's float code;
+    // pair k holds rows r0 + 4 k and r0 + 4 k + 2
+    const float pw = __fmul_rn(P.p, (float)w);
+    float2 php[2], dhp[2], q2p[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int ra = r0 + 4 * k, rb = ra + 2;
+        php[k] = make_float2(__fmul_rn(P.p, (float)(ty_t * WT + ra)), __fmul_rn(P.p, (float)(ty_t * WT + rb)));
+        dhp[k] = make_float2((float)ra - 7.5f, (float)rb - 7.5f);
+        q2p[k] = make_float2(dw * dw + dhp[k].x * dhp[k].x, dw * dw + dhp[k].y * dhp[k].y);
+    }
+    // the warp's strip in metres
+    const float xl = __fmul_rn(P.p, (float)(tx_t * WT)), xr = __fmul_rn(P.p, (float)(tx_t * WT + WT - 1));
+    const float yl = __fmul_rn(P.p, (float)(ty_t * WT + 8 * warp)), yr = __fmul_rn(P.p, (float)(ty_t * WT + 8 * warp + 7));
     const int beg = P.offset[t], cnt = P.offset[t + 1] - beg;
-    float2 acc = make_float2(0.f, 0.f);
-    const bool sorted = cnt <= WLIST_MAX;
+    const bool sorted = cnt <= sort_cap;
     if (sorted) {
         int np2 = 1;
         while (np2 < cnt) np2 <<= 1;
-        for (int i = tid; i < np2; i += 256) ids[i] = i < cnt ? P.list[beg + i] : 0x7fffffff;
+        for (int i = tid; i < np2; i += WNT) ids[i] = i < cnt ? P.list[beg + i] : 0x7fffffff;
         __syncthreads();
-        bitonic_sort(ids, np2, tid, 256);
+        bitonic_sort(ids, np2, tid, WNT);
     }
-    for (int b0 = 0; b0 < cnt; b0 += 256) {
+    float2 acc[4]; // (re, im) of rows r0, r0 + 2, r0 + 4, r0 + 6
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] = make_float2(0.f, 0.f);
+    for (int b0 = 0; b0 < cnt; b0 += WNB) {
         const int k = b0 + tid;
         float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = make_float4(0.f, 0.f, -1.f, 0.f);
         if (k < cnt) {
@@ -168,35 +207,64 @@ __global__ void __launch_bounds__(256) k_wrp_tile(WrpParams P)
             c0 = make_float4(df_frac(df_mul(rho2, k2)), 2.0f * Dx.hi * P.p * kk, 2.0f * Dy.hi * P.p * kk,
                              P.p * P.p * kk);
             const float R = P.R[j];
-            const float Rt = P.window == 0 ? __fmul_rn(R, R) : R;
+            const float Rt = WIN == 0 ? __fmul_rn(R, R) : R;
             c1 = make_float4(x, y, Rt, 1.0f / fabsf(dz.hi + dz.lo));
         }
         cst[tid][0] = c0;
         cst[tid][1] = c1;
         __syncthreads();
-        const int m = min(256, cnt - b0);
-        float2 part = make_float2(0.f, 0.f);
+        const int m = min(WNB, cnt - b0);
+        float2 part[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) part[q] = make_float2(0.f, 0.f);
         for (int i = 0; i < m; ++i) {
-            const float4 a = cst[i][0], b = cst[i][1];
-            const float ddx = __fsub_rn(pw, b.x), ddy = __fsub_rn(ph, b.y);
-            bool inside;
-            if (P.window == 0) {
-                inside = __fadd_rn(__fmul_rn(ddx, ddx), __fmul_rn(ddy, ddy)) < b.z;
-            } else {
-                inside = (__fmul_rn(fabsf(ddx), 2.0f) <= b.z) && (__fmul_rn(fabsf(ddy), 2.0f) <= b.z);
-            }
-            if (inside) {
-                const float c = fmaf(a.y, dw, fmaf(a.z, dh, fmaf(a.w, q2, a.x)));
-                const float2 e = cis_cycles(wrap_cycles(c));
-                part.x = fmaf(b.w, e.x, part.x);
-                part.y = fmaf(b.w, e.y, part.y);
+            const float4 b = cst[i][1];
+            // warp-uniform: can the window reach the strip at all?
+            const float ex = fmaxf(fmaxf(xl - b.x, b.x - xr), 0.f), ey = fmaxf(fmaxf(yl - b.y, b.y - yr), 0.f);
+            const float lim = b.z * 1.0001f;
+            const bool reach = WIN == 0 ? ex * ex + ey * ey <= lim : (2.f * ex <= lim && 2.f * ey <= lim);
+            if (!reach) continue;
+            const float4 a = cst[i][0];
+            const float ddx = __fsub_rn(pw, b.x);
+            const float ddx2 = __fmul_rn(ddx, ddx);
+            const bool xin = __fmul_rn(fabsf(ddx), 2.0f) <= b.z;
+            const float base = fmaf(a.y, dw, a.x);
+#pragma unroll
+            for (int pr = 0; pr < 2; ++pr) {
+                // the window test in scalar rounded operations (never contracted)
+                const float dya = __fsub_rn(php[pr].x, b.y), dyb = __fsub_rn(php[pr].y, b.y);
+                bool in0, in1;
+                if (WIN == 0) {
+                    in0 = __fadd_rn(ddx2, __fmul_rn(dya, dya)) < b.z;
+                    in1 = __fadd_rn(ddx2, __fmul_rn(dyb, dyb)) < b.z;
+                } else {
+                    in0 = xin && __fmul_rn(fabsf(dya), 2.0f) <= b.z;
+                    in1 = xin && __fmul_rn(fabsf(dyb), 2.0f) <= b.z;
+                }
+                if (!__any_sync(0xffffffffu, in0 || in1)) continue;
+                const float wa = in0 ? b.w : 0.f, wb = in1 ? b.w : 0.f;
+                const float2 cyc = __ffma2_rn(f2(a.z), dhp[pr], __ffma2_rn(f2(a.w), q2p[pr], f2(base)));
+                const float2 r = __fadd2_rn(__fadd2_rn(cyc, f2(12582912.0f)), f2(-12582912.0f));
+                const float2 ang = __fmul2_rn(__ffma2_rn(r, f2(-1.0f), cyc), f2(6.283185307179586f));
+                float sa, ca, sb, cb;
+                __sincosf(ang.x, &sa, &ca);
+                __sincosf(ang.y, &sb, &cb);
+                part[2 * pr] = __ffma2_rn(f2(wa), make_float2(ca, sa), part[2 * pr]);
+                part[2 * pr + 1] = __ffma2_rn(f2(wb), make_float2(cb, sb), part[2 * pr + 1]);
             }
         }
-        acc.x += part.x;
-        acc.y += part.y;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] = __fadd2_rn(acc[q], part[q]);
         __syncthreads();
     }
-    if (w < P.nx && h < P.ny) P.U[(size_t)h * P.nx + w] = acc;
+    if (w < P.nx) {
+        // acc[2 pr + e] is row r0 + 4 pr + 2 e
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int h = ty_t * WT + r0 + 4 * (q >> 1) + 2 * (q & 1);
+            if (h < P.ny) P.U[(size_t)h * P.nx + w] = acc[q];
+        }
+    }
 }
 
 } // namespace olg
@@ -238,14 +306,14 @@ extern "C" int olg_wrp_step1_c64(const float *points, int n_points, void *U, int
     const int T = P.tiles_x * P.tiles_y;
     P.U = (float2 *)U;
     const size_t nb = (size_t)(n_points > 0 ? n_points : 1);
-    const size_t head = align_up(nb * 4, 256) + align_up(nb * 16, 256) + 3 * align_up((size_t)(T + 1) * 4, 256);
+    const size_t head = align_up(nb * 4, 256) + align_up(nb * 16, 256) + 3 * align_up((size_t)(T + 2) * 4, 256);
     Scratch s1;
     if (int rc = s1.acquire(nullptr, 0, head, st)) return rc;
     char *b = (char *)s1.ptr;
     P.R = (float *)b; b += align_up(nb * 4, 256);
     P.bbox = (int4 *)b; b += align_up(nb * 16, 256);
-    P.count = (int *)b; b += align_up((size_t)(T + 1) * 4, 256);
-    P.offset = (int *)b; b += align_up((size_t)(T + 1) * 4, 256);
+    P.count = (int *)b; b += align_up((size_t)(T + 2) * 4, 256);
+    P.offset = (int *)b; b += align_up((size_t)(T + 2) * 4, 256);
     P.cursor = (int *)b;
     cudaError_t e = cudaMemsetAsync(P.count, 0, (size_t)(T + 1) * 4, st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
@@ -257,10 +325,14 @@ extern "C" int olg_wrp_step1_c64(const float *points, int n_points, void *U, int
     k_wrp_scan<<<1, 1024, 0, st>>>(P.count, P.offset, P.cursor, T);
     count_launch();
     if (int rc = check_launch("k_wrp_scan")) return rc;
-    int total = 0;
-    e = cudaMemcpyAsync(&total, P.offset + T, sizeof(int), cudaMemcpyDeviceToHost, st);
+    int tot_max[2] = {0, 0}; // pairs, longest tile list
+    e = cudaMemcpyAsync(tot_max, P.offset + T, sizeof(tot_max), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "reading the WRP pair count");
+    const int total = tot_max[0];
+    // tile lists up to WLIST_MAX entries are sorted in shared memory (deterministic sums)
+    int sort_cap = 1;
+    while (sort_cap < tot_max[1] && sort_cap < WLIST_MAX) sort_cap <<= 1;
     Scratch s2;
     if (int rc = s2.acquire(nullptr, 0, (size_t)(total > 0 ? total : 1) * 4, st)) return rc;
     P.list = (int *)s2.ptr;
@@ -269,7 +341,9 @@ extern "C" int olg_wrp_step1_c64(const float *points, int n_points, void *U, int
         count_launch();
         if (int rc = check_launch("k_wrp_fill")) return rc;
     }
-    k_wrp_tile<<<T, 256, 0, st>>>(P);
+    const size_t smem = (size_t)sort_cap * sizeof(int);
+    if (window == OLG_WINDOW_CIRCLE) k_wrp_tile<0><<<T, WNT, smem, st>>>(P, sort_cap);
+    else k_wrp_tile<1><<<T, WNT, smem, st>>>(P, sort_cap);
     count_launch();
     return check_launch("k_wrp_tile");
 }
