@@ -18,8 +18,9 @@
  *  - Asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream).
  *  - `work`/`work_bytes`: optional caller-provided device scratch of at least
  *    the size reported by the matching *_workspace_bytes() query.  With
- *    work == NULL the library takes stream-ordered scratch from the CUDA memory
- *    pool (cudaMallocAsync / cudaFreeAsync on `stream`).
+ *    work == NULL the library takes stream-ordered scratch on `stream` from
+ *    its own CUDA memory pool per device, which keeps up to 8 GiB of freed
+ *    scratch mapped between calls (the device's default pool is not used).
  *  - In-place operation is allowed wherever an input and an output pointer
  *    have the same shape (u_in == u_out).
  *  - Sizes: each axis n (ny or nx) is a power of two in [16, 4096] (tuned

@@ -4,6 +4,8 @@
 #include <cstdio>
 #include <string>
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace olg {
@@ -33,6 +35,35 @@ int check_launch(const char *what)
 
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// The library's own stream-ordered pool per device.  It keeps up to 8 GiB of
+// freed scratch mapped between calls: the default pool returns everything at
+// each synchronisation, and re-mapping a few hundred MB per call (the WRP pair
+// lists) cost more than the kernels that use it.  Leaves the device's default
+// pool untouched.
+static cudaMemPool_t scratch_pool()
+{
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pools[dev]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t p = nullptr;
+        if (cudaMemPoolCreate(&p, &props) == cudaSuccess) {
+            unsigned long long keep = 8ull << 30;
+            cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+            pools[dev] = p;
+        } else if (cudaDeviceGetDefaultMemPool(&p, dev) == cudaSuccess) {
+            pools[dev] = p;
+        }
+    }
+    return pools[dev];
+}
+
 int Scratch::acquire(void *work, size_t work_bytes, size_t need, cudaStream_t s)
 {
     stream = s;
@@ -44,10 +75,10 @@ int Scratch::acquire(void *work, size_t work_bytes, size_t need, cudaStream_t s)
         owned = false;
         return OLG_OK;
     }
-    cudaError_t e = cudaMallocAsync(&ptr, need, s);
+    cudaError_t e = cudaMallocFromPoolAsync(&ptr, need, scratch_pool(), s);
     if (e != cudaSuccess) {
         ptr = nullptr;
-        return cuda_fail(e, "cudaMallocAsync (scratch)");
+        return cuda_fail(e, "cudaMallocFromPoolAsync (scratch)");
     }
     bytes = need;
     owned = true;

@@ -6,17 +6,23 @@
 // useful terms.  Here the points are binned onto 16 x 16 pixel tiles by the
 // bounding box of their window, and one CTA per tile sums only the points
 // listed for it:
-//   k_wrp_prep   per point: window radius (float, as the reference computes
-//                it), tile bounding box, per-tile counts (atomics)
-//   k_wrp_scan   exclusive scan of the counts (one CTA)
-//   k_wrp_fill   per point: append its index to each covered tile's list
-//   k_wrp_tile   per tile: sort the list (deterministic order), then for each
-//                listed point a warp-uniform cull of the warp's 16 x 8 strip, and
-//                for each pixel x kept point: window test in float32 exactly as
-//                the reference evaluates it (each operation rounded), and the
-//                term exp(i pi rho^2 / (lambda dz)) / |dz| with the phase anchored
-//                at the tile centre in double-float arithmetic.
+//   k_wrp_prep     per point: window radius (float, as the reference computes
+//                  it), tile bounding box and its tile count
+//   (CUB scan)     each point's first slot in the (tile, point) pair list
+//   k_wrp_pairs    per point: its (tile, point) pairs, in point order
+//   (CUB sort)     stable radix sort of the pairs by tile: every tile's list
+//                  comes out in increasing point order (deterministic sums)
+//   k_wrp_offsets  per tile: start of its list (binary search of the keys)
+//   k_wrp_tile     per tile: for each listed point a warp-uniform cull of the
+//                  warp's 16 x 8 strip, and for each pixel x kept point: window
+//                  test in float32 exactly as the reference evaluates it (each
+//                  operation rounded), and the term exp(i pi rho^2 / (lambda dz))
+//                  / |dz| with the phase anchored at the tile centre in
+//                  double-float arithmetic.
 // Step 2 is the fused propagation in prop.cu.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
 #include <cmath>
 #include <cstdio>
 
@@ -25,19 +31,21 @@
 namespace olg {
 
 constexpr int WT = 16;          // tile edge (pixels)
-constexpr int WLIST_MAX = 4096; // list entries sorted in shared memory
 
 struct WrpParams {
     const float *pts;
     int n, ny, nx, tiles_x, tiles_y, window;
     float p, lambda, plane_z, plimit;
     float l_hi, l_lo;
-    float *R;    // per point: W (circle) or D (square)
-    int4 *bbox;  // per point: tile range [tx0, tx1] x [ty0, ty1], tx0 > tx1 if none
-    int *count;  // tiles + 1
-    int *offset; // tiles + 1
-    int *cursor; // tiles
-    int *list;
+    float *R;        // per point: W (circle) or D (square)
+    int4 *bbox;      // per point: tile range [tx0, tx1] x [ty0, ty1], tx0 > tx1 if none
+    int *pcount;     // per point: tiles in its box (n + 1 entries, last 0)
+    int *ppos;       // per point: first pair slot (exclusive scan of pcount; ppos[n] = pairs)
+    int *keys, *vals;     // pairs (tile, point), point-major
+    const int *skeys;     // pairs sorted by tile
+    const int *list;      // their points: every tile's list in increasing point order
+    int *offset;     // per tile: start of its list (tiles + 1 entries)
+    int pairs;
     float2 *U;
 };
 
@@ -55,6 +63,7 @@ __device__ __forceinline__ float wrp_radius(float z, const WrpParams &P)
 __global__ void k_wrp_prep(WrpParams P)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j == P.n) P.pcount[j] = 0;
     if (j >= P.n) return;
     const float x = P.pts[3 * j], y = P.pts[3 * j + 1], z = P.pts[3 * j + 2];
     const float R = wrp_radius(z, P);
@@ -67,77 +76,43 @@ __global__ void k_wrp_prep(WrpParams P)
     w0 = max(w0, 0L); h0 = max(h0, 0L);
     w1 = min(w1, (long)P.nx - 1); h1 = min(h1, (long)P.ny - 1);
     int4 bb;
+    int cnt = 0;
     if (w0 > w1 || h0 > h1 || !(R > 0.f)) {
         bb = make_int4(1, 0, 1, 0);
     } else {
         bb = make_int4((int)(w0 / WT), (int)(w1 / WT), (int)(h0 / WT), (int)(h1 / WT));
-        for (int ty = bb.z; ty <= bb.w; ++ty)
-            for (int tx = bb.x; tx <= bb.y; ++tx) atomicAdd(P.count + ty * P.tiles_x + tx, 1);
+        cnt = (bb.y - bb.x + 1) * (bb.w - bb.z + 1);
     }
     P.bbox[j] = bb;
+    P.pcount[j] = cnt;
 }
 
-// exclusive scan of count[0..T) into offset[0..T], and the largest count into
-// offset[T + 1]; one CTA of 1024 threads
-__global__ void __launch_bounds__(1024) k_wrp_scan(const int *count, int *offset, int *cursor, int T)
+// per point (one warp each, coalesced stores): its (tile, point) pairs from
+// slot ppos[j], tiles in raster order
+__global__ void k_wrp_pairs(WrpParams P)
 {
-    __shared__ int part[1024];
-    __shared__ int cmax;
-    const int tid = threadIdx.x;
-    const int per = (T + 1023) / 1024;
-    const int b = tid * per, e = min(b + per, T);
-    if (tid == 0) cmax = 0;
-    __syncthreads();
-    int s = 0, mx = 0;
-    for (int i = b; i < e; ++i) {
-        s += count[i];
-        mx = max(mx, count[i]);
-    }
-    atomicMax(&cmax, mx);
-    part[tid] = s;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const int v = tid >= off ? part[tid - off] : 0;
-        __syncthreads();
-        part[tid] += v;
-        __syncthreads();
-    }
-    int run = part[tid] - s;
-    for (int i = b; i < e; ++i) {
-        offset[i] = run;
-        cursor[i] = run;
-        run += count[i];
-    }
-    if (tid == 1023) offset[T] = part[1023];
-    if (tid == 0) offset[T + 1] = cmax;
-}
-
-__global__ void k_wrp_fill(WrpParams P)
-{
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = (int)(((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (j >= P.n) return;
     const int4 bb = P.bbox[j];
-    for (int ty = bb.z; ty <= bb.w; ++ty)
-        for (int tx = bb.x; tx <= bb.y; ++tx) {
-            const int pos = atomicAdd(P.cursor + ty * P.tiles_x + tx, 1);
-            P.list[pos] = j;
-        }
+    const int cnt = P.pcount[j], wdt = bb.y - bb.x + 1, o = P.ppos[j];
+    for (int k = lane; k < cnt; k += 32) {
+        P.keys[o + k] = (bb.z + k / wdt) * P.tiles_x + bb.x + k % wdt;
+        P.vals[o + k] = j;
+    }
 }
 
-__device__ __forceinline__ void bitonic_sort(int *a, int n, int tid, int nt)
+// offset[t] = first slot of tile t in the sorted keys (t = 0 .. tiles)
+__global__ void k_wrp_offsets(WrpParams P, int T)
 {
-    for (int k = 2; k <= n; k <<= 1)
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < n; i += nt) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const int ai = a[i], al = a[l];
-                    const bool up = (i & k) == 0;
-                    if ((ai > al) == up) { a[i] = al; a[l] = ai; }
-                }
-            }
-            __syncthreads();
-        }
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > T) return;
+    int lo = 0, hi = P.pairs;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (P.skeys[mid] < t) lo = mid + 1;
+        else hi = mid;
+    }
+    P.offset[t] = lo;
 }
 
 // One CTA of two warps per 16 x 16 tile.  Warp w covers the 8-row strip
@@ -147,17 +122,15 @@ __device__ __forceinline__ void bitonic_sort(int *a, int n, int tid, int nt)
 // warp skips, uniformly, every point whose window cannot reach its strip (a
 // conservative test with a 1e-4 relative margin; the exact float test decides
 // every pixel it keeps), and every row pair with no pixel inside.  Pixels
-// outside the window get weight 0 instead of a branch.  ids: the tile's point
-// list, sorted (dynamic shared memory, `sort_cap` entries).
+// outside the window get weight 0 instead of a branch.
 constexpr int WNT = 64; // threads per tile
 constexpr int WNB = 64; // points per batch
 
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 
 template <int WIN>
-__global__ void __launch_bounds__(WNT) k_wrp_tile(WrpParams P, int sort_cap)
+__global__ void __launch_bounds__(WNT) k_wrp_tile(WrpParams P)
 {
-    extern __shared__ int ids[];
     __shared__ float4 cst[WNB][2]; // {c0, ax, ay, b} {x, y, Rtest, A}
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int t = blockIdx.x;
@@ -181,14 +154,6 @@ __global__ void __launch_bounds__(WNT) k_wrp_tile(WrpParams P, int sort_cap)
     const float xl = __fmul_rn(P.p, (float)(tx_t * WT)), xr = __fmul_rn(P.p, (float)(tx_t * WT + WT - 1));
     const float yl = __fmul_rn(P.p, (float)(ty_t * WT + 8 * warp)), yr = __fmul_rn(P.p, (float)(ty_t * WT + 8 * warp + 7));
     const int beg = P.offset[t], cnt = P.offset[t + 1] - beg;
-    const bool sorted = cnt <= sort_cap;
-    if (sorted) {
-        int np2 = 1;
-        while (np2 < cnt) np2 <<= 1;
-        for (int i = tid; i < np2; i += WNT) ids[i] = i < cnt ? P.list[beg + i] : 0x7fffffff;
-        __syncthreads();
-        bitonic_sort(ids, np2, tid, WNT);
-    }
     float2 acc[4]; // (re, im) of rows r0, r0 + 2, r0 + 4, r0 + 6
 #pragma unroll
     for (int k = 0; k < 4; ++k) acc[k] = make_float2(0.f, 0.f);
@@ -196,7 +161,7 @@ __global__ void __launch_bounds__(WNT) k_wrp_tile(WrpParams P, int sort_cap)
         const int k = b0 + tid;
         float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = make_float4(0.f, 0.f, -1.f, 0.f);
         if (k < cnt) {
-            const int j = sorted ? ids[k] : P.list[beg + k];
+            const int j = P.list[beg + k];
             const float x = P.pts[3 * j], y = P.pts[3 * j + 1], z = P.pts[3 * j + 2];
             const df2 dz = df_two_sum(z, -P.plane_z);
             const df2 Dx = df_add_f(df_two_prod(P.p, wc), -x);
@@ -306,44 +271,60 @@ extern "C" int olg_wrp_step1_c64(const float *points, int n_points, void *U, int
     const int T = P.tiles_x * P.tiles_y;
     P.U = (float2 *)U;
     const size_t nb = (size_t)(n_points > 0 ? n_points : 1);
-    const size_t head = align_up(nb * 4, 256) + align_up(nb * 16, 256) + 3 * align_up((size_t)(T + 2) * 4, 256);
+    size_t scan_tmp = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, scan_tmp, (const int *)nullptr, (int *)nullptr, n_points + 1);
+    const size_t head = align_up(nb * 4, 256) + align_up(nb * 16, 256) + 2 * align_up((nb + 1) * 4, 256) +
+                        align_up((size_t)(T + 1) * 4, 256) + align_up(scan_tmp, 256);
     Scratch s1;
     if (int rc = s1.acquire(nullptr, 0, head, st)) return rc;
     char *b = (char *)s1.ptr;
     P.R = (float *)b; b += align_up(nb * 4, 256);
     P.bbox = (int4 *)b; b += align_up(nb * 16, 256);
-    P.count = (int *)b; b += align_up((size_t)(T + 2) * 4, 256);
-    P.offset = (int *)b; b += align_up((size_t)(T + 2) * 4, 256);
-    P.cursor = (int *)b;
-    cudaError_t e = cudaMemsetAsync(P.count, 0, (size_t)(T + 1) * 4, st);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    P.pcount = (int *)b; b += align_up((nb + 1) * 4, 256);
+    P.ppos = (int *)b; b += align_up((nb + 1) * 4, 256);
+    P.offset = (int *)b; b += align_up((size_t)(T + 1) * 4, 256);
+    void *scan_buf = b;
+    int pairs = 0;
     if (n_points > 0) {
-        k_wrp_prep<<<(n_points + 255) / 256, 256, 0, st>>>(P);
+        k_wrp_prep<<<(n_points + 1 + 255) / 256, 256, 0, st>>>(P);
         count_launch();
         if (int rc = check_launch("k_wrp_prep")) return rc;
+        cudaError_t e = cub::DeviceScan::ExclusiveSum(scan_buf, scan_tmp, P.pcount, P.ppos, n_points + 1, st);
+        if (e != cudaSuccess) return cuda_fail(e, "cub::DeviceScan::ExclusiveSum");
+        e = cudaMemcpyAsync(&pairs, P.ppos + n_points, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(e, "reading the WRP pair count");
+        if (pairs < 0) return fail(OLG_ERR_UNSUPPORTED_SIZE, "too many (tile, point) pairs");
     }
-    k_wrp_scan<<<1, 1024, 0, st>>>(P.count, P.offset, P.cursor, T);
-    count_launch();
-    if (int rc = check_launch("k_wrp_scan")) return rc;
-    int tot_max[2] = {0, 0}; // pairs, longest tile list
-    e = cudaMemcpyAsync(tot_max, P.offset + T, sizeof(tot_max), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return cuda_fail(e, "reading the WRP pair count");
-    const int total = tot_max[0];
-    // tile lists up to WLIST_MAX entries are sorted in shared memory (deterministic sums)
-    int sort_cap = 1;
-    while (sort_cap < tot_max[1] && sort_cap < WLIST_MAX) sort_cap <<= 1;
+    P.pairs = pairs;
+    int end_bit = 1;
+    while ((1 << end_bit) < T) ++end_bit;
+    size_t sort_tmp = 0;
+    if (pairs > 0)
+        cub::DeviceRadixSort::SortPairs(nullptr, sort_tmp, (const int *)nullptr, (int *)nullptr, (const int *)nullptr,
+                                        (int *)nullptr, pairs, 0, end_bit);
+    const size_t pb = align_up((size_t)(pairs > 0 ? pairs : 1) * 4, 256);
     Scratch s2;
-    if (int rc = s2.acquire(nullptr, 0, (size_t)(total > 0 ? total : 1) * 4, st)) return rc;
-    P.list = (int *)s2.ptr;
-    if (n_points > 0) {
-        k_wrp_fill<<<(n_points + 255) / 256, 256, 0, st>>>(P);
+    if (int rc = s2.acquire(nullptr, 0, 4 * pb + align_up(sort_tmp, 256), st)) return rc;
+    char *c = (char *)s2.ptr;
+    P.keys = (int *)c;
+    P.vals = (int *)(c + pb);
+    int *skeys = (int *)(c + 2 * pb), *svals = (int *)(c + 3 * pb);
+    P.skeys = skeys;
+    P.list = svals;
+    if (pairs > 0) {
+        k_wrp_pairs<<<(int)(((long)n_points * 32 + 255) / 256), 256, 0, st>>>(P);
         count_launch();
-        if (int rc = check_launch("k_wrp_fill")) return rc;
+        if (int rc = check_launch("k_wrp_pairs")) return rc;
+        const cudaError_t e = cub::DeviceRadixSort::SortPairs(c + 4 * pb, sort_tmp, P.keys, skeys, P.vals, svals,
+                                                              pairs, 0, end_bit, st);
+        if (e != cudaSuccess) return cuda_fail(e, "cub::DeviceRadixSort::SortPairs");
     }
-    const size_t smem = (size_t)sort_cap * sizeof(int);
-    if (window == OLG_WINDOW_CIRCLE) k_wrp_tile<0><<<T, WNT, smem, st>>>(P, sort_cap);
-    else k_wrp_tile<1><<<T, WNT, smem, st>>>(P, sort_cap);
+    k_wrp_offsets<<<(T + 1 + 255) / 256, 256, 0, st>>>(P, T);
+    count_launch();
+    if (int rc = check_launch("k_wrp_offsets")) return rc;
+    if (window == OLG_WINDOW_CIRCLE) k_wrp_tile<0><<<T, WNT, 0, st>>>(P);
+    else k_wrp_tile<1><<<T, WNT, 0, st>>>(P);
     count_launch();
     return check_launch("k_wrp_tile");
 }
