@@ -43,6 +43,13 @@ ADAM_DESC = "adam 2048x2048 phase, 8 planes z=80..150mm, p=6.4um, lambda=532nm, 
 CGH = dict(ny=1080, nx=1920, p=8e-6, lam=532e-9, n=10000, zc=0.1, box=5e-3, seed=20261203 + 2)
 ASM = dict(n=1024, p=8e-6, lam=532e-9, z=0.05, seed=20261203 + 1)
 WRP = dict(N=4096, p=4e-6, lam=532e-9, n=200000, zw=0.15, ext=10e-3, seed=20261203 + 3)
+# tilted planes (the row beside the path): the ASM workload's field, rotated 0.1 rad (source form)
+# or 2 mrad (reference form: its frequency shift a13 / (lambda du) is ~30 samples per mrad here)
+BATCH_DESC = ("batch 96 fields, sizes U{512,1024,2048,4096}^2, ASM/Fresnel/ARSS (s=0.5), z U[10,300]mm, "
+              "lambda U{640,532,450}nm, p=8um; one persistent launch in a CUDA graph")
+TILT = dict(n=1024, p=8e-6, lam=532e-9, z=0.05, angle=0.1, angle_ref=2e-3, seed=20261203 + 1)
+TILT_DESC = ("tilt 1024x1024 padded 2048x2048, p=8um, lambda=532nm, z=50mm, TiltedSourceProp ASM bilinear, "
+             "0.1 rad")
 ADAM = dict(n=2048, p=6.4e-6, lam=532e-9, planes=8, z0=0.08, dz=0.01, lr=0.05, seed=20261203 + 4)
 
 
@@ -154,6 +161,41 @@ def cpu_asm_sample():
     return 1.0 / (time.perf_counter() - t0)
 
 
+def cpu_tilt_sample():
+    import oracle as O
+    u = asm_input().astype(np.complex128)
+    t0 = time.perf_counter()
+    O.tilted_prop(u, TILT["p"], TILT["p"], TILT["lam"], TILT["z"], TILT["angle"], 0, 0, False)
+    return 1.0 / (time.perf_counter() - t0)
+
+
+def cpu_batch_sample():
+    """The batch's 96 fields drawn as the batch draws them; one field of each
+    size class propagated by the FP64 oracle (its own method, z, lambda),
+    every field of that class costed as it.  Returns props/s and the classes."""
+    import oracle as O
+    rng = np.random.default_rng(20261203 + 5)
+    sizes = rng.choice([512, 1024, 2048, 4096], 96)
+    methods = rng.choice(["asm", "fresnel", "arss"], 96)
+    zs = 0.01 + 0.29 * rng.random(96)
+    lams = rng.choice([640e-9, 532e-9, 450e-9], 96)
+    t_cls = {}
+    fr = np.random.default_rng(5)
+    for m in (512, 1024, 2048, 4096):
+        k = int(np.nonzero(sizes == m)[0][0])
+        u = (fr.random((m, m)) < 0.5) * np.exp(2j * np.pi * fr.random((m, m)))
+        t0 = time.perf_counter()
+        if methods[k] == "asm":
+            O.asm_prop(u, 8e-6, 8e-6, float(lams[k]), float(zs[k]))
+        elif methods[k] == "fresnel":
+            O.fresnel_prop(u, 8e-6, 8e-6, float(lams[k]), float(zs[k]))
+        else:
+            O.arss_prop(u, 8e-6, 8e-6, float(lams[k]), float(zs[k]), 0.5)
+        t_cls[m] = time.perf_counter() - t0
+    total = sum(t_cls[int(m)] for m in sizes)
+    return 96 / total, t_cls
+
+
 def wrp_points():
     c = WRP
     rng = np.random.default_rng(c["seed"])
@@ -234,6 +276,23 @@ def run_reference(args):
         metric, unit = "WRP holograms/s", "holograms/s"
         sample = "WRP step 1 on a seeded 1% point subset (scaled x100) + full 4096^2 FP64 ASM, per step"
         config = {"workload": WRP_DESC}
+    elif wl == "batch":
+        for k in range(1 + min(args.steps, 2)):
+            v, _ = cpu_batch_sample()
+            if k >= 1:
+                vals.append(v)
+        metric, unit = "batched props/s", "props/s"
+        sample = ("one field per size class (512^2 .. 4096^2) of the 96-field batch, FP64, each class costed "
+                  "for all its fields, per step")
+        config = {"workload": BATCH_DESC}
+    elif wl == "tilt":
+        for k in range(1 + min(args.steps, 3)):
+            v = cpu_tilt_sample()
+            if k >= 1:
+                vals.append(v)
+        metric, unit = "tilted props/s", "props/s"
+        sample = "one full 1024^2 -> 2048^2 FP64 TiltedSourceProp (ASM, bilinear) per step"
+        config = {"workload": TILT_DESC}
     else:
         for k in range(1 + min(args.steps, 3)):
             v, _ = cpu_adam_sample()
@@ -663,9 +722,8 @@ def run_ours(args):
         out = {
             "metric": "batched props/s", "value": ws * nprop / (t_step * 1e-3), "unit": "props/s",
             "ms_per_step": t_step, "dtype": "f32",
-            "config": {"workload": "batch 96 fields, sizes U{512,1024,2048,4096}^2, ASM/Fresnel/ARSS (s=0.5), "
-                                   "z U[10,300]mm, lambda U{640,532,450}nm, p=8um; one persistent launch in a CUDA graph",
-                       "items": plan.n_items, "l2": "inputs larger than L2 (%.1f GB)" % (nbytes / 1e9)},
+            "config": {"workload": BATCH_DESC, "items": plan.n_items,
+                       "l2": "inputs larger than L2 (%.1f GB)" % (nbytes / 1e9)},
             "e2e": {"value": ws * nprop / (t_e2e * 1e-3), "unit": "props/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
             "gpu_launches": int(launches),
@@ -688,6 +746,74 @@ def run_ours(args):
             "clocks": clocks,
         }
         plan.close()
+        if rank == 0 and ws == 1 and not args.no_cpu:
+            v, t_cls = cpu_batch_sample()
+            out["cpu_baseline"] = {"value": v, "unit": "props/s", "cores": cpu_threads(), "kind": "port",
+                                   "sample": "one FP64 field per size class (%s s), each class costed for all its "
+                                             "fields" % ", ".join("%d^2 %.2f" % (m, t) for m, t in t_cls.items())}
+    elif args.workload == "tilt":
+        c = TILT
+        n = c["n"]
+        tuned = og.autotune(n, n)
+        u0 = asm_input()
+        src = torch.from_numpy(u0).cuda()
+        dst = torch.empty_like(src)
+        tws = og.tilted_workspace(n, n)
+        kw = dict(dy=c["p"], dx=c["p"], lam=c["lam"], z=c["z"], work=tws)
+
+        def run(interp, mode, refm):
+            ang = c["angle_ref"] if refm else c["angle"]
+            return lambda: og.tilted_prop(src, dst, angle=ang, interp=interp, propmode=mode, reference=refm, **kw)
+
+        step = run(0, 0, False)
+        with ClockSampler(local) as clk:
+            l0 = og.launch_count()
+            ms = timed(torch, step, K, W, flush, stream, barrier)
+            launches = (og.launch_count() - l0) // (K + W) * K
+            forms = {}
+            for refm in (False, True):
+                for mode in (0, 1):
+                    for interp in (0, 1):
+                        name = "%s_%s_%s" % ("reference" if refm else "source", "fresnel" if mode else "asm",
+                                             "bicubic" if interp else "bilinear")
+                        mf = timed(torch, run(interp, mode, refm), K, W, flush, stream, barrier)
+                        forms[name] = {"props/s": 1e3 / statistics.mean(mf), "ms": statistics.mean(mf)}
+            ms_asm = timed(torch, lambda: og.asm_prop(src, dst, dy=c["p"], dx=c["p"], lam=c["lam"], z=c["z"]),
+                           K, W, flush, stream, barrier)
+        clocks = clk.summary()
+        t_step = max_over_ranks(statistics.mean(ms))
+        hsrc = torch.from_numpy(u0).pin_memory()
+        hdst = torch.empty_like(hsrc).pin_memory()
+
+        def step_e2e():
+            src.copy_(hsrc, non_blocking=True)
+            step()
+            hdst.copy_(dst, non_blocking=True)
+
+        ms_e = timed(torch, step_e2e, K, W, flush, stream, barrier)
+        t_e2e = max_over_ranks(statistics.mean(ms_e))
+        # row pass 8n in + 16n out, column FFTs 16n + 32n, resample 32n + 32n,
+        # inverse columns 32n + 16n, inverse rows 16n + 8n
+        b_alg = 208 * n * n
+        ach = b_alg / (statistics.mean(ms) * 1e-3) / 1e9
+        forms["plain_asm_same_field"] = {"props/s": 1e3 / statistics.mean(ms_asm), "ms": statistics.mean(ms_asm)}
+        out = {
+            "metric": "tilted props/s", "value": ws / (t_step * 1e-3), "unit": "props/s", "ms_per_step": t_step,
+            "dtype": "f32 (FP64 sampling positions at the grid edges)",
+            "config": {"workload": TILT_DESC, "l2": "flushed between steps (256 MiB write)",
+                       "launch_variants": {f"{k}:{m}": v for (k, m), v in tuned.items()}},
+            "e2e": {"value": ws / (t_e2e * 1e-3), "unit": "props/s", "h2d_bytes_per_step": u0.nbytes,
+                    "d2h_bytes_per_step": u0.nbytes},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": ach / pk["hbm_gbs"], "traffic": None,
+                         "note": f"208 n bytes per tilted propagation (n = 1024^2); peak {pk_kind}"},
+            "forms": forms,
+            "clocks": clocks,
+        }
+        if rank == 0 and ws == 1 and not args.no_cpu:
+            out["cpu_baseline"] = {"value": cpu_tilt_sample(), "unit": "props/s", "cores": cpu_threads(),
+                                   "kind": "port", "sample": "one full 1024^2 FP64 TiltedSourceProp (ASM, bilinear)"}
 
     if rank == 0:
         line = {"metric": out["metric"], "value": out["value"], "unit": out["unit"], "n_gpus": ws, "steps": K,
@@ -708,7 +834,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cgh", choices=["cgh", "asm", "wrp", "adam", "batch"])
+    ap.add_argument("--workload", default="cgh", choices=["cgh", "asm", "wrp", "adam", "batch", "tilt"])
     ap.add_argument("--cpu-rows", type=int, default=48)
     ap.add_argument("--ref-rows", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")

@@ -1604,6 +1604,21 @@ extern "C" int olg_tilted_prop_c64(const void *u_in, void *u_out, int ny, int nx
     T.J0 = (float)a11;
     T.Jb = (float)(-a13);
     T.invN = (float)(1.0 / N);
+    {
+        // a11 - 1 = -2 sin^2(ang / 2), without cancellation
+        const double sh = std::sin(ang / 2);
+        set_quad(T.c1_hi, T.c1_lo, -2.0 * sh * sh);
+        const double K = reference ? a13 * f0 / du : 0.0;
+        const double Ki = std::nearbyint(K);
+        T.Ki = (int)Ki;
+        T.Kf = (float)(K - Ki);
+        T.a13f = (float)a13;
+        T.duf = (float)du;
+        T.dvf = (float)dv;
+        T.dv2du = (float)(dv * dv / du);
+        T.f0f = (float)f0;
+        T.f0sq = (float)(f0 * f0);
+    }
     T.Hx = TL.Hx; T.Hy = TL.Hy;
     T.C = TL.C; T.D = TL.D;
     PropParams &tf = T.tf;

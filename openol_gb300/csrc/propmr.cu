@@ -151,40 +151,84 @@ __device__ __forceinline__ float tilt_cubic(float d)
 }
 
 // One resampled sample per thread: output frequency (n, m) of the centred
-// grid, stored at its natural-order position in D.  The sampling position
-// (x, y) is formed in FP64 operation by operation as the reference forms it
-// (each rounding explicit, so that the cell and boundary decisions agree);
-// weights, Jacobian and products are FP32.
+// grid, stored at its natural-order position in D.
+//
+// Sampling position.  The reference forms x = fsx / du + NX/2 and y = fsy / dv
+// + NY/2 in double; the interpolation is continuous in (x, y) except where
+// the cell crosses the grid's edges (x or y near 0, N - 1 or N: inside /
+// nearest sample / outside), and in the bilinear rule's last column, whose
+// nearest sample takes row floor(y) as is.  So the position is formed in FP32 as
+//   x = NX/2 + m' + (a11 - 1) m' + K - a13 g / du,   g = f0 - fpz = (fpx^2 + fpy^2) / (f0 + fpz),
+// with (a11 - 1) m' split exactly into an integer and a fraction, and y = n
+// (the reference's y is n to within an ulp); near an x edge, on the first and
+// last rows and in that last column the coordinate is recomputed in FP64
+// operation by operation as the reference forms it (each rounding explicit),
+// so those cases are decided on the reference's numbers.
+// Weights, the Jacobian and all products are FP32.
+__device__ __forceinline__ double tilt_x_exact(const TiltArgs &T, double fpx, double fpy)
+{
+    const double fpz = __dsqrt_rn(__dsub_rn(__dsub_rn(T.fsqr, __dmul_rn(fpx, fpx)), __dmul_rn(fpy, fpy)));
+    double fsx = __dadd_rn(__dmul_rn(T.a11, fpx), __dmul_rn(T.a13, fpz));
+    if (!T.reference) fsx = __dsub_rn(fsx, T.a13f0);
+    return __dadd_rn(__ddiv_rn(fsx, T.du), (double)(T.NX / 2));
+}
+
 __global__ void __launch_bounds__(256) k_tilt_resample(TiltArgs T)
 {
     const int NX = T.NX, NY = T.NY;
     const int n = blockIdx.y, m = blockIdx.x * 256 + threadIdx.x;
     if (m >= NX) return;
-    const double fpy = __dmul_rn((double)(n - NY / 2), T.dv);
-    const double fpx = __dmul_rn((double)(m - NX / 2), T.du);
-    const double fpz = __dsqrt_rn(__dsub_rn(__dsub_rn(T.fsqr, __dmul_rn(fpx, fpx)), __dmul_rn(fpy, fpy)));
-    double fsx = __dadd_rn(__dmul_rn(T.a11, fpx), __dmul_rn(T.a13, fpz));
-    if (!T.reference) fsx = __dsub_rn(fsx, T.a13f0);
-    const double x = __dadd_rn(__ddiv_rn(fsx, T.du), (double)(NX / 2));
-    const double y = __dadd_rn(__ddiv_rn(fpy, T.dv), (double)(NY / 2));
-    const double xf = floor(x), yf = floor(y);
+    const int mp = m - NX / 2, np = n - NY / 2;
+    const float mpf = (float)mp, npf = (float)np;
+    const float fpxf = mpf * T.duf, fpyf = npf * T.dvf;
+    const float fpzf = sqrtf(T.f0sq - fpxf * fpxf - fpyf * fpyf);
+    // (a11 - 1) m' = I + F exactly enough: integer I, |F| <= 1/2
+    const float p = __fmul_rn(T.c1_hi, mpf);
+    const float e = __fmaf_rn(T.c1_hi, mpf, -p);
+    const float i1 = round_int(p);
+    const float t1 = (p - i1) + (e + T.c1_lo * mpf);
+    const float i2 = round_int(t1);
+    const float gdu = (mpf * mpf * T.duf + npf * npf * T.dv2du) / (T.f0f + fpzf);
+    int xi = NX / 2 + mp + T.Ki + (int)i1 + (int)i2;
+    float d = (t1 - i2) + T.Kf - T.a13f * gdu;
+    const float xa = (float)xi + d;
+    if (fabsf(xa) < 0.01f || fabsf(xa - (float)(NX - 1)) < 0.01f || fabsf(xa - (float)NX) < 0.01f) {
+        const double x = tilt_x_exact(T, __dmul_rn((double)mp, T.du), __dmul_rn((double)np, T.dv));
+        const double xf = floor(x);
+        if (!(xf >= -4.0 && xf <= (double)NX + 4.0)) {
+            xi = -8; // far outside: zero
+            d = 0.f;
+        } else {
+            xi = (int)xf;
+            d = (float)(x - xf);
+        }
+    }
+    const float fx = floorf(d);
+    const int ms = xi + (int)fx;
+    const float s = d - fx;
+    // y = n, except where its last bits decide a case: the first and last rows,
+    // and (bilinear) the last column, whose nearest-sample rule takes row floor(y)
+    int ns = n;
+    float t = 0.f;
+    if (n == 0 || n == NY - 1 || (T.interp == 0 && ms == NX - 1)) {
+        const double y = __dadd_rn(__ddiv_rn(__dmul_rn((double)np, T.dv), T.dv), (double)(NY / 2));
+        const double yf = floor(y);
+        ns = (int)yf;
+        t = (float)(y - yf);
+    }
     const float2 *C = T.C;
     float2 v = make_float2(0.f, 0.f);
     if (T.interp == 0) {
-        if (xf >= 0.0 && xf < (double)(NX - 1) && yf >= 0.0 && yf < (double)(NY - 1)) {
-            const int ms = (int)xf, ns = (int)yf;
-            const float s = (float)(x - xf), t = (float)(y - yf);
-            const float2 *p = C + (size_t)ns * NX + ms;
-            const float2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + NX), d = __ldg(p + NX + 1);
+        if (ms >= 0 && ms < NX - 1 && ns >= 0 && ns < NY - 1) {
+            const float2 *q = C + (size_t)ns * NX + ms;
+            const float2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + NX), dd = __ldg(q + NX + 1);
             const float2 u1 = make_float2((1.f - s) * a.x + s * b.x, (1.f - s) * a.y + s * b.y);
-            const float2 u2 = make_float2((1.f - s) * c.x + s * d.x, (1.f - s) * c.y + s * d.y);
+            const float2 u2 = make_float2((1.f - s) * c.x + s * dd.x, (1.f - s) * c.y + s * dd.y);
             v = make_float2((1.f - t) * u1.x + t * u2.x, (1.f - t) * u1.y + t * u2.y);
-        } else if (xf >= 0.0 && xf < (double)NX && yf >= 0.0 && yf < (double)NY) {
-            v = __ldg(C + (size_t)(int)yf * NX + (int)xf);
+        } else if (ms >= 0 && ms < NX && ns >= 0 && ns < NY) {
+            v = __ldg(C + (size_t)ns * NX + ms);
         }
-    } else if (xf >= 0.0 && xf < (double)NX && yf >= 0.0 && yf < (double)NY) {
-        const int ms = (int)xf, ns = (int)yf;
-        const float s = (float)(x - xf), t = (float)(y - yf);
+    } else if (ms >= 0 && ms < NX && ns >= 0 && ns < NY) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int nn = ns - 1 + j;
@@ -202,7 +246,7 @@ __global__ void __launch_bounds__(256) k_tilt_resample(TiltArgs T)
             }
         }
     }
-    const float J = T.J0 + T.Jb * (float)fpx / (float)fpz;
+    const float J = T.J0 + T.Jb * fpxf / fpzf;
     v = cscale(v, J);
     const int ky = n < NY / 2 ? n + NY / 2 : n - NY / 2, kx = m < NX / 2 ? m + NX / 2 : m - NX / 2;
     if (!T.reference) {
@@ -210,8 +254,9 @@ __global__ void __launch_bounds__(256) k_tilt_resample(TiltArgs T)
         if (T.fresnel) {
             H = cmul(__ldg(T.Hx + kx), __ldg(T.Hy + ky));
         } else {
-            // exp(2 pi i z w), w = sqrt(fsqr - (fpx + a13 f0)^2 - fpy^2), in cycles
-            const double uu = __dadd_rn(fpx, T.a13f0);
+            // exp(2 pi i z w), w = sqrt(fsqr - (fpx + a13 f0)^2 - fpy^2), in cycles (FP64)
+            const double fpy = __dmul_rn((double)np, T.dv);
+            const double uu = __dadd_rn(__dmul_rn((double)mp, T.du), T.a13f0);
             const double w = __dsqrt_rn(__dsub_rn(__dsub_rn(T.fsqr, __dmul_rn(uu, uu)), __dmul_rn(fpy, fpy)));
             const double cyc = w * T.z;
             H = cis_cycles((float)(cyc - rint(cyc)));

@@ -28,6 +28,12 @@ struct TiltArgs {
     int fresnel;                 // transfer function Hx[kx] Hy[ky] (else ASM)
     double du, dv, fsqr, a11, a13, a13f0, z;
     float J0, Jb, invN;
+    // FP32 form of the sampling position (see k_tilt_resample):
+    //   x = NX/2 + m' + round(c1 m') + Ki + [frac(c1 m') + Kf - a13 g / du],
+    //   c1 = a11 - 1 (split hi + lo), K = Ki + Kf = a13 f0 / du (reference form, else 0),
+    //   g / du = (m'^2 du + n'^2 dv^2 / du) / (f0 + fpz)
+    float c1_hi, c1_lo, Kf, a13f, duf, dvf, dv2du, f0f, f0sq;
+    int Ki;
     PropParams tf;               // reference form: tf_at() of the unrotated grid
     const float2 *Hx, *Hy;       // Fresnel spectra, natural order (Hx carries 1/N)
     float2 *C;                   // centred spectrum, NY x NX
