@@ -1618,6 +1618,11 @@ extern "C" int olg_tilted_prop_c64(const void *u_in, void *u_out, int ny, int nx
         T.dv2du = (float)(dv * dv / du);
         T.f0f = (float)f0;
         T.f0sq = (float)(f0 * f0);
+        set_quad(T.du_hi, T.du_lo, du);
+        set_quad(T.dv_hi, T.dv_lo, dv);
+        set_quad(T.c_hi, T.c_lo, a13 * f0);
+        set_quad(T.f0sq_hi, T.f0sq_lo, fsqr);
+        set_quad(T.z_hi, T.z_lo, z);
     }
     T.Hx = TL.Hx; T.Hy = TL.Hy;
     T.C = TL.C; T.D = TL.D;

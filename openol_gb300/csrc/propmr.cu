@@ -254,12 +254,15 @@ __global__ void __launch_bounds__(256) k_tilt_resample(TiltArgs T)
         if (T.fresnel) {
             H = cmul(__ldg(T.Hx + kx), __ldg(T.Hy + ky));
         } else {
-            // exp(2 pi i z w), w = sqrt(fsqr - (fpx + a13 f0)^2 - fpy^2), in cycles (FP64)
-            const double fpy = __dmul_rn((double)np, T.dv);
-            const double uu = __dadd_rn(__dmul_rn((double)mp, T.du), T.a13f0);
-            const double w = __dsqrt_rn(__dsub_rn(__dsub_rn(T.fsqr, __dmul_rn(uu, uu)), __dmul_rn(fpy, fpy)));
-            const double cyc = w * T.z;
-            H = cis_cycles((float)(cyc - rint(cyc)));
+            // exp(2 pi i z w), w = sqrt(f0^2 - (fpx + a13 f0)^2 - fpy^2), in double-float
+            // (~44 bits: z w ~ 1e5 cycles keeps ~1e-8 cycles; FP64 runs at a small
+            // fraction of the FP32 rate on this GPU)
+            const df2 u = df_add(df_mul(df2{T.du_hi, T.du_lo}, df2{mpf, 0.f}), df2{T.c_hi, T.c_lo});
+            const df2 v = df_mul(df2{T.dv_hi, T.dv_lo}, df2{npf, 0.f});
+            const df2 u2 = df_mul(u, u), v2 = df_mul(v, v);
+            const df2 w2 = df_add(df2{T.f0sq_hi, T.f0sq_lo}, df_add(df2{-u2.hi, -u2.lo}, df2{-v2.hi, -v2.lo}));
+            const df2 w = df_sqrt(w2);
+            H = cis_cycles(df_frac(df_mul(w, df2{T.z_hi, T.z_lo})));
         }
         v = cmul(v, H);
     }

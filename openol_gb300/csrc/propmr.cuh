@@ -34,6 +34,8 @@ struct TiltArgs {
     //   g / du = (m'^2 du + n'^2 dv^2 / du) / (f0 + fpz)
     float c1_hi, c1_lo, Kf, a13f, duf, dvf, dv2du, f0f, f0sq;
     int Ki;
+    // double-float constants of the source form's ASM phase z sqrt(f0^2 - (fpx + a13 f0)^2 - fpy^2)
+    float du_hi, du_lo, dv_hi, dv_lo, c_hi, c_lo, f0sq_hi, f0sq_lo, z_hi, z_lo;
     PropParams tf;               // reference form: tf_at() of the unrotated grid
     const float2 *Hx, *Hy;       // Fresnel spectra, natural order (Hx carries 1/N)
     float2 *C;                   // centred spectrum, NY x NX
