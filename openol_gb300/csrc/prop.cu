@@ -651,7 +651,10 @@ template <> struct ColVar<4> : Shape<256, 8192, 2, true> {};
 template <> struct ColVar<5> : Shape<512, 16384, 1, true> {};
 template <> struct ColVar<6> : Shape<128, 4096, 4, true> {};
 template <> struct ColVar<7> : Shape<64, 2048, 8, true> {};
-constexpr int N_COL_VARIANTS = 8;
+// register-capped shapes: two / four CTAs per SM for more resident warps
+template <> struct ColVar<8> : Shape<512, 8192, 2> {};
+template <> struct ColVar<9> : Shape<256, 4096, 4> {};
+constexpr int N_COL_VARIANTS = 10;
 
 template <int N, class V>
 struct RowShape {
@@ -925,6 +928,8 @@ bool col_variant_valid(int i)
     case 5: return ColShape<N, ColVar<5>>::valid;
     case 6: return ColShape<N, ColVar<6>>::valid;
     case 7: return ColShape<N, ColVar<7>>::valid;
+    case 8: return ColShape<N, ColVar<8>>::valid;
+    case 9: return ColShape<N, ColVar<9>>::valid;
     default: return false;
     }
 }
@@ -971,6 +976,8 @@ int launch_cols(const PropParams &P, cudaStream_t st)
         case 5: return launch_cols_v<N, 5>(P, st);
         case 6: return launch_cols_v<N, 6>(P, st);
         case 7: return launch_cols_v<N, 7>(P, st);
+        case 8: return launch_cols_v<N, 8>(P, st);
+        case 9: return launch_cols_v<N, 9>(P, st);
         default: return launch_cols_v<N, 0>(P, st);
         }
     } else {
