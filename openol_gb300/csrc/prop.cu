@@ -1524,6 +1524,21 @@ extern "C" int olg_split_prop_c64(const void *u_in, void *u_out, int ny, int nx,
 
 // ------------------------------------------------------------- tilted
 namespace olg {
+
+const float2 *twiddle_table()
+{
+    static const float2 *cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (!cache[dev]) {
+        if (ensure_twiddles() != OLG_OK) return nullptr;
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_tw) != cudaSuccess) return nullptr;
+        cache[dev] = (const float2 *)p;
+    }
+    return cache[dev];
+}
+
 namespace {
 
 struct TiltLayout {

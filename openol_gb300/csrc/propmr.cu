@@ -439,6 +439,13 @@ int mr_chirp_axis(const ChirpAxis &A, cudaStream_t st)
 
 int tilt_middle(const TiltArgs &T, cudaStream_t st)
 {
+    if (is_pow2(T.NY) && T.NY >= 256) {
+        if (int rc = tilt_cols_pow2(T, false, st)) return rc;
+        k_tilt_resample<<<dim3((T.NX + 255) / 256, T.NY), 256, 0, st>>>(T);
+        count_launch();
+        if (int rc = check_launch("k_tilt_resample")) return rc;
+        return tilt_cols_pow2(T, true, st);
+    }
     MrPlan pl;
     if (!mr_plan(T.NY, &pl) || mr_nseq(pl) < 1)
         return fail(OLG_ERR_UNSUPPORTED_SIZE, "height: 2 ny must be a power of two or 2^a 3^b 5^c <= 7680");

@@ -45,5 +45,10 @@ struct TiltArgs {
 // column FFTs of the row spectra (D) -> C, resampling C -> D, inverse column
 // FFTs D -> D's first ny rows (x 1/N)
 int tilt_middle(const TiltArgs &T, cudaStream_t st);
+// tuned column FFTs of the tilted path for power-of-two heights 256..8192 (tilt.cu)
+int tilt_cols_pow2(const TiltArgs &T, bool inverse, cudaStream_t st);
+// device address of the FFT_MAX-point twiddle table of the tuned passes
+// (prop.cu; uploaded on first use on this device), or nullptr
+const float2 *twiddle_table();
 
 } // namespace olg

@@ -12,7 +12,7 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("shape", [(128, 256), (512, 512), (2048, 1024)])
+@pytest.mark.parametrize("shape", [(128, 256), (512, 512), (2048, 1024), (64, 4096), (4096, 64)])
 def test_every_launch_variant_matches_oracle(shape):
     ny, nx = shape
     rng = np.random.default_rng(ny + nx)
@@ -20,7 +20,8 @@ def test_every_launch_variant_matches_oracle(shape):
     uc = u0.astype(np.complex128)
     ref_asm = O.asm_prop(uc, 6e-6, 8e-6, 532e-9, 0.04)
     ref_arss = O.arss_prop(uc, 6e-6, 8e-6, 532e-9, 0.04, 0.5, 1e-4, -2e-4)
-    lens = {0: 2 * nx, 1: 2 * ny, 2: 2 * nx}
+    # lengths below 256 have one fixed launch shape (no variants)
+    lens = {k: n for k, n in {0: 2 * nx, 1: 2 * ny, 2: 2 * nx}.items() if n >= 256}
     tried = 0
     try:
         for kind, n in lens.items():
@@ -41,7 +42,7 @@ def test_every_launch_variant_matches_oracle(shape):
     finally:
         for kind, n in lens.items():
             og.set_variant(kind, n, 0)
-    assert tried >= 6
+    assert tried >= 2 * len(lens)
 
 
 def test_autotune_keeps_a_valid_variant():
