@@ -633,7 +633,13 @@ def run_ours(args):
 
         ms_e = timed(torch, step_e2e, K, W, flush, stream, barrier)
         t_e2e = max_over_ranks(statistics.mean(ms_e))
-        b_alg = 1316 * n * n
+        # bytes of the shared-spectrum gradient (n = 2048^2 elements, P planes):
+        # e^{i phi} row pass 20 n + forward column pass to the full spectrum 48 n;
+        # per plane: inverse column pass 48 n, seed row pass 28 n, its forward row
+        # pass 24 n, forward column pass into the summed spectrum 80 n (48 n for
+        # the first); the final inverse column + row passes 72 n; Adam 32 n
+        P = len(zs)
+        b_alg = (68 + 100 * P + 80 * P - 32 + 72 + 32) * n * n
         ach = b_alg / (statistics.mean(ms) * 1e-3) / 1e9
         out = {
             "metric": "grad-steps/s", "value": ws / (t_step * 1e-3), "unit": "grad-steps/s", "ms_per_step": t_step,
@@ -645,8 +651,9 @@ def run_ours(args):
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                          "frac": ach / pk["hbm_gbs"], "traffic": None,
-                         "note": f"1316 n bytes per step (16 propagations x 80 n + elementwise), n = 2048^2; "
-                                 f"peak {pk_kind}"},
+                         "note": f"{b_alg // (n * n)} n bytes per step (one shared forward spectrum, per plane an "
+                                 f"inverse column pass, two row passes and a forward column pass into the summed "
+                                 f"adjoint spectrum; Adam), n = 2048^2; peak {pk_kind}"},
             "forms": {"fused_adjoint": {"grad-steps/s": 1e3 / statistics.mean(ms), "ms": statistics.mean(ms)},
                       "plain_torch_autograd_cufft": {"grad-steps/s": 1e3 / statistics.mean(ms_plain),
                                                       "ms": statistics.mean(ms_plain)},

@@ -2210,11 +2210,13 @@ extern "C" int olg_batch_plan_destroy(olg_batch_plan plan)
 
 // ------------------------------------------- multi-plane phase optimisation
 // Phase-only hologram phi (ny x nx) propagated by ASM to P depth planes;
-// loss L = sum_p mean((|A_p e^{i phi}|^2 - t_p)^2).  Per plane: one forward
-// propagation whose pass 1 forms e^{i phi} from phi and whose pass 3 writes
-// the seed dL/dv* = (2/n)(|v|^2 - t) v (and sums the loss), then one adjoint
-// propagation (conjugate transfer function) of the seed accumulated into
-// g = dL/du*.  No plane's field is stored.  dL/dphi = -2 Im(u conj(g)).
+// loss L = sum_p mean((|A_p e^{i phi}|^2 - t_p)^2).  Per plane: the forward
+// propagation, whose pass 3 writes the seed dL/dv* = (2/n)(|v|^2 - t) v (and
+// sums the loss), then the adjoint propagation (conjugate transfer function)
+// of the seed, accumulated into g = dL/du*.  No plane's field is stored.
+// dL/dphi = -2 Im(u conj(g)).  For padded heights 256..8192 the planes share
+// the forward spectrum of e^{i phi} and sum their adjoint spectra (spec.cu);
+// otherwise each plane runs two full three-pass propagations.
 namespace olg {
 
 __global__ void k_phase_grad(const float *phi, const float2 *g, float *grad, long n)
@@ -2271,14 +2273,16 @@ PropParams asm_params(const void *in, void *out, int ny, int nx, double dy, doub
     return P;
 }
 
-size_t phase_ws(int ny, int nx, size_t *off_seed, size_t *off_g, size_t *off_loss)
+// [propagation layout][seed][g][loss][F0: NY x NX][G: NY x NX]
+size_t phase_ws(int ny, int nx, size_t *off_seed, size_t *off_g, size_t *off_loss, size_t *off_spec = nullptr)
 {
     const size_t lb = layout_bytes(ny, nx, nullptr, nullptr);
     const size_t f = align_up((size_t)ny * nx * sizeof(float2), 256);
     if (off_seed) *off_seed = lb;
     if (off_g) *off_g = lb + f;
     if (off_loss) *off_loss = lb + 2 * f;
-    return lb + 2 * f + 256;
+    if (off_spec) *off_spec = lb + 2 * f + 256;
+    return lb + 2 * f + 256 + 2 * 4 * f;
 }
 
 int phase_loss_grad(const float *phi, const float *targets, const double *z, int np, int ny, int nx, double dy,
@@ -2292,6 +2296,45 @@ int phase_loss_grad(const float *phi, const float *targets, const double *z, int
     const long n = (long)ny * nx;
     cudaError_t e = cudaMemsetAsync(loss, 0, sizeof(double), st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(loss)");
+    if (spec_cols_ok(2 * ny)) {
+        // Every plane's forward propagation starts from the same e^{i phi}: its
+        // padded spectrum F0 is formed once.  The adjoints are linear in their
+        // seeds, so their conjugate-transfer-function spectra add into G and
+        // one inverse transform gives g.  Per plane this leaves one inverse
+        // and one forward column transform and two row passes.
+        size_t ospec;
+        phase_ws(ny, nx, nullptr, nullptr, nullptr, &ospec);
+        float2 *F0 = (float2 *)(ws + ospec);
+        float2 *G = F0 + (size_t)4 * n;
+        SpecArgs A{};
+        A.ny = ny; A.NY = 2 * ny; A.NX = 2 * nx;
+        PropParams R = asm_params(nullptr, nullptr, ny, nx, dy, dx, lambda, z[0], false, L);
+        R.in_phase = phi;
+        if (int rc = rows_pass(R, false, st)) return rc;
+        A.in = L.S; A.out = F0; A.tf = 0; A.accumulate = 0;
+        if (int rc = spec_cols(A, false, st)) return rc;
+        for (int p = 0; p < np; ++p) {
+            PropParams F = asm_params(nullptr, seed, ny, nx, dy, dx, lambda, z[p], false, L);
+            F.post_mode = OP_SEED;
+            F.target = targets + (size_t)p * n;
+            F.seed_scale = (float)(2.0 / (double)n);
+            F.loss = loss;
+            A.in = F0; A.out = L.S; A.tf = 1; A.accumulate = 0; A.P = F;
+            if (int rc = spec_cols(A, true, st)) return rc;
+            if (int rc = rows_pass(F, true, st)) return rc;
+            PropParams B = asm_params(seed, nullptr, ny, nx, dy, dx, lambda, z[p], true, L);
+            if (int rc = rows_pass(B, false, st)) return rc;
+            A.in = L.S; A.out = G; A.tf = 1; A.accumulate = p > 0 ? 1 : 0; A.P = B;
+            if (int rc = spec_cols(A, false, st)) return rc;
+        }
+        A.in = G; A.out = L.S; A.tf = 0; A.accumulate = 0;
+        if (int rc = spec_cols(A, true, st)) return rc;
+        PropParams Gp = asm_params(nullptr, g, ny, nx, dy, dx, lambda, z[0], false, L);
+        if (int rc = rows_pass(Gp, true, st)) return rc;
+        k_loss_scale<<<1, 1, 0, st>>>(loss, 1.0 / (double)n);
+        count_launch();
+        return check_launch("k_loss_scale");
+    }
     for (int p = 0; p < np; ++p) {
         PropParams F = asm_params(nullptr, seed, ny, nx, dy, dx, lambda, z[p], false, L);
         F.in_phase = phi;

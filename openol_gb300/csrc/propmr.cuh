@@ -47,6 +47,19 @@ struct TiltArgs {
 int tilt_middle(const TiltArgs &T, cudaStream_t st);
 // tuned column FFTs of the tilted path for power-of-two heights 256..8192 (tilt.cu)
 int tilt_cols_pow2(const TiltArgs &T, bool inverse, cudaStream_t st);
+// Column FFTs between a half-padded row spectrum (ny x NX) and a full padded
+// spectrum (NY x NX elements, stored by column tiles; private to spec.cu)
+// (spec.cu).  Forward: out = FFT_col(in) [x T] [+ out]; inverse:
+// out = central ny rows of IFFT_col(in [x T]).  T = tf_at(P) when tf != 0.
+struct SpecArgs {
+    int ny, NY, NX;
+    const float2 *in;
+    float2 *out;
+    int tf, accumulate;
+    PropParams P;
+};
+bool spec_cols_ok(int NY);
+int spec_cols(const SpecArgs &A, bool inverse, cudaStream_t st);
 // device address of the FFT_MAX-point twiddle table of the tuned passes
 // (prop.cu; uploaded on first use on this device), or nullptr
 const float2 *twiddle_table();
