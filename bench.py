@@ -635,11 +635,12 @@ def run_ours(args):
         t_e2e = max_over_ranks(statistics.mean(ms_e))
         # bytes of the shared-spectrum gradient (n = 2048^2 elements, P planes):
         # e^{i phi} row pass 20 n + forward column pass to the full spectrum 48 n;
-        # per plane: inverse column pass 48 n, seed row pass 28 n, its forward row
-        # pass 24 n, forward column pass into the summed spectrum 80 n (48 n for
-        # the first); the final inverse column + row passes 72 n; Adam 32 n
+        # per plane: inverse column pass 48 n, the fused seed row pass (row
+        # spectrum in and out, targets) 36 n, forward column pass into the summed
+        # spectrum 80 n (48 n for the first); the final inverse column + row
+        # passes 72 n; Adam 32 n
         P = len(zs)
-        b_alg = (68 + 100 * P + 80 * P - 32 + 72 + 32) * n * n
+        b_alg = (68 + 84 * P + 80 * P - 32 + 72 + 32) * n * n
         ach = b_alg / (statistics.mean(ms) * 1e-3) / 1e9
         out = {
             "metric": "grad-steps/s", "value": ws / (t_step * 1e-3), "unit": "grad-steps/s", "ms_per_step": t_step,
@@ -652,8 +653,8 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                          "frac": ach / pk["hbm_gbs"], "traffic": None,
                          "note": f"{b_alg // (n * n)} n bytes per step (one shared forward spectrum, per plane an "
-                                 f"inverse column pass, two row passes and a forward column pass into the summed "
-                                 f"adjoint spectrum; Adam), n = 2048^2; peak {pk_kind}"},
+                                 f"inverse column pass, the fused seed row pass and a forward column pass into the "
+                                 f"summed adjoint spectrum; Adam), n = 2048^2; peak {pk_kind}"},
             "forms": {"fused_adjoint": {"grad-steps/s": 1e3 / statistics.mean(ms), "ms": statistics.mean(ms)},
                       "plain_torch_autograd_cufft": {"grad-steps/s": 1e3 / statistics.mean(ms_plain),
                                                       "ms": statistics.mean(ms_plain)},

@@ -452,6 +452,97 @@ __device__ __forceinline__ void rows_inv_body_persist(const PropParams &P, float
     }
 }
 
+// ======================================================= seed round trip
+// The multi-plane gradient's forward pass 3 and adjoint pass 1 in one pass:
+// per row, the inverse row FFT of S, the crop, the seed (2/n)(|v|^2 - t) v
+// and the loss (OP_SEED), then the zero-padded forward row FFT of the seed
+// back into the same row of S.  The thread that ends the inverse transform
+// with the central outputs w = j + (k - 4) B (k = 4..11) is the one that
+// starts the forward transform from inputs j + r B (r = 4..11): the seed
+// stays in its registers.
+template <int N, int NT, int NSEQ>
+__device__ __forceinline__ void rows_seed_body(const PropParams &P, int r0, float2 *sm, int tid, float &lsum)
+{
+    constexpr int SS = padded_len(N), B = N / 16;
+    constexpr int BPT = NSEQ * B / NT;
+    float2 u[BPT][16];
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
+        float2 v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r)
+            v[r] = h < P.ny ? __ldcg(P.S + (size_t)h * N + j + r * B) : make_float2(0.f, 0.f);
+        dft<16, +1>(v);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+    }
+    __syncthreads();
+    mid_stages<N, +1, NT, false, NSEQ>(sm, SS, g_tw, tid);
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
+        float2 v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+        last_twiddle<N, +1>(v, j, g_tw);
+        dft16_out_mid<+1>(v);
+#pragma unroll
+        for (int k = 4; k < 12; ++k) {
+            float2 a = v[outpos<16>(k)];
+            if (h < P.ny) {
+                const float r2 = a.x * a.x + a.y * a.y - __ldg(P.target + (size_t)h * P.nx + j + (k - 4) * B);
+                lsum = fmaf(r2, r2, lsum);
+                a = cscale(a, P.seed_scale * r2);
+            } else {
+                a = make_float2(0.f, 0.f);
+            }
+            u[t][k] = a;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B;
+        dft16_in_mid<-1>(u[t]);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = u[t][outpos<16>(k)];
+    }
+    __syncthreads();
+    mid_stages<N, -1, NT, false, NSEQ>(sm, SS, g_tw, tid);
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
+        float2 v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+        last_twiddle<N, -1>(v, j, g_tw);
+        dft<16, -1>(v);
+        if (h < P.ny) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) __stcg(P.S + (size_t)h * N + j + k * B, v[outpos<16>(k)]);
+        }
+    }
+}
+
+// one shape for every length: 256 threads, 4096 elements (NSEQ rows) per CTA
+template <int N>
+struct SeedCfg {
+    static constexpr int NT = 256, NSEQ = N >= 4096 ? 1 : 4096 / N;
+    static constexpr int SMEM = NSEQ * padded_len(N) * 8;
+};
+
+template <int N>
+__global__ void __launch_bounds__(256) k_rows_seed(PropParams P)
+{
+    pdl_enter();
+    extern __shared__ float2 sm[];
+    using C = SeedCfg<N>;
+    float lsum = 0.f;
+    rows_seed_body<N, C::NT, C::NSEQ>(P, blockIdx.x * C::NSEQ, sm, threadIdx.x, lsum);
+    loss_reduce(lsum, P.loss, threadIdx.x, C::NT);
+}
+
 // ======================================================= paired passes
 // Two rows (passes 1 and 3) or two adjacent columns (pass 2) per butterfly,
 // in planar pairs on the paired FP32 pipe (fftp.cuh).  Same stages, pruning
@@ -985,6 +1076,29 @@ int launch_cols(const PropParams &P, cudaStream_t st)
         const int grid = (P.NX + C::C - 1) / C::C;
         if (int rc = prep_smem(k_cols<N>, C::SMEM)) return rc;
         return launch_pdl(k_cols<N>, grid, C::NT, C::SMEM, st, P, "k_cols");
+    }
+}
+
+template <int N>
+int launch_rows_seed(const PropParams &P, cudaStream_t st)
+{
+    using C = SeedCfg<N>;
+    if (int rc = prep_smem(k_rows_seed<N>, C::SMEM)) return rc;
+    return launch_pdl(k_rows_seed<N>, (P.ny + C::NSEQ - 1) / C::NSEQ, C::NT, C::SMEM, st, P, "k_rows_seed");
+}
+
+// forward pass 3 (OP_SEED) and adjoint pass 1 of one plane, fused; padded
+// widths 256..8192 (the first and last radix-16 stages need N >= 256)
+int rows_seed_pass(const PropParams &P, cudaStream_t st)
+{
+    switch (P.NX) {
+    case 256: return launch_rows_seed<256>(P, st);
+    case 512: return launch_rows_seed<512>(P, st);
+    case 1024: return launch_rows_seed<1024>(P, st);
+    case 2048: return launch_rows_seed<2048>(P, st);
+    case 4096: return launch_rows_seed<4096>(P, st);
+    case 8192: return launch_rows_seed<8192>(P, st);
+    default: return fail(OLG_ERR_UNSUPPORTED_SIZE, "fused seed pass: padded width 256..8192");
     }
 }
 
@@ -2321,9 +2435,15 @@ int phase_loss_grad(const float *phi, const float *targets, const double *z, int
             F.loss = loss;
             A.in = F0; A.out = L.S; A.tf = 1; A.accumulate = 0; A.P = F;
             if (int rc = spec_cols(A, true, st)) return rc;
-            if (int rc = rows_pass(F, true, st)) return rc;
             PropParams B = asm_params(seed, nullptr, ny, nx, dy, dx, lambda, z[p], true, L);
-            if (int rc = rows_pass(B, false, st)) return rc;
+            if (2 * nx >= 256) {
+                // the seed goes from the forward's inverse row FFT to the
+                // adjoint's forward row FFT in registers
+                if (int rc = rows_seed_pass(F, st)) return rc;
+            } else {
+                if (int rc = rows_pass(F, true, st)) return rc;
+                if (int rc = rows_pass(B, false, st)) return rc;
+            }
             A.in = L.S; A.out = G; A.tf = 1; A.accumulate = p > 0 ? 1 : 0; A.P = B;
             if (int rc = spec_cols(A, false, st)) return rc;
         }
