@@ -246,7 +246,10 @@ int olg_batch_plan_destroy(olg_batch_plan plan);
  * targets: n_planes x ny x nx float intensities; z: n_planes host doubles.
  * Loss L = sum_p mean((|ASM_{z_p}(e^{i phi})|^2 - t_p)^2).  The gradient is
  * formed with the hand-written adjoint (conjugate transfer function), each
- * plane's field recomputed rather than stored: 2 propagations per plane.
+ * plane's field recomputed rather than stored.  For padded heights
+ * 256..8192 the planes share the forward spectrum of e^{i phi} and sum
+ * their adjoint spectra: per plane one inverse and one forward column
+ * transform and one row pass; otherwise 2 propagations per plane.
  * loss (nullable) is a device double receiving L. */
 size_t olg_phase_opt_workspace_bytes(int ny, int nx);
 int olg_phase_loss_grad(const float *phi, const float *targets, const double *z, int n_planes, int ny, int nx,

@@ -2,9 +2,11 @@
 
 phi (ny x nx, float32 radians) is propagated by ASM to P depth planes; the
 loss is sum_p mean((|A_p e^{i phi}|^2 - t_p)^2).  Gradients come from
-olg_phase_loss_grad / olg_phase_adam_step: per plane one forward propagation
-(fused e^{i phi} input and loss seed epilogue) and one adjoint propagation
-accumulated into dL/du*, no stored per-plane fields.
+olg_phase_loss_grad / olg_phase_adam_step, with no stored per-plane fields:
+the planes share one forward spectrum of e^{i phi}; per plane an inverse
+column transform, one row pass that forms the loss, the seed and the seed's
+row transform, and a forward column transform summed into the adjoint
+spectrum; one inverse transform of that sum gives dL/du*.
 """
 from __future__ import annotations
 
