@@ -29,6 +29,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <mutex>
 
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
 namespace {
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-double g_tail_weight = 1.2;
+std::atomic<double> g_tail_weight{1.2};
 std::mutex g_encode_mu;
 int *g_err_flag[64] = {};
 
@@ -391,13 +392,19 @@ int get_encode()
 int err_flag(int **out)
 {
     int dev = 0;
-    cudaGetDevice(&dev);
+    if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return fail(OLG_ERR_INVALID_ARG, "device index out of range");
     std::lock_guard<std::mutex> lk(g_encode_mu);
     if (!g_err_flag[dev]) {
-        cudaError_t e = cudaMalloc(&g_err_flag[dev], sizeof(int));
+        int *f = nullptr;
+        cudaError_t e = cudaMalloc(&f, sizeof(int));
         if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (error flag)");
-        e = cudaMemset(g_err_flag[dev], 0, sizeof(int));
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMemset (error flag)");
+        e = cudaMemset(f, 0, sizeof(int));
+        if (e != cudaSuccess) {
+            cudaFree(f);
+            return cuda_fail(e, "cudaMemset (error flag)");
+        }
+        g_err_flag[dev] = f;
     }
     *out = g_err_flag[dev];
     return OLG_OK;
@@ -492,17 +499,24 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
     P.tiles = (int)tiles;
     P.U = (float2 *)U;
     P.err = err;
-    static bool attr_done[64] = {};
-    static int sm_count[64] = {};
+    // per device, once: the shared-memory opt-in and the SM count
+    static std::atomic<int> sm_count[64];
     int dev = 0;
-    cudaGetDevice(&dev);
-    if (!attr_done[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k_cgh_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm)");
-        e = cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(SM count)");
-        attr_done[dev] = true;
+    if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return fail(OLG_ERR_INVALID_ARG, "device index out of range");
+    if (!sm_count[dev]) {
+        std::lock_guard<std::mutex> lk(g_encode_mu);
+        if (!sm_count[dev]) {
+            cudaError_t e = cudaFuncSetAttribute(k_cgh_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm)");
+            int n = 0;
+            e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(SM count)");
+            sm_count[dev] = n;
+        }
     }
+    const int nsm = sm_count[dev];
+    const double tw = g_tail_weight.load(std::memory_order_relaxed);
     // SMs left over after one CTA per tile (one CTA per SM: ~197 KB of shared
     // memory) take the K tails: with e extra CTAs each holds `per` tails.  A
     // tail K block costs g_tail_weight tile K blocks (its operands are not
@@ -511,10 +525,10 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
     const int total = 3 * P.kblocks;
     P.split = total;
     P.extra = 0;
-    if (tiles < sm_count[dev] && g_tail_weight > 0.0) {
-        const int e = sm_count[dev] - (int)tiles;
+    if (tiles < nsm && tw > 0.0) {
+        const int e = nsm - (int)tiles;
         const int per = ((int)tiles + e - 1) / e;
-        const double pw = per * g_tail_weight;
+        const double pw = per * tw;
         const int split = (int)((double)total * pw / (pw + 1.0));
         if (split > 0 && split < total) {
             P.split = split;
@@ -533,9 +547,8 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
 
 extern "C" double olg_cgh_gemm_tail_weight(double w)
 {
-    const double old = g_tail_weight;
-    if (w >= 0.0 && w <= 16.0) g_tail_weight = w;
-    return old;
+    if (w >= 0.0 && w <= 16.0) return g_tail_weight.exchange(w);
+    return g_tail_weight.load();
 }
 
 extern "C" int olg_device_fault_check(int clear)

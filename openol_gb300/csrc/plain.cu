@@ -144,7 +144,7 @@ std::map<std::pair<int, std::pair<int, int>>, Plan> g_plans;
 int get_plan(int ny, int nx, Plan **out)
 {
     int dev = 0;
-    cudaGetDevice(&dev);
+    if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     std::lock_guard<std::mutex> lk(g_mu);
     auto key = std::make_pair(dev, std::make_pair(ny, nx));
     auto it = g_plans.find(key);
@@ -154,7 +154,11 @@ int get_plan(int ny, int nx, Plan **out)
         const size_t bytes = (size_t)4 * ny * nx * sizeof(float2);
         cudaError_t e = cudaMalloc(&p.b1, bytes);
         if (e == cudaSuccess) e = cudaMalloc(&p.b2, bytes);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (plain buffers)");
+        if (e != cudaSuccess) {
+            cudaFree(p.b1);
+            cufftDestroy(p.h);
+            return cuda_fail(e, "cudaMalloc (plain buffers)");
+        }
         it = g_plans.emplace(key, p).first;
     }
     *out = &it->second;

@@ -24,6 +24,7 @@
 // two 1-D FFTs, which k_chirp computes per call (exactly the DFT of the sampled
 // response the reference builds, golprop.h:184-187, olprop.h:133-137).
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <vector>
 #include <cmath>
@@ -930,13 +931,14 @@ int launch_pdl(void (*kern)(Arg), int grid, int block, int smem, cudaStream_t st
     return check_launch(what);
 }
 
-// selected variant per FFT length (index log2 N) and pass kind (0 rows fwd, 1 cols, 2 rows inv)
-int g_variant[3][14] = {};
+// selected variant per FFT length (index log2 N) and pass kind (0 rows fwd, 1 cols, 2 rows inv);
+// atomic so that a set or an autotune on one host thread races no launch on another
+std::atomic<int> g_variant[3][14];
 
 // SMs of the current device (cached per device; 152 on GB300)
 int sm_count()
 {
-    static int cache[64] = {};
+    static std::atomic<int> cache[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
     if (!cache[dev]) {
@@ -1641,7 +1643,7 @@ namespace olg {
 
 const float2 *twiddle_table()
 {
-    static const float2 *cache[64] = {};
+    static std::atomic<const float2 *> cache[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
     if (!cache[dev]) {

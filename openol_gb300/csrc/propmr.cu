@@ -311,7 +311,10 @@ int mr_table(int N, const float2 **out)
         e = cudaMalloc(&d, sizeof(float2) * N);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (twiddle table)");
         e = cudaMemcpy(d, t.data(), sizeof(float2) * N, cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) return cuda_fail(e, "twiddle table upload");
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            return cuda_fail(e, "twiddle table upload");
+        }
         it = g_mr_tw.emplace(std::make_pair(dev, N), d).first;
     }
     *out = it->second;
