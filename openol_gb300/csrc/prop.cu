@@ -1861,9 +1861,17 @@ extern "C" int olg_autotune_prop(int ny, int nx, int reps, olg_stream_t stream)
     layout_bytes(ny, nx, &L, (char *)sc.ptr);
     PropSetup S;
     if (int rc = setup_asm(buf.ptr, buf.ptr, ny, nx, 8e-6, 8e-6, 532e-9, 0.05, 0, L, &S)) return rc;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    // events released on every return path
+    struct Events {
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~Events()
+        {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } ev;
+    if ((e = cudaEventCreate(&ev.a)) != cudaSuccess || (e = cudaEventCreate(&ev.b)) != cudaSuccess)
+        return cuda_fail(e, "cudaEventCreate");
     // Coordinate descent over the three passes, timing whole propagations:
     // a pass's speed depends on its neighbours (L2 contents, dependent-launch
     // overlap), so passes are not timed alone.
@@ -1879,15 +1887,15 @@ extern "C" int olg_autotune_prop(int ny, int nx, int reps, olg_stream_t stream)
         int rc = run_passes(S.P, st);
         *ms = 0.f;
         for (int r = 0; r < reps && !rc; ++r) {
-            const cudaError_t fe = cudaMemsetAsync(flush.ptr, r & 0xff, flush_bytes, st);
-            if (fe != cudaSuccess) return cuda_fail(fe, "cudaMemsetAsync (L2 flush)");
-            cudaEventRecord(e0, st);
+            cudaError_t te = cudaMemsetAsync(flush.ptr, r & 0xff, flush_bytes, st);
+            if (te != cudaSuccess) return cuda_fail(te, "cudaMemsetAsync (L2 flush)");
+            if ((te = cudaEventRecord(ev.a, st)) != cudaSuccess) return cuda_fail(te, "cudaEventRecord");
             rc = run_passes(S.P, st);
-            cudaEventRecord(e1, st);
             if (rc) break;
-            cudaEventSynchronize(e1);
+            if ((te = cudaEventRecord(ev.b, st)) != cudaSuccess) return cuda_fail(te, "cudaEventRecord");
+            if ((te = cudaEventSynchronize(ev.b)) != cudaSuccess) return cuda_fail(te, "cudaEventSynchronize");
             float t = 0.f;
-            cudaEventElapsedTime(&t, e0, e1);
+            if ((te = cudaEventElapsedTime(&t, ev.a, ev.b)) != cudaSuccess) return cuda_fail(te, "cudaEventElapsedTime");
             *ms += t;
         }
         return rc;
@@ -1902,8 +1910,7 @@ extern "C" int olg_autotune_prop(int ny, int nx, int reps, olg_stream_t stream)
                 g_variant[kind][ln] = i;
                 float ms = 0.f;
                 if (int rc = time_prop(&ms)) {
-                    cudaEventDestroy(e0);
-                    cudaEventDestroy(e1);
+                    g_variant[kind][ln] = best_i; // keep the last good choice
                     return rc;
                 }
                 if (ms < best) {
@@ -1914,8 +1921,6 @@ extern "C" int olg_autotune_prop(int ny, int nx, int reps, olg_stream_t stream)
             g_variant[kind][ln] = best_i;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     return OLG_OK;
 }
 
@@ -2157,10 +2162,12 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
             return fail(OLG_ERR_UNSUPPORTED_SIZE, "batched fields must be powers of two in [256, 4096]");
     }
     if (int rc = ensure_twiddles()) return rc;
+    int dev = 0;
+    if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     auto *plan = new olg_batch_plan_s();
     plan->n = n_fields;
     plan->fields.assign(fields, fields + n_fields);
-    cudaGetDevice(&plan->dev);
+    plan->dev = dev;
     // device memory: [PropParams x n][ChirpAxis jobs][items][done 3n][target 3n][head, err][per-field scratch]
     std::vector<PropSetup> setups(n_fields);
     std::vector<ChirpAxis> jobs;
@@ -2264,9 +2271,7 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
     plan->D.err = C + 6 * n_fields + 1;
     plan->counters_off = offC;
     plan->counters_bytes = sizeof(int) * 3 * n_fields;
-    int nsm = 0;
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, plan->dev);
-    plan->grid = (nsm > 0 ? nsm : 1) * BATCH_CTAS_PER_SM;
+    plan->grid = sm_count() * BATCH_CTAS_PER_SM;
     e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, BATCH_SMEM);
     if (e != cudaSuccess) {
         cudaFree(plan->mem);
