@@ -38,6 +38,43 @@ __device__ __forceinline__ float2 mul_di(float2 a)
     return DIR < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
 }
 
+// v[r] *= w^r for r = 1 .. R-1 with w = table[m] (conjugated for DIR > 0).
+// Only w, w^2, w^4 and w^8 are read from the table; the other powers are
+// products of those, at most three roundings deep (~2e-7 relative).  Four
+// loads in flight instead of R - 1 keep ~20 fewer registers live across the
+// butterfly.  Needs (R - 1) m < FFT_MAX, as the direct lookups do.
+template <int R, int DIR>
+__device__ __forceinline__ void twiddle_powers(float2 (&v)[R], const float2 *__restrict__ table, int m)
+{
+    static_assert(R == 2 || R == 4 || R == 8 || R == 16, "radix 2, 4, 8 or 16");
+    const float2 w1 = twid<DIR>(table, m);
+    v[1] = cmul(v[1], w1);
+    if constexpr (R >= 4) {
+        const float2 w2 = twid<DIR>(table, 2 * m), w3 = cmul(w2, w1);
+        v[2] = cmul(v[2], w2);
+        v[3] = cmul(v[3], w3);
+        if constexpr (R >= 8) {
+            const float2 w4 = twid<DIR>(table, 4 * m);
+            const float2 w5 = cmul(w4, w1), w6 = cmul(w4, w2), w7 = cmul(w4, w3);
+            v[4] = cmul(v[4], w4);
+            v[5] = cmul(v[5], w5);
+            v[6] = cmul(v[6], w6);
+            v[7] = cmul(v[7], w7);
+            if constexpr (R == 16) {
+                const float2 w8 = twid<DIR>(table, 8 * m);
+                v[8] = cmul(v[8], w8);
+                v[9] = cmul(cmul(v[9], w8), w1);
+                v[10] = cmul(cmul(v[10], w8), w2);
+                v[11] = cmul(cmul(v[11], w8), w3);
+                v[12] = cmul(cmul(v[12], w8), w4);
+                v[13] = cmul(cmul(v[13], w8), w5);
+                v[14] = cmul(cmul(v[14], w8), w6);
+                v[15] = cmul(cmul(v[15], w8), w7);
+            }
+        }
+    }
+}
+
 template <int DIR>
 __device__ __forceinline__ void dft4(float2 &a, float2 &b, float2 &c, float2 &d)
 {
@@ -144,8 +181,7 @@ __device__ __forceinline__ void fft_stage(float2 *s, int ss, const float2 *__res
         if constexpr (NS > 1) {
             const int k = j & (NS - 1);
             constexpr int STEP = FFT_MAX / (NS * R);
-#pragma unroll
-            for (int r = 1; r < R; ++r) v[t][r] = cmul(v[t][r], twid<DIR>(tw, r * k * STEP));
+            twiddle_powers<R, DIR>(v[t], tw, k * STEP);
         }
         dft<R, DIR>(v[t]);
     }

@@ -75,8 +75,7 @@ template <int N, int DIR>
 __device__ __forceinline__ void last_twiddle(float2 (&v)[16], int j, const float2 *__restrict__ tw)
 {
     constexpr int STEP = FFT_MAX / N;
-#pragma unroll
-    for (int r = 1; r < 16; ++r) v[r] = cmul(v[r], twid<DIR>(tw, r * j * STEP));
+    twiddle_powers<16, DIR>(v, tw, j * STEP);
 }
 
 // Middle stages: Stockham from Ns = 16 up to Ns = N/16 (none when N == 256).

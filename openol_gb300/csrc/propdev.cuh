@@ -107,7 +107,7 @@ __device__ __forceinline__ float2 asm_tf(const PropParams &P, int fx, int fy)
     const float fx2 = (float)(fx * fx), fy2 = (float)(fy * fy);
     const float t = P.tx * fx2 + P.ty * fy2;
     const float s = sqrtf(1.0f - t);
-    const float q = t / (1.0f + s);
+    const float q = __fdividef(t, 1.0f + s); // 1 + s in [1, 2]: the fast divide is within 2 ulp
     const float g = 0.5f * q * q;
     float cyc = P.c0 - frac_mul(P.ax_hi, P.ax_lo, fx2) - frac_mul(P.ay_hi, P.ay_lo, fy2) - P.zl * g;
     if (P.shift) {
