@@ -54,13 +54,64 @@ __device__ __forceinline__ cpair cp_rot(const cpair &v, float2 C, float2 S, floa
     return {__ffma2_rn(v.im, NS, __fmul2_rn(v.re, C)), __ffma2_rn(v.re, S, __fmul2_rn(v.im, C))};
 }
 
-// v * table twiddle m (DIR < 0: exp(-2 pi i m / FFT_MAX); DIR > 0: its conjugate)
+// a twiddle broadcast to both lanes: (c, c), (s, s) and (-s, -s); loaded
+// from table entry m it is exp(-2 pi i m / FFT_MAX) for DIR < 0, else its
+// conjugate
+struct cptw {
+    float2 C, S, NS;
+};
+
 template <int DIR>
-__device__ __forceinline__ cpair cp_twid(const cpair &v, const float4 *__restrict__ tw, int m)
+__device__ __forceinline__ cptw cp_tw_load(const float4 *__restrict__ tw, int m)
 {
     const float4 w = __ldg(tw + m);
-    const float2 C = make_float2(w.x, w.y), S = make_float2(w.z, w.w), NS = pneg(S);
-    return DIR < 0 ? cp_rot(v, C, S, NS) : cp_rot(v, C, NS, S);
+    const float2 S = make_float2(w.z, w.w), NS = pneg(S);
+    return DIR < 0 ? cptw{make_float2(w.x, w.y), S, NS} : cptw{make_float2(w.x, w.y), NS, S};
+}
+
+// a b for two broadcast twiddles (paired ops; the lanes stay equal)
+__device__ __forceinline__ cptw cp_tw_mul(const cptw &a, const cptw &b)
+{
+    const float2 C = __ffma2_rn(a.S, b.NS, __fmul2_rn(a.C, b.C));
+    const float2 S = __ffma2_rn(a.S, b.C, __fmul2_rn(a.C, b.S));
+    return {C, S, pneg(S)};
+}
+
+__device__ __forceinline__ cpair cp_rot(const cpair &v, const cptw &w) { return cp_rot(v, w.C, w.S, w.NS); }
+
+// v[r] *= w^r for r = 1 .. R-1 with w = table[m] (conjugated for DIR > 0):
+// w, w^2, w^4, w^8 from the table, the other powers as products of those,
+// as twiddle_powers does for the scalar form.
+template <int R, int DIR>
+__device__ __forceinline__ void cp_twiddle_powers(cpair (&v)[R], const float4 *__restrict__ tw, int m)
+{
+    static_assert(R == 2 || R == 4 || R == 8 || R == 16, "radix 2, 4, 8 or 16");
+    const cptw w1 = cp_tw_load<DIR>(tw, m);
+    v[1] = cp_rot(v[1], w1);
+    if constexpr (R >= 4) {
+        const cptw w2 = cp_tw_load<DIR>(tw, 2 * m), w3 = cp_tw_mul(w2, w1);
+        v[2] = cp_rot(v[2], w2);
+        v[3] = cp_rot(v[3], w3);
+        if constexpr (R >= 8) {
+            const cptw w4 = cp_tw_load<DIR>(tw, 4 * m);
+            const cptw w5 = cp_tw_mul(w4, w1), w6 = cp_tw_mul(w4, w2), w7 = cp_tw_mul(w4, w3);
+            v[4] = cp_rot(v[4], w4);
+            v[5] = cp_rot(v[5], w5);
+            v[6] = cp_rot(v[6], w6);
+            v[7] = cp_rot(v[7], w7);
+            if constexpr (R == 16) {
+                const cptw w8 = cp_tw_load<DIR>(tw, 8 * m);
+                v[8] = cp_rot(v[8], w8);
+                v[9] = cp_rot(cp_rot(v[9], w8), w1);
+                v[10] = cp_rot(cp_rot(v[10], w8), w2);
+                v[11] = cp_rot(cp_rot(v[11], w8), w3);
+                v[12] = cp_rot(cp_rot(v[12], w8), w4);
+                v[13] = cp_rot(cp_rot(v[13], w8), w5);
+                v[14] = cp_rot(cp_rot(v[14], w8), w6);
+                v[15] = cp_rot(cp_rot(v[15], w8), w7);
+            }
+        }
+    }
 }
 
 template <int DIR>
@@ -195,8 +246,7 @@ template <int N, int DIR>
 __device__ __forceinline__ void cp_last_twiddle(cpair (&v)[16], int j, const float4 *__restrict__ tw)
 {
     constexpr int STEP = FFT_MAX / N;
-#pragma unroll
-    for (int r = 1; r < 16; ++r) v[r] = cp_twid<DIR>(v[r], tw, r * j * STEP);
+    cp_twiddle_powers<16, DIR>(v, tw, j * STEP);
 }
 
 template <int N, int NSP, bool COLS>
@@ -227,8 +277,7 @@ __device__ __forceinline__ void cp_fft_stage(float4 *s, int ss, const float4 *__
         if constexpr (NS > 1) {
             const int k = j & (NS - 1);
             constexpr int STEP = FFT_MAX / (NS * R);
-#pragma unroll
-            for (int r = 1; r < R; ++r) v[t][r] = cp_twid<DIR>(v[t][r], tw, r * k * STEP);
+            cp_twiddle_powers<R, DIR>(v[t], tw, k * STEP);
         }
         cp_dft<R, DIR>(v[t]);
     }
