@@ -215,9 +215,12 @@ int olg_prop_c64(void *u, int ny, int nx, double dy, double dx, double lambda, d
  * its own chain of kernels and cuFFT calls).  Sizes: ny, nx powers of two in
  * [256, 4096].  olg_batch_plan_create uploads the descriptors and takes all
  * scratch (cudaMalloc; synchronous); olg_batch_execute then only resets
- * counters and launches one kernel on `stream`, so it can be captured in a
- * CUDA graph and replayed.  olg_batch_execute_serial runs the same fields one
- * after another through the single-field entry points (the baseline). */
+ * counters and launches on `stream`, so it can be captured in a CUDA graph
+ * and replayed.  Fields of at least olg_batch_direct_pixels() pixels (default
+ * 2048 x 2048; each fills the GPU alone) run after the persistent kernel
+ * through the single-field passes; the persistent kernel takes the rest.
+ * olg_batch_execute_serial runs every field one after another through the
+ * single-field passes (the baseline). */
 #define OLG_BATCH_ASM 0
 #define OLG_BATCH_FRESNEL 1
 #define OLG_BATCH_ARSS 2
@@ -238,6 +241,12 @@ int olg_batch_execute_serial(olg_batch_plan plan, olg_stream_t stream);
 /* Synchronous: OLG_ERR_CUDA if an item of the last execution gave up on its bounded wait. */
 int olg_batch_check(olg_batch_plan plan);
 int olg_batch_plan_items(olg_batch_plan plan);
+/* Fields of this plan that run through the single-field passes. */
+int olg_batch_plan_direct_fields(olg_batch_plan plan);
+/* Sets the size (ny * nx) from which plans created afterwards run a field
+ * through the single-field passes (pixels > 0); returns the previous value
+ * (pixels <= 0: only returns the current one). */
+long long olg_batch_direct_pixels(long long pixels);
 int olg_batch_plan_destroy(olg_batch_plan plan);
 
 /* -------------------------------------------------- phase optimisation */

@@ -58,6 +58,8 @@ SIGNATURES = {
     "olg_fresnel_prop_check": (_i, [_i, _i, _d, _d, _d, _d, _i]),
     "olg_prop_c64": (_i, [_p, _i, _i, _d, _d, _d, _d, _i, _i, C.POINTER(_i), _p, _sz, _p]),
     "olg_batch_plan_create": (_i, [C.POINTER(OlgField), _i, C.POINTER(_p)]),
+    "olg_batch_direct_pixels": (C.c_longlong, [C.c_longlong]),
+    "olg_batch_plan_direct_fields": (_i, [_p]),
     "olg_batch_execute": (_i, [_p, _p]),
     "olg_batch_execute_serial": (_i, [_p, _p]),
     "olg_batch_check": (_i, [_p]),

@@ -1,5 +1,7 @@
 """Batched propagation: many fields of different sizes, methods, distances and
-wavelengths in one persistent launch (olg_batch_*), replayable from a CUDA graph."""
+wavelengths in one persistent launch (olg_batch_*), replayable from a CUDA graph.
+Fields of at least ``direct_pixels()`` pixels (default 2048 x 2048) each fill the
+GPU alone and run after it through the single-field passes."""
 from __future__ import annotations
 
 import ctypes as C
@@ -34,9 +36,11 @@ class BatchPlan:
         call("olg_batch_plan_create", arr, len(fields), C.byref(self._plan))
         self.n_fields = len(fields)
         self.n_items = int(lib().olg_batch_plan_items(self._plan))
+        self.n_direct = int(lib().olg_batch_plan_direct_fields(self._plan))
 
     def execute(self, stream=None):
-        """One persistent launch (capturable in a CUDA graph)."""
+        """One persistent launch for the small fields, then the single-field passes
+        for the large ones (capturable in a CUDA graph)."""
         call("olg_batch_execute", self._plan, _stream(stream))
 
     def execute_serial(self, stream=None):
@@ -44,6 +48,7 @@ class BatchPlan:
         call("olg_batch_execute_serial", self._plan, _stream(stream))
 
     def check(self):
+        """Raises OlgError if an item of the last persistent launch gave up on its bounded wait."""
         call("olg_batch_check", self._plan)
 
     def close(self):
@@ -56,6 +61,13 @@ class BatchPlan:
             self.close()
         except Exception:
             pass
+
+
+def direct_pixels(pixels=None):
+    """The size (ny * nx) from which plans created afterwards run a field through
+    the single-field passes instead of the persistent kernel; with ``pixels``,
+    sets it and returns the previous value."""
+    return int(lib().olg_batch_direct_pixels(int(pixels) if pixels else 0))
 
 
 def config5_fields(n=96, seed=20261203 + 5, p=8e-6, s=0.5, device="cuda"):

@@ -2123,6 +2123,7 @@ __global__ void __launch_bounds__(BATCH_NT, BATCH_CTAS_PER_SM) k_batch(BatchDev 
 struct olg_batch_plan_s {
     int dev = 0, n = 0, n_items = 0, grid = 0;
     std::vector<olg_field> fields;
+    std::vector<char> direct; // per field: run through the tuned per-field passes, not k_batch
     std::vector<size_t> ws_off;
     char *mem = nullptr;
     size_t bytes = 0;
@@ -2134,6 +2135,13 @@ namespace olg {
 namespace {
 
 bool batch_size_ok(int n) { return n >= 256 && n <= FFT_MAX / 2 && is_pow2(n); }
+
+// Fields of at least this many pixels leave the persistent kernel: each fills
+// the GPU on its own, and the per-field passes (autotuned launch shapes, no
+// register cap shared with the largest length) run them faster; the
+// persistent launch keeps the many small fields, where launches would cost
+// more than the work.
+std::atomic<long long> g_batch_direct_pixels{2048LL * 2048LL};
 
 int field_setup(const olg_field &F, const Layout &L, PropSetup *S)
 {
@@ -2168,6 +2176,9 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
     plan->n = n_fields;
     plan->fields.assign(fields, fields + n_fields);
     plan->dev = dev;
+    const long long direct_px = g_batch_direct_pixels.load();
+    plan->direct.resize(n_fields);
+    for (int i = 0; i < n_fields; ++i) plan->direct[i] = (long long)fields[i].ny * fields[i].nx >= direct_px;
     // device memory: [PropParams x n][ChirpAxis jobs][items][done 3n][target 3n][head, err][per-field scratch]
     std::vector<PropSetup> setups(n_fields);
     std::vector<ChirpAxis> jobs;
@@ -2214,7 +2225,7 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
             return rc;
         }
         setups[i].P.coherent = 1;
-        if (setups[i].chirps) {
+        if (setups[i].chirps && !plan->direct[i]) {
             for (int a = 0; a < 2; ++a) {
                 const ChirpAxis &A = a ? setups[i].ay : setups[i].ax;
                 const int jidx = (int)jobs.size();
@@ -2230,6 +2241,7 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
     }
     for (int kind = BK_FWD; kind <= BK_INV; ++kind)
         for (int i : order) {
+            if (plan->direct[i]) continue;
             const olg_field &F = plan->fields[i];
             const int NX = 2 * F.nx, NY = 2 * F.ny;
             if (kind == BK_COLS) {
@@ -2282,6 +2294,23 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
     return OLG_OK;
 }
 
+namespace olg {
+namespace {
+
+// one field through the single-field passes, in the plan's workspace
+int batch_field_direct(olg_batch_plan plan, int i, cudaStream_t st)
+{
+    const olg_field &F = plan->fields[i];
+    Layout L;
+    layout_bytes(F.ny, F.nx, &L, plan->mem + plan->ws_off[i]);
+    PropSetup S;
+    if (int rc = field_setup(F, L, &S)) return rc;
+    return run_setup(S, st);
+}
+
+} // namespace
+} // namespace olg
+
 extern "C" int olg_batch_execute(olg_batch_plan plan, olg_stream_t stream)
 {
     if (!plan) return fail(OLG_ERR_INVALID_ARG, "null plan");
@@ -2290,24 +2319,38 @@ extern "C" int olg_batch_execute(olg_batch_plan plan, olg_stream_t stream)
     cudaError_t e = cudaMemsetAsync(plan->D.done, 0, plan->counters_bytes, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(plan->D.head, 0, 2 * sizeof(int), st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync (batch counters)");
-    k_batch<<<plan->grid, BATCH_NT, BATCH_SMEM, st>>>(plan->D);
-    count_launch();
-    return check_launch("k_batch");
+    if (plan->n_items > 0) {
+        k_batch<<<plan->grid, BATCH_NT, BATCH_SMEM, st>>>(plan->D);
+        count_launch();
+        if (int rc = check_launch("k_batch")) return rc;
+    }
+    for (int i = 0; i < plan->n; ++i)
+        if (plan->direct[i])
+            if (int rc = batch_field_direct(plan, i, st)) return rc;
+    return OLG_OK;
 }
 
 extern "C" int olg_batch_execute_serial(olg_batch_plan plan, olg_stream_t stream)
 {
     if (!plan) return fail(OLG_ERR_INVALID_ARG, "null plan");
     cudaStream_t st = (cudaStream_t)stream;
-    for (int i = 0; i < plan->n; ++i) {
-        const olg_field &F = plan->fields[i];
-        Layout L;
-        layout_bytes(F.ny, F.nx, &L, plan->mem + plan->ws_off[i]);
-        PropSetup S;
-        if (int rc = field_setup(F, L, &S)) return rc;
-        if (int rc = run_setup(S, st)) return rc;
-    }
+    for (int i = 0; i < plan->n; ++i)
+        if (int rc = batch_field_direct(plan, i, st)) return rc;
     return OLG_OK;
+}
+
+extern "C" long long olg_batch_direct_pixels(long long pixels)
+{
+    if (pixels > 0) return g_batch_direct_pixels.exchange(pixels);
+    return g_batch_direct_pixels.load();
+}
+
+extern "C" int olg_batch_plan_direct_fields(olg_batch_plan plan)
+{
+    if (!plan) return 0;
+    int n = 0;
+    for (char d : plan->direct) n += d ? 1 : 0;
+    return n;
 }
 
 extern "C" int olg_batch_check(olg_batch_plan plan)

@@ -44,6 +44,16 @@ def test_status_strings():
     assert b"argument" in L.olg_status_string(-1)
 
 
+def test_batch_direct_threshold_without_gpu():
+    L = _lib.lib()
+    cur = L.olg_batch_direct_pixels(0)
+    assert cur == 2048 * 2048
+    assert L.olg_batch_direct_pixels(1000) == cur
+    assert L.olg_batch_direct_pixels(-5) == 1000  # <= 0 only reads
+    assert L.olg_batch_direct_pixels(cur) == 1000
+    assert L.olg_batch_plan_direct_fields(None) == 0
+
+
 def test_auto_checks_match_reference_float_and_double(golden):
     L = _lib.lib()
     for ny, nx, p, lam, z, a64, a32, f64, f32 in golden["checks"]:

@@ -78,3 +78,29 @@ def test_batch_cuda_graph_replay_and_in_place():
         twice = oracle_of(f2)
         assert rel_l2(f["u_in"].cpu().numpy(), twice) < 2e-5, f["method"]
     plan.close()
+
+
+def test_batch_large_fields_run_through_single_field_passes():
+    # lower the threshold so that four of the seven mixed fields (ASM, Fresnel
+    # and ARSS among them) leave the persistent kernel, then capture and replay
+    old = og.batch_direct_pixels(512 * 512)
+    try:
+        fields = mixed_fields(seed=11)
+        plan = og.BatchPlan(fields)
+        assert plan.n_direct == 4
+        s = torch.cuda.Stream()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                plan.execute(stream=s)
+        for f in fields:
+            f["u_out"].zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        plan.check()
+        for f in fields:
+            assert rel_l2(f["u_out"].cpu().numpy(), oracle_of(f)) < 1e-5, (f["method"], tuple(f["u_in"].shape))
+        plan.close()
+    finally:
+        og.batch_direct_pixels(old)
+    assert og.batch_direct_pixels() == old
