@@ -85,6 +85,12 @@ const char *olg_status_string(int status);
 const char *olg_last_error(void);
 /* Number of kernels this library has launched so far in this process. */
 unsigned long long olg_launch_count(void);
+/* Device address of page-locked (pinned) host memory.  Passed as u_in /
+ * u_out of olg_asm_prop_c64, it lets pass 1 read the input and pass 3 write
+ * the output over the host link (NVLink-C2C on GB300) with no staging copies.
+ * OLG_ERR_INVALID_ARG if `host` is not page-locked memory mapped for the
+ * current device. */
+int olg_host_device_pointer(const void *host, void **dev);
 
 /* ------------------------------------------------------------ propagation */
 /* Device scratch for one propagation of an ny x nx field (any method). */

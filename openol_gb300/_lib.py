@@ -37,6 +37,7 @@ SIGNATURES = {
     "olg_status_string": (C.c_char_p, [_i]),
     "olg_last_error": (C.c_char_p, []),
     "olg_launch_count": (C.c_ulonglong, []),
+    "olg_host_device_pointer": (_i, [_p, C.POINTER(_p)]),
     "olg_prop_workspace_bytes": (_sz, [_i, _i]),
     "olg_asm_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _p, _sz, _p]),
     "olg_shifted_asm_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _i, _p, _sz, _p]),

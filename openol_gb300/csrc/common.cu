@@ -110,3 +110,16 @@ extern "C" const char *olg_status_string(int status)
 extern "C" const char *olg_last_error(void) { return olg::t_err.c_str(); }
 
 extern "C" unsigned long long olg_launch_count(void) { return olg::g_launches.load(); }
+
+extern "C" int olg_host_device_pointer(const void *host, void **dev)
+{
+    if (!host || !dev) return olg::fail(OLG_ERR_INVALID_ARG, "null pointer");
+    *dev = nullptr;
+    cudaPointerAttributes a{};
+    const cudaError_t e = cudaPointerGetAttributes(&a, host);
+    if (e != cudaSuccess) return olg::cuda_fail(e, "cudaPointerGetAttributes");
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer)
+        return olg::fail(OLG_ERR_INVALID_ARG, "not page-locked host memory mapped for the device");
+    *dev = a.devicePointer;
+    return OLG_OK;
+}

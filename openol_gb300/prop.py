@@ -65,19 +65,39 @@ def _host_roundtrip(u, ny, nx, fn):
 
 
 # ------------------------------------------------------------------ general
+def _pinned_ptr(u, ny, nx, name):
+    """Device address of a page-locked host field (olg_host_device_pointer)."""
+    if u.dtype != torch.complex64 or not u.is_contiguous() or u.numel() != ny * nx:
+        raise ValueError(f"{name} must be a contiguous complex64 tensor with ny*nx = {ny * nx} elements")
+    d = C.c_void_p()
+    call("olg_host_device_pointer", u.data_ptr(), C.byref(d))
+    return d.value
+
+
+def _field_ptr(u, ny, nx, name):
+    """CUDA tensors by address; pinned CPU tensors by their mapped device address."""
+    if isinstance(u, torch.Tensor) and not u.is_cuda and u.is_pinned():
+        return _pinned_ptr(u, ny, nx, name)
+    return _dev_field(u, ny, nx, name).data_ptr()
+
+
 def asm_prop(u_in, u_out=None, *, dy, dx, lam, z, adjoint=False, normalize=True, stream=None, work=None):
-    """Angular spectrum method on device tensors (olg_asm_prop_c64).
+    """Angular spectrum method (olg_asm_prop_c64) on CUDA tensors or on pinned
+    (page-locked) CPU tensors.  For pinned fields pass 1 reads the input and
+    pass 3 writes the output over the host link directly, with no staging
+    copies; as for device fields, the result is ready once ``stream`` is.
 
     ``adjoint`` applies the conjugate transfer function (the adjoint operator);
     ``normalize=False`` omits 1/Np like the host-pointer overload.
     """
     ny, nx = u_in.shape
-    _dev_field(u_in, ny, nx, "u_in")
-    u_out = u_in if u_out is None else _dev_field(u_out, ny, nx, "u_out")
+    pin = _field_ptr(u_in, ny, nx, "u_in")
+    u_out = u_in if u_out is None else u_out
+    pout = _field_ptr(u_out, ny, nx, "u_out")
     flags = (OLG_CONJ if adjoint else 0) | (0 if normalize else OLG_NO_NORMALIZE)
     wp, wb = (work.data_ptr(), work.numel() * work.element_size()) if work is not None else (None, 0)
-    call("olg_asm_prop_c64", u_in.data_ptr(), u_out.data_ptr(), ny, nx, float(dy), float(dx), float(lam), float(z),
-         flags, wp, wb, _stream(stream))
+    call("olg_asm_prop_c64", pin, pout, ny, nx, float(dy), float(dx), float(lam), float(z), flags, wp, wb,
+         _stream(stream))
     return u_out
 
 

@@ -109,6 +109,8 @@ def test_argument_validation_without_gpu():
     assert L.olg_split_prop_c64(base, base, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 0, 2, 2, 0, None, 0, None) == -1
     assert b"overlap" in L.olg_last_error()
     assert L.olg_split_prop_c64(base, base + 16, 64, 64, 8e-6, 8e-6, 532e-9, 0.05, 2, 2, 2, 0, None, 0, None) == -1
+    out = C.c_void_p()
+    assert L.olg_host_device_pointer(None, C.byref(out)) == -1 and out.value is None
     # tilted planes: interpolation, mode, evanescent grid, Fresnel at z = 0, unsupported length
     tp = L.olg_tilted_prop_c64
     assert tp(base, base, 64, 64, 8e-6, 8e-6, 532e-9, 0.02, 0.1, 2, 0, 0, None, 0, None) == -1

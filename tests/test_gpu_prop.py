@@ -172,3 +172,4 @@ def test_errors_raise():
     v = torch.zeros((64, 64), dtype=torch.complex64, device="cuda")
     with pytest.raises(og.OlgError):
         og.arss_prop(v, dy=8e-6, dx=8e-6, lam=532e-9, z=0.05, s=1.0)
+
