@@ -82,7 +82,7 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
-        except Exception:
+        except OSError:  # nvidia-smi missing: the line then says so
             self.proc = None
         return self
 
@@ -92,7 +92,7 @@ class ClockSampler:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
-            except Exception:
+            except subprocess.TimeoutExpired:
                 self.proc.kill()
 
     def summary(self):
