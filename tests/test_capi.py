@@ -52,6 +52,9 @@ def test_batch_direct_threshold_without_gpu():
     assert L.olg_batch_direct_pixels(-5) == 1000  # <= 0 only reads
     assert L.olg_batch_direct_pixels(cur) == 1000
     assert L.olg_batch_plan_direct_fields(None) == 0
+    import openol_gb300 as og
+    assert og.batch_direct_pixels() == cur
+    assert og.batch_direct_pixels(4096) == cur and og.batch_direct_pixels(cur) == 4096
 
 
 def test_auto_checks_match_reference_float_and_double(golden):
