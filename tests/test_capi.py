@@ -57,6 +57,27 @@ def test_batch_direct_threshold_without_gpu():
     assert og.batch_direct_pixels(4096) == cur and og.batch_direct_pixels(cur) == 4096
 
 
+def test_tuning_knobs_without_gpu():
+    L = _lib.lib()
+    # launch-shape table of the three passes (host state only)
+    n_var = L.olg_prop_variant_count()
+    assert n_var >= 10
+    old = L.olg_prop_get_variant(1, 2048)
+    assert 0 <= old < n_var
+    assert L.olg_prop_set_variant(1, 2048, 8) == 0 and L.olg_prop_get_variant(1, 2048) == 8
+    assert L.olg_prop_set_variant(1, 2048, n_var) == -1  # no such shape
+    assert L.olg_prop_set_variant(3, 2048, 0) == -1      # no such pass
+    assert L.olg_prop_set_variant(0, 3000, 0) == -1      # not a tuned length
+    assert L.olg_prop_get_variant(0, 100) == -1
+    assert L.olg_prop_set_variant(1, 2048, old) == 0
+    # GEMM K-tail weight: out-of-range values leave it unchanged
+    w = L.olg_cgh_gemm_tail_weight(-1.0)
+    assert w == 1.2
+    assert L.olg_cgh_gemm_tail_weight(2.0) == w
+    assert L.olg_cgh_gemm_tail_weight(99.0) == 2.0
+    assert L.olg_cgh_gemm_tail_weight(w) == 2.0
+
+
 def test_auto_checks_match_reference_float_and_double(golden):
     L = _lib.lib()
     for ny, nx, p, lam, z, a64, a32, f64, f32 in golden["checks"]:
