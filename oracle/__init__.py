@@ -35,10 +35,14 @@ _p = C.c_void_p
 
 
 def build(ref: bool = False) -> None:
-    """Compile libolcpu.so (and the reference build when ``ref``)."""
+    """Compile libolcpu.so.  With ``ref``, also the reference's own CPU build
+    and a staged copy of its headers for the GPU harness (both only where the
+    reference tree is present; the recipe skips them elsewhere)."""
     subprocess.run(["make", "-s", "-C", HERE, "libolcpu.so"], check=True)
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref-gpu-src"], check=False,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
 
 
 def _ptr(a):

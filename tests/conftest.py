@@ -42,6 +42,12 @@ def golden():
     return np.load(os.path.join(ROOT, "tests", "golden", "ref_golden.npz"))
 
 
+@pytest.fixture(scope="session")
+def golden_dir():
+    import pathlib
+    return pathlib.Path(ROOT) / "tests" / "golden"
+
+
 def rel_l2(a, b):
     import numpy as np
     a = np.asarray(a, np.complex128)
