@@ -89,6 +89,32 @@ void WRPStep1_D(gObject<_Tp> &obj, cuda::unique_ptr<thrust::complex<COMPLEX_T>[]
     olgb::sync("WRPStep1_D");
 }
 
+// golcgh.h:494-517: propagate the WRP by d.  AUTO takes gAsmProp when
+// AsmPropCheck passes; otherwise gFresnelProp when FresnelPropCheck passes,
+// else gAsmProp after a warning (not the band-limited Fresnel of Prop).
+// Prints the choice like the reference.
+template <typename COMPLEX_T, typename PREC_T>
+void WRPStep2(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &U, int ny, int nx, PREC_T p, PREC_T lambda, PREC_T d,
+              PROPMODE propmode = PROPMODE::AUTO)
+{
+    if (propmode == PROPMODE::FRESNEL) {
+        gFresnelProp(U, ny, nx, p, p, lambda, d);
+    } else if (propmode == PROPMODE::ASM) {
+        gAsmProp(U, ny, nx, p, p, lambda, d);
+    } else if (propmode == PROPMODE::AUTO) {
+        if (AsmPropCheck(ny, nx, p, p, lambda, d)) {
+            std::printf("WRP Step2 is AsmProp\n");
+            gAsmProp(U, ny, nx, p, p, lambda, d);
+        } else if (!FresnelPropCheck(ny, nx, p, p, lambda, d)) {
+            std::printf("warning!!\neither AsmProp or FresnelProp does not meet the condition.\n");
+            gAsmProp(U, ny, nx, p, p, lambda, d);
+        } else {
+            std::printf("WRP Step2 is FresnelProp\n");
+            gFresnelProp(U, ny, nx, p, p, lambda, d);
+        }
+    }
+}
+
 namespace olgb {
 template <typename _Tp, typename COMPLEX_T, typename PREC_T>
 void wrp_method(gObject<_Tp> &obj, cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &U, int ny, int nx, PREC_T p,

@@ -22,8 +22,9 @@ template <typename F, typename N>
 void check_error(const ::cudaError_t e, F &&f, N &&n)
 {
     if (e != ::cudaSuccess) {
-        std::stringstream s;
-        s << ::cudaGetErrorName(e) << " (" << e << ")@" << f << "#L" << n << ": " << ::cudaGetErrorString(e);
+        std::ostringstream s;
+        s << "CUDA call failed at " << f << ":" << n << " -- " << ::cudaGetErrorString(e) << " ["
+          << ::cudaGetErrorName(e) << ", code " << static_cast<int>(e) << "]";
         throw std::runtime_error{s.str()};
     }
 }

@@ -5,7 +5,7 @@
  * returns with the device synchronised; errors throw std::runtime_error (the
  * reference's CHECK_CUDA_ERROR behaviour) instead of passing silently.
  * Fields are complex64 (thrust::complex<float>).  AsmPropCheck /
- * FresnelPropCheck stay in the reference's CPU olprop.h; Prop evaluates them
+ * FresnelPropCheck live in olprop.h, as in the reference; Prop evaluates them
  * through olg_asm_prop_check / olg_fresnel_prop_check in PREC_T precision.
  */
 #ifndef OLGB300_GOLPROP_H
@@ -20,32 +20,9 @@
 #include "../olgb300.h"
 #include "golclass.h"
 #include "oldefine.h"
+#include "olprop.h"
 
 namespace ol {
-namespace olgb {
-inline void check(int rc, const char *where)
-{
-    if (rc != OLG_OK) throw std::runtime_error(std::string(where) + ": " + olg_last_error());
-}
-inline void sync(const char *where) { CHECK_CUDA_ERROR(cudaDeviceSynchronize()); (void)where; }
-template <typename C>
-constexpr void complex64_only()
-{
-    static_assert(std::is_same<C, float>::value, "libolgb300 propagates complex64 (thrust::complex<float>) fields");
-}
-template <typename COMPLEX_T, typename F>
-void host_roundtrip(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int ny, int nx, F &&fn)
-{
-    complex64_only<COMPLEX_T>();
-    const size_t bytes = sizeof(std::complex<float>) * (size_t)ny * nx;
-    void *d = nullptr;
-    CHECK_CUDA_ERROR(cudaMalloc(&d, bytes));
-    CHECK_CUDA_ERROR(cudaMemcpy(d, u.get(), bytes, cudaMemcpyHostToDevice));
-    fn(d);
-    CHECK_CUDA_ERROR(cudaMemcpy(u.get(), d, bytes, cudaMemcpyDeviceToHost));
-    CHECK_CUDA_ERROR(cudaFree(d));
-}
-} // namespace olgb
 
 // device overload, golprop.h:507-534
 template <typename COMPLEX_T, typename PREC_T>
@@ -62,7 +39,7 @@ template <typename COMPLEX_T, typename PREC_T>
 void gAsmProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx, PREC_T lambda,
               PREC_T d)
 {
-    olgb::host_roundtrip(u, ny, nx, [&](void *p) {
+    olgb::host_field(u, ny, nx, [&](void *p) {
         olgb::check(olg_asm_prop_c64(p, p, ny, nx, dy, dx, lambda, d, OLG_NO_NORMALIZE, nullptr, 0, nullptr), "gAsmProp");
     });
 }
@@ -83,7 +60,7 @@ template <typename COMPLEX_T, typename PREC_T>
 void gFresnelProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx, PREC_T lambda,
                   PREC_T d)
 {
-    olgb::host_roundtrip(u, ny, nx, [&](void *p) {
+    olgb::host_field(u, ny, nx, [&](void *p) {
         olgb::check(olg_fresnel_prop_c64(p, p, ny, nx, dy, dx, lambda, d, 0, OLG_NO_NORMALIZE, nullptr, 0, nullptr),
                     "gFresnelProp");
     });
@@ -185,40 +162,8 @@ void gsplitProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int64_t height, i
     olgb::check(rc, "gsplitProp");
 }
 
-// TiltedSourceProp olprop.h:414-521 / TiltedReferenceProp olprop.h:523-600:
-// the reference's CPU templates, here on the GPU for a host field (copied in
-// and out) or a device field (in place)
-namespace olgb {
-inline int tilt_mode(PROPMODE propmode)
-{
-    return propmode == PROPMODE::ASM ? OLG_ASM : propmode == PROPMODE::FRESNEL ? OLG_FRESNEL : -1;
-}
-} // namespace olgb
-
-template <typename PREC_T = float, typename COMPLEX_T>
-void TiltedSourceProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx,
-                      PREC_T lambda, PREC_T z, PREC_T angle_src2dst, INTERPOLATION inp = BILINEAR,
-                      PROPMODE propmode = ASM)
-{
-    olgb::host_roundtrip(u, ny, nx, [&](void *d) {
-        olgb::check(olg_tilted_prop_c64(d, d, ny, nx, dy, dx, lambda, z, angle_src2dst, (int)inp,
-                                        olgb::tilt_mode(propmode), 0, nullptr, 0, nullptr),
-                    "TiltedSourceProp");
-    });
-}
-
-template <typename PREC_T = float, typename COMPLEX_T>
-void TiltedReferenceProp(std::unique_ptr<std::complex<COMPLEX_T>[]> &u, int64_t ny, int64_t nx, PREC_T dy, PREC_T dx,
-                         PREC_T lambda, PREC_T z, PREC_T rotate, INTERPOLATION inp = BILINEAR,
-                         PROPMODE propmode = ASM)
-{
-    olgb::host_roundtrip(u, (int)ny, (int)nx, [&](void *d) {
-        olgb::check(olg_tilted_prop_c64(d, d, (int)ny, (int)nx, dy, dx, lambda, z, rotate, (int)inp,
-                                        olgb::tilt_mode(propmode), 1, nullptr, 0, nullptr),
-                    "TiltedReferenceProp");
-    });
-}
-
+// TiltedSourceProp / TiltedReferenceProp on device fields (the host-field
+// overloads of olprop.h:414-600 are in olprop.h), in place
 template <typename PREC_T = float, typename COMPLEX_T>
 void TiltedSourceProp(cuda::unique_ptr<thrust::complex<COMPLEX_T>[]> &u, int ny, int nx, PREC_T dy, PREC_T dx,
                       PREC_T lambda, PREC_T z, PREC_T angle_src2dst, INTERPOLATION inp = BILINEAR,

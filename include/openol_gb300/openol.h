@@ -5,6 +5,8 @@
 #include "olclass.h"
 #include "oldefine.h"
 #include "golclass.h"
+#include "olprop.h"
+#include "olcgh.h"
 #include "golprop.h"
 #include "golcgh.h"
 #include "olobject.h"

@@ -6,14 +6,15 @@ the host-side mirror of the reference's golprop.h / golcgh.h / olimg.h calls,
 with PyTorch CUDA tensors standing in for the reference's device buffers.
 """
 from ._lib import OlgError, launch_count, lib  # noqa: F401
-from .cgh import (Object2cuda, WRPMethod, WRPMethod_D, WRPStep1, WRPStep1_D, WRPStep2,  # noqa: F401
-                  cgh_exact, cgh_fresnel, cgh_fresnel_gemm, cgh_gemm_workspace, device_fault_check, gCgh, gCghReduction, gObject, wrp_plane_z)
+from .cgh import (Cgh, Object2cuda, WRPMethod, WRPMethod_D, WRPStep1, WRPStep1_D, WRPStep2,  # noqa: F401
+                  cgh_exact, cgh_exact_adjoint, cgh_fresnel, cgh_fresnel_adjoint, cgh_fresnel_gemm, cgh_gemm_workspace, device_fault_check, gCgh, gCghReduction, gObject, wrp_plane_z)
 from .img import MODE, binarize, complex2img  # noqa: F401
 from .objects import (OBJSET_MODE, ZMIDDLE, ZMIN, bmpread, bmpwrite, objinfo, objread, objset, objsort,  # noqa: F401
                       objwrite_3d)
 from .batch import BatchPlan, config5_fields, direct_pixels as batch_direct_pixels  # noqa: F401
 from .optim import PhaseOptimizer, make_targets, phase_loss_grad  # noqa: F401
-from .prop import (ASM, AUTO, FRESNEL, PROPMODE, ARSSFresnelProp, AsmPropCheck, FresnelPropCheck,  # noqa: F401
+from .prop import (ASM, AUTO, FRESNEL, PROPMODE, ARSSFresnelProp, AsmProp, AsmPropCheck, FresnelProp,
+                   FresnelPropBandLimit, FresnelPropCheck, PropHost,  # noqa: F401
                    Prop, arss_prop, asm_prop, fresnel_prop, gAsmProp, gFresnelProp, gFresnelPropBandLimit,
                    autotune, get_variant, set_variant, variant_count, workspace, workspace_bytes,
                    gshiftedAsmProp, gshiftedFresnelProp, gsplitProp, shiftedAsmProp, shiftedFresnelProp, shiftedProp,

@@ -190,6 +190,51 @@ def Prop(u, ny, nx, dy, dx, lam, d, propmode=PROPMODE.AUTO, verbose=True, single
 Prop.last_choice = -1
 
 
+# ------------------------------------------- host-field templates of olprop.h
+# The reference's CPU templates take host fields of any std::complex<COMPLEX_T>;
+# these mirrors take host arrays (numpy or CPU tensors) of any complex dtype,
+# propagate them in complex64 on the GPU and write the result back in place.
+def AsmProp(u, height, width, dy, dx, lam, z):
+    """ol::AsmProp, olprop.h:227-248: crop(IFFT(H FFT(pad u)) / Np), in place."""
+    return _host_roundtrip(u, height, width, lambda d: asm_prop(d, dy=dy, dx=dx, lam=lam, z=z))
+
+
+def FresnelProp(u, height, width, dy, dx, lam, z):
+    """ol::FresnelProp, olprop.h:125-148 (both spectra scaled by 1/Np), in place."""
+    return _host_roundtrip(u, height, width, lambda d: fresnel_prop(d, dy=dy, dx=dx, lam=lam, z=z))
+
+
+def FresnelPropBandLimit(u, height, width, dy, dx, lam, z):
+    """ol::FresnelPropBandLimit, olprop.h:150-170: the response zeroed outside the
+    x and y limits of FresnelResponseBandLimit (olprop.h:26-50), in place."""
+    return _host_roundtrip(u, height, width, lambda d: fresnel_prop(d, dy=dy, dx=dx, lam=lam, z=z, bandlimit=2))
+
+
+def PropHost(u, ny, nx, dy, dx, lam, d, propmode=PROPMODE.AUTO, verbose=True, single_precision=False):
+    """ol::Prop for host fields, olprop.h:656-682: AUTO takes AsmProp when
+    AsmPropCheck passes, else FresnelProp when FresnelPropCheck passes, else the
+    CPU FresnelPropBandLimit.  The checks run in double unless
+    ``single_precision`` (the reference's PREC_T)."""
+    say = print if verbose else (lambda *a: None)
+    pm = int(propmode)
+    if pm == PROPMODE.FRESNEL:
+        say("FresnelProp")
+        return FresnelProp(u, ny, nx, dy, dx, lam, d)
+    if pm == PROPMODE.ASM:
+        say("AsmProp")
+        return AsmProp(u, ny, nx, dy, dx, lam, d)
+    if pm != PROPMODE.AUTO:
+        raise ValueError("invalid PROPMODE")
+    if AsmPropCheck(ny, nx, dy, dx, lam, d, single_precision):
+        say("AsmProp")
+        return AsmProp(u, ny, nx, dy, dx, lam, d)
+    if not FresnelPropCheck(ny, nx, dy, dx, lam, d, single_precision):
+        say("warning!!\neither AsmProp or FresnelProp does not meet the condition.")
+        return FresnelPropBandLimit(u, ny, nx, dy, dx, lam, d)
+    say("FresnelProp")
+    return FresnelProp(u, ny, nx, dy, dx, lam, d)
+
+
 # ------------------------------------------------------- shifted / split
 def _work(work):
     return (work.data_ptr(), work.numel() * work.element_size()) if work is not None else (None, 0)

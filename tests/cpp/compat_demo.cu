@@ -2,8 +2,10 @@
 // reference's tests/gProp_test.cu and tests/CghProp_test.cu), compiled
 // against the drop-in headers and linked with libolgb300.so.  Writes each
 // result as raw complex64 (or float) to <outdir>/<name>.bin for the parity test.
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <random>
 #include <string>
 
@@ -122,6 +124,87 @@ int main(int argc, char **argv)
         auto img = std::make_unique<uint8_t[]>(H * W);
         for (int i = 0; i < H * W; ++i) img[i] = (uint8_t)(i * 7);
         ol::bmpwrite((out + "/img.bmp").c_str(), img, H, W);
+    }
+    // host-field templates of olprop.h / olcgh.h (the reference's CPU API)
+    {
+        auto w32 = [&](const std::string &name, std::unique_ptr<std::complex<float>[]> &a) {
+            FILE *f = fopen((out + "/" + name + ".bin").c_str(), "wb");
+            fwrite(a.get(), sizeof(std::complex<float>), H * W, f);
+            fclose(f);
+        };
+        auto w64 = [&](const std::string &name, std::unique_ptr<std::complex<double>[]> &a) {
+            FILE *f = fopen((out + "/" + name + ".bin").c_str(), "wb");
+            fwrite(a.get(), sizeof(std::complex<double>), H * W, f);
+            fclose(f);
+        };
+        auto copy32 = [&]() {
+            auto a = std::make_unique<std::complex<float>[]>(H * W);
+            for (int i = 0; i < H * W; ++i) a[i] = u[i];
+            return a;
+        };
+        auto copy64 = [&]() {
+            auto a = std::make_unique<std::complex<double>[]>(H * W);
+            for (int i = 0; i < H * W; ++i) a[i] = std::complex<double>(u[i].real(), u[i].imag());
+            return a;
+        };
+        auto a = copy64();
+        ol::AsmProp(a, H, W, (double)p, (double)p, (double)lambda, 0.02);
+        w64("host_asm_f64", a);
+        auto b = copy32();
+        ol::AsmProp<float>(b, H, W, p, p, lambda, 0.02f);
+        w32("host_asm_f32", b);
+        auto c = copy64();
+        ol::FresnelProp(c, H, W, (double)p, (double)p, (double)lambda, 0.1);
+        w64("host_fresnel", c);
+        auto e = copy64();
+        ol::FresnelPropBandLimit(e, H, W, (double)p, (double)p, (double)lambda, 0.05);
+        w64("host_fresnel_bl", e);
+        const double zs[3] = {0.02, 0.05, 0.1};
+        for (int k = 0; k < 3; ++k) {
+            auto f = copy64();
+            ol::Prop(f, H, W, (double)p, (double)p, (double)lambda, zs[k], ol::PROPMODE::AUTO);
+            w64("host_prop_auto" + std::to_string(k), f);
+        }
+        auto g = copy64();
+        std::unique_ptr<std::complex<double>[]> gd;
+        ol::shiftedAsmProp(g, gd, H, W, (double)p, (double)p, (double)lambda, 0.02, 2e-4, -1e-4);
+        w64("host_shifted_asm", gd);
+        auto sf = copy32();
+        ol::shiftedFresnelProp(sf, H, W, p, p, lambda, 0.05f, 0.7f, 1e-4f, 0.f);
+        w32("host_shifted_fresnel", sf);
+        auto sp = copy32();
+        ol::splitAsmProp(sp, H, W, p, p, lambda, 0.02f, 2, 2);
+        w32("host_split_asm", sp);
+        // Cgh: the four overloads, float and double clouds
+        ol::Object<double> objd(N);
+        for (int j = 0; j < N; ++j) objd[j] = ol::Vect3<double>(obj[j].x, obj[j].y, obj[j].z);
+        std::unique_ptr<std::complex<double>[]> hc;
+        ol::Cgh(objd, hc, H, W, (double)p, (double)lambda);
+        w64("host_cgh", hc);
+        std::unique_ptr<std::complex<float>[]> hc2;
+        ol::Cgh(obj, hc2, H, W, p, p, lambda);
+        w32("host_cgh_pypx", hc2);
+        std::unique_ptr<float[]> hp;
+        ol::Cgh(obj, hp, H, W, p, lambda);
+        std::unique_ptr<double[]> hp2;
+        ol::Cgh(objd, hp2, H, W, (double)p, (double)p, (double)lambda);
+        {
+            FILE *f = fopen((out + "/host_cgh_phase.bin").c_str(), "wb");
+            fwrite(hp.get(), sizeof(float), H * W, f);
+            fclose(f);
+            f = fopen((out + "/host_cgh_phase_f64.bin").c_str(), "wb");
+            fwrite(hp2.get(), sizeof(double), H * W, f);
+            fclose(f);
+        }
+        std::unique_ptr<std::complex<float>[]> hw;
+        ol::WRPStep1(obj, hw, H, W, p, lambda, 0.f);
+        w32("host_wrp_step1", hw);
+        // WRPStep2 on a device field: AUTO at 0.02 (ASM) and 0.1 (Fresnel)
+        for (int k = 0; k < 2; ++k) {
+            ol::cpu2cuda(u, d_u, H * W);
+            ol::WRPStep2(d_u, H, W, p, lambda, k == 0 ? 0.02f : 0.1f);
+            dump(out + "/wrp_step2_" + std::to_string(k) + ".bin", d_u, H * W);
+        }
     }
     printf("compat_demo ok\n");
     return 0;
