@@ -91,6 +91,15 @@ unsigned long long olg_launch_count(void);
  * OLG_ERR_INVALID_ARG if `host` is not page-locked memory mapped for the
  * current device. */
 int olg_host_device_pointer(const void *host, void **dev);
+/* Budget of every bounded device-side wait of the persistent batch kernel
+ * and launches after this call, in SM clock cycles (default 4e9, about 2 s):
+ * a wait that runs out records an error and the kernel returns instead of
+ * hanging.  Sets the budget when cycles > 0; returns the previous value. */
+long long olg_wait_budget_cycles(long long cycles);
+/* Host-side fault injection for tests: the next n scratch allocations from
+ * the library's pool fail with OLG_ERR_NOMEM before touching the device, as
+ * an exhausted device would.  Returns the previous count. */
+int olg_inject_alloc_failures(int n);
 
 /* ------------------------------------------------------------ propagation */
 /* Device scratch for one propagation of an ny x nx field (any method). */
@@ -181,10 +190,13 @@ int olg_tilted_prop_c64(const void *u_in, void *u_out, int ny, int nx, double dy
  * not allocate device memory while they run: a holographic display loop with
  * a fixed per-frame budget (an allocation can synchronise the device and miss
  * a frame), or a plugin inside a host application that owns all GPU memory.
- * Limit: ny * nx <= 1048576 (e.g. 1024 x 1024); larger fields return
- * OLG_ERR_WORKSPACE.  The first call on each device looks up the array's
- * device address and uploads the FFT twiddle table; make that first call
- * before any stream capture.  All calls on a device share the one array:
+ * Limits: ny and nx powers of two in [16, 4096] (mixed-radix sizes, which
+ * olg_asm_prop_c64 accepts, return OLG_ERR_UNSUPPORTED_SIZE: their twiddle
+ * tables are allocated on first use) and ny * nx <= 1048576 (e.g. 1024 x 1024
+ * or 256 x 4096); larger fields return OLG_ERR_WORKSPACE.  The first call in
+ * each CUDA context (per device, and again after a device reset) looks up the
+ * array's device address and uploads the FFT twiddle table; make that first
+ * call before any stream capture.  All calls on a device share the one array:
  * calls that overlap on the GPU (e.g. on two streams) race and corrupt each
  * other's results, so serialise them. */
 int olg_asm_prop_noalloc_c64(const void *u_in, void *u_out, int ny, int nx, double dy, double dx, double lambda,
@@ -246,6 +258,13 @@ int olg_batch_execute(olg_batch_plan plan, olg_stream_t stream);
 int olg_batch_execute_serial(olg_batch_plan plan, olg_stream_t stream);
 /* Synchronous: OLG_ERR_CUDA if an item of the last execution gave up on its bounded wait. */
 int olg_batch_check(olg_batch_plan plan);
+/* For tests of the bounded waits (no counterpart in the reference): raises by
+ * `delta` the number of finished units that the items of `field` wait for at
+ * `stage` (0 set-up jobs, 1 pass-1 units, 2 pass-2 units), so that those
+ * waits can never be satisfied and run out of their budget
+ * (olg_wait_budget_cycles); the kernel then skips those items, records the
+ * error for olg_batch_check and returns.  Synchronous. */
+int olg_batch_plan_raise_target(olg_batch_plan plan, int field, int stage, int delta);
 int olg_batch_plan_items(olg_batch_plan plan);
 /* Fields of this plan that run through the single-field passes. */
 int olg_batch_plan_direct_fields(olg_batch_plan plan);
@@ -295,6 +314,25 @@ int olg_cgh_fresnel_c64(const float *points, const float *amp, const float *phas
  * range reduced per pixel tile in double-float arithmetic. */
 int olg_cgh_exact_c64(const float *points, const float *amp, const float *phase0, int n_points, void *U,
                       int ny, int nx, double py, double px, double lambda, int flags, olg_stream_t stream);
+
+/* Adjoints of the two CGH sums (the transposed sum; hand-written kernels
+ * with no counterpart in the reference, which has only the forward sums).
+ * With K_j(h,w) the unit-weight kernel of the forward routine (no a_j, no
+ * phi_j) and G an ny x nx complex64 field,
+ *   g_j = sum_{h,w} conj(K_j(h,w)) G[h,w]        (n_points complex64),
+ * the adjoint of the linear map from complex point amplitudes a_j e^{i phi_j}
+ * to the hologram: the gradient of a real loss of U with respect to the
+ * amplitudes is g evaluated at G = dL/dU*.  Parallel over points, as the
+ * reference's gCghReduction (golcgh.h:147-195) is; per-band partial sums are
+ * added in a fixed order, so results are deterministic.  OLG_ACCUMULATE
+ * adds into g.  Scratch: olg_cgh_adjoint_workspace_bytes (work == NULL:
+ * stream-ordered pool). */
+size_t olg_cgh_adjoint_workspace_bytes(int n_points, int ny, int nx, int exact);
+int olg_cgh_fresnel_adjoint_c64(const float *points, int n_points, const void *G, void *g, int ny, int nx, double py,
+                                double px, double lambda, int flags, void *work, size_t work_bytes,
+                                olg_stream_t stream);
+int olg_cgh_exact_adjoint_c64(const float *points, int n_points, const void *G, void *g, int ny, int nx, double py,
+                              double px, double lambda, int flags, void *work, size_t work_bytes, olg_stream_t stream);
 
 /* Fresnel-form CGH (same sum as olg_cgh_fresnel_c64, amplitudes/phases
  * included) as a split-FP16 complex GEMM on the tcgen05 tensor cores:

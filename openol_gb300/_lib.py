@@ -72,6 +72,12 @@ SIGNATURES = {
                                  _sz, _p]),
     "olg_cgh_fresnel_c64": (_i, [_p, _p, _p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p]),
     "olg_cgh_exact_c64": (_i, [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d, _i, _p]),
+    "olg_cgh_adjoint_workspace_bytes": (_sz, [_i, _i, _i, _i]),
+    "olg_wait_budget_cycles": (C.c_longlong, [C.c_longlong]),
+    "olg_inject_alloc_failures": (_i, [_i]),
+    "olg_batch_plan_raise_target": (_i, [_p, _i, _i, _i]),
+    "olg_cgh_fresnel_adjoint_c64": (_i, [_p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_cgh_exact_adjoint_c64": (_i, [_p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),
     "olg_cgh_gemm_workspace_bytes": (_sz, [_i, _i, _i]),
     "olg_cgh_fresnel_gemm_c64": (_i, [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),
     "olg_device_fault_check": (_i, [_i]),

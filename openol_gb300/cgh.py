@@ -71,6 +71,31 @@ def cgh_exact(gobj, U, *, ny, nx, py, px, lam, amp=None, phase0=None, accumulate
     return U
 
 
+def _cgh_adjoint(fn, gobj, G, g, ny, nx, py, px, lam, accumulate, stream, work):
+    _dev_field(G, ny, nx, "G")
+    n = gobj.size
+    if g is None:
+        g = torch.zeros(n, dtype=torch.complex64, device=G.device)
+    if not (g.is_cuda and g.dtype == torch.complex64 and g.is_contiguous() and g.numel() == n):
+        raise TypeError("g must be a contiguous CUDA complex64 tensor with one entry per point")
+    wp, wb = (work.data_ptr(), work.numel() * work.element_size()) if work is not None else (None, 0)
+    call(fn, gobj.points.data_ptr(), n, G.data_ptr(), g.data_ptr(), ny, nx, float(py), float(px), float(lam),
+         OLG_ACCUMULATE if accumulate else 0, wp, wb, _stream(stream))
+    return g
+
+
+def cgh_fresnel_adjoint(gobj, G, g=None, *, ny, nx, py, px, lam, accumulate=False, stream=None, work=None):
+    """Adjoint of the Fresnel-form CGH (olg_cgh_fresnel_adjoint_c64):
+    g_j = sum_{h,w} conj(exp(i pi rho^2 / (lambda z_j))) G[h,w]."""
+    return _cgh_adjoint("olg_cgh_fresnel_adjoint_c64", gobj, G, g, ny, nx, py, px, lam, accumulate, stream, work)
+
+
+def cgh_exact_adjoint(gobj, G, g=None, *, ny, nx, py, px, lam, accumulate=False, stream=None, work=None):
+    """Adjoint of the exact spherical CGH (olg_cgh_exact_adjoint_c64):
+    g_j = sum_{h,w} conj(exp(i k r_j) / r_j) G[h,w]."""
+    return _cgh_adjoint("olg_cgh_exact_adjoint_c64", gobj, G, g, ny, nx, py, px, lam, accumulate, stream, work)
+
+
 def cgh_fresnel_gemm(gobj, U, *, ny, nx, py, px, lam, amp=None, phase0=None, accumulate=False, stream=None,
                      work=None, reuse_operands=False):
     """Fresnel-form CGH as a split-FP16 tensor-core GEMM (olg_cgh_fresnel_gemm_c64).
@@ -115,6 +140,32 @@ def gCghReduction(gobj, U, ny, nx, p, lam):
 
 
 # ---------------------------------------------------------------------- WRP
+def Cgh(obj, out, ny, nx, *params):
+    """ol::Cgh for host point clouds and host holograms (olcgh.h:351-379):
+    ``Cgh(obj, out, ny, nx, p, lam)`` or ``Cgh(obj, out, ny, nx, py, px, lam)``.
+    ``obj``: (N, 3) host points (rounded to float32, the GPU path's point type);
+    ``out``: a complex host array (the hologram) or a real one (its phase,
+    atan2 as _CghFresnel olcgh.h:276-295 returns it), written in place."""
+    if len(params) == 2:
+        py = px = params[0]
+        lam = params[1]
+    elif len(params) == 3:
+        py, px, lam = params
+    else:
+        raise TypeError("Cgh(obj, out, ny, nx, p, lam) or Cgh(obj, out, ny, nx, py, px, lam)")
+    g = gObject(np.asarray(obj, np.float32).reshape(-1, 3))
+    if np.iscomplexobj(out):
+        U = torch.zeros((ny, nx), dtype=torch.complex64, device="cuda")
+        gCgh(g, U, ny, nx, py, px, lam)
+        res = U.cpu().numpy()
+    else:
+        ph = torch.zeros((ny, nx), dtype=torch.float32, device="cuda")
+        cgh_fresnel(g, None, ny=ny, nx=nx, py=py, px=px, lam=lam, phase_out=ph)
+        res = ph.cpu().numpy()
+    out[...] = res.reshape(out.shape).astype(out.dtype, copy=False)
+    return out
+
+
 def wrp_plane_z(window, ny, nx, p, lam, zmin, s, p_limit=None) -> float:
     return float(lib().olg_wrp_plane_z(int(window), ny, nx, p, 0.0 if p_limit is None else p_limit, lam, zmin, s))
 

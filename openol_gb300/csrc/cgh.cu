@@ -271,9 +271,215 @@ static int cgh_launch(bool exact, const float *points, const float *amp, const f
     return check_launch(exact ? "k_cgh<exact>" : "k_cgh<fresnel>");
 }
 
+// ------------------------------------------------------------------ adjoint
+// Transposed sum g_j = sum_{h,w} conj(K_j(h,w)) G[h,w], K_j the unit-weight
+// kernel of the forward sum (no a_j, no phi_j): the adjoint of the linear map
+// from the complex point amplitudes c_j = a_j e^{i phi_j} to the hologram.
+// Like the reference's gCghReduction (golcgh.h:147-195) it is parallel over
+// points.  CTA = 256 threads over 256 points: thread t owns points t and
+// t + 128 of its chunk in the two lanes of the paired FP32 pipe, and pixel
+// rows 8 (t / 128) .. +7 of each 16 x 16 subtile, so one warp reads one G
+// value per step (a shared-memory broadcast) for two terms.  Each CTA walks
+// a band of subtiles; per (subtile, point) the phase is anchored at the
+// subtile centre in double-float (prep_sub, as the forward), each pixel adds
+// the local expansion in FP32.  Per-band partial sums go to scratch and
+// k_cgh_adj_reduce adds the bands in a fixed order: deterministic.
+constexpr int ADJ_PTS = 256;
+
+struct AdjParams {
+    CghParams P;       // points, sizes, pitches, lambda (amp / ph0 unused)
+    const float2 *G;   // ny x nx
+    float2 *part;      // bands x n partial sums
+    float2 *g;         // n
+    int bands, nsub_x, nsub;
+};
+
+__device__ __forceinline__ float2 ld_sub_g(const AdjParams &A, int s, int i)
+{
+    const int sy = s / A.nsub_x, sx = s - sy * A.nsub_x;
+    const int h = sy * 16 + (i >> 4), w = sx * 16 + (i & 15);
+    if (s >= A.nsub || h >= A.P.ny || w >= A.P.nx) return make_float2(0.f, 0.f);
+    return __ldg(A.G + (size_t)h * A.P.nx + w);
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_cgh_adj(AdjParams A)
+{
+    __shared__ float2 gs[16][17];
+    const CghParams &P = A.P;
+    const int tid = threadIdx.x;
+    const int chunk = blockIdx.x, band = blockIdx.y;
+    const int pa = tid & 127, lane = tid >> 7;
+    const int ja = chunk * ADJ_PTS + pa, jb = ja + 128;
+    const bool va = ja < P.n, vb = jb < P.n;
+    float xa = 0.f, ya = 0.f, za = 1.f, xb = 0.f, yb = 0.f, zb = 1.f;
+    if (va) { xa = __ldg(P.pts + 3 * ja); ya = __ldg(P.pts + 3 * ja + 1); za = __ldg(P.pts + 3 * ja + 2); }
+    if (vb) { xb = __ldg(P.pts + 3 * jb); yb = __ldg(P.pts + 3 * jb + 1); zb = __ldg(P.pts + 3 * jb + 2); }
+    // subtiles [s0, s1) of this band
+    const int per = (A.nsub + A.bands - 1) / A.bands;
+    const int s0 = band * per, s1 = min(A.nsub, s0 + per);
+    float2 accr = make_float2(0.f, 0.f), acci = make_float2(0.f, 0.f); // (a, b) lanes
+    float2 gnext = s0 < s1 ? ld_sub_g(A, s0, tid) : make_float2(0.f, 0.f);
+    for (int s = s0; s < s1; ++s) {
+        __syncthreads();
+        gs[tid >> 4][tid & 15] = gnext;
+        __syncthreads();
+        if (s + 1 < s1) gnext = ld_sub_g(A, s + 1, tid);
+        const int sy = s / A.nsub_x, sx = s - sy * A.nsub_x;
+        const float wc = (float)(sx * 16) + 7.5f, hc = (float)(sy * 16) + 7.5f;
+        const Sub ra = prep_sub<EXACT>(P, xa, ya, za, va ? 1.f : 0.f, 0.f, wc, hc);
+        const Sub rb = prep_sub<EXACT>(P, xb, yb, zb, vb ? 1.f : 0.f, 0.f, wc, hc);
+        const bool closed = EXACT && (xbound(ra) > SERIES_XMAX || xbound(rb) > SERIES_XMAX);
+        const float2 ax = make_float2(ra.ax, rb.ax), bx = make_float2(ra.bx, rb.bx);
+        for (int r = 0; r < 8; ++r) {
+            const int row = lane * 8 + r;
+            const float dh = (float)row - 7.5f, dh2 = dh * dh;
+            // row part of the expansion: c0 + ay dh + by dh^2 (Fresnel) or ay dh + by dh^2 (exact x)
+            const float2 u = make_float2(fmaf(ra.by, dh2, fmaf(ra.ay, dh, EXACT ? 0.f : ra.c0)),
+                                         fmaf(rb.by, dh2, fmaf(rb.ay, dh, EXACT ? 0.f : rb.c0)));
+#pragma unroll 4
+            for (int c = 0; c < 16; ++c) {
+                const float dw = (float)c - 7.5f;
+                const float2 gv = gs[row][c];
+                const float2 t = __ffma2_rn(bx, f2(dw * dw), __ffma2_rn(ax, f2(dw), u));
+                float2 cyc, amp;
+                if (!EXACT) {
+                    cyc = t;
+                    amp = make_float2(ra.A, rb.A);
+                } else if (!closed) {
+                    cyc = __ffma2_rn(t, __ffma2_rn(t, __ffma2_rn(t, make_float2(ra.h3, rb.h3), make_float2(ra.h2, rb.h2)),
+                                                     make_float2(ra.h1, rb.h1)),
+                                     make_float2(ra.c0, rb.c0));
+                    amp = __ffma2_rn(make_float2(ra.Ah, rb.Ah), t, make_float2(ra.A, rb.A));
+                } else {
+                    const float qa = sqrtf(1.0f + t.x), qb = sqrtf(1.0f + t.y);
+                    cyc = make_float2(fmaf(ra.R, t.x / (1.0f + qa), ra.c0), fmaf(rb.R, t.y / (1.0f + qb), rb.c0));
+                    amp = make_float2(ra.A / qa, rb.A / qb);
+                }
+                const float2 rr = __fadd2_rn(__fadd2_rn(cyc, f2(12582912.0f)), f2(-12582912.0f));
+                const float2 a = __fmul2_rn(__ffma2_rn(rr, f2(-1.0f), cyc), f2(6.283185307179586f));
+                float sa, ca, sb, cb;
+                __sincosf(a.x, &sa, &ca);
+                __sincosf(a.y, &sb, &cb);
+                const float2 cc = __fmul2_rn(amp, make_float2(ca, cb));
+                const float2 ss = __fmul2_rn(amp, make_float2(sa, sb));
+                // conj(amp e^{i a}) * G
+                accr = __ffma2_rn(cc, f2(gv.x), __ffma2_rn(ss, f2(gv.y), accr));
+                acci = __ffma2_rn(cc, f2(gv.y), __ffma2_rn(ss, f2(-gv.x), acci));
+            }
+        }
+    }
+    // add the two row halves (lanes 0 and 1 hold the same points) in a fixed order
+    __shared__ float4 red[128];
+    if (lane == 1) red[pa] = make_float4(accr.x, acci.x, accr.y, acci.y);
+    __syncthreads();
+    if (lane == 0) {
+        const float4 o = red[pa];
+        float2 *dst = A.part + (size_t)band * P.n;
+        if (va) dst[ja] = make_float2(accr.x + o.x, acci.x + o.y);
+        if (vb) dst[jb] = make_float2(accr.y + o.z, acci.y + o.w);
+    }
+}
+
+__global__ void k_cgh_adj_reduce(AdjParams A)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= A.P.n) return;
+    float2 s = A.P.accumulate ? A.g[j] : make_float2(0.f, 0.f);
+    for (int b = 0; b < A.bands; ++b) {
+        const float2 v = A.part[(size_t)b * A.P.n + j];
+        s.x += v.x;
+        s.y += v.y;
+    }
+    A.g[j] = s;
+}
+
+// bands so that chunks x bands fills about 8 waves of the resident CTAs
+static int adj_bands(bool exact, int chunks, int nsub)
+{
+    int dev = 0, nsm = 152, occ = 4;
+    if (cudaGetDevice(&dev) == cudaSuccess) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0) nsm = v;
+        v = 0;
+        const cudaError_t e = exact ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cgh_adj<true>, 256, 0)
+                                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cgh_adj<false>, 256, 0);
+        if (e == cudaSuccess && v > 0) occ = v;
+    }
+    const long target = 8L * nsm * occ;
+    long b = target / chunks;
+    if (b < 1) b = 1;
+    if (b > nsub) b = nsub;
+    return (int)b;
+}
+
+static size_t adj_workspace(int n, int ny, int nx, bool exact, int *bands_out)
+{
+    const int nsub = ((ny + 15) / 16) * ((nx + 15) / 16);
+    const int chunks = (n + ADJ_PTS - 1) / ADJ_PTS;
+    const int bands = adj_bands(exact, chunks > 0 ? chunks : 1, nsub);
+    if (bands_out) *bands_out = bands;
+    return (size_t)bands * (size_t)(n > 0 ? n : 1) * sizeof(float2);
+}
+
+static int cgh_adjoint(bool exact, const float *points, int n, const void *G, void *g, int ny, int nx, double py,
+                       double px, double lambda, int flags, void *work, size_t work_bytes, olg_stream_t stream)
+{
+    if (n < 0 || ny <= 0 || nx <= 0) return fail(OLG_ERR_INVALID_ARG, "bad sizes");
+    if (n > 0 && (!points || !G || !g)) return fail(OLG_ERR_INVALID_ARG, "null pointer");
+    if (((uintptr_t)G & 7) || ((uintptr_t)g & 7)) return fail(OLG_ERR_INVALID_ARG, "G and g must be 8-byte aligned");
+    if (!(px > 0) || !(py > 0) || !(lambda > 0)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (n == 0) return OLG_OK;
+    AdjParams A{};
+    CghParams &P = A.P;
+    P.pts = points; P.n = n; P.ny = ny; P.nx = nx;
+    DF d = split_df(px); P.px_hi = d.hi; P.px_lo = d.lo;
+    d = split_df(py); P.py_hi = d.hi; P.py_lo = d.lo;
+    d = split_df(1.0 / lambda); P.il_hi = d.hi; P.il_lo = d.lo;
+    d = split_df(lambda); P.l_hi = d.hi; P.l_lo = d.lo;
+    P.accumulate = (flags & OLG_ACCUMULATE) ? 1 : 0;
+    A.G = (const float2 *)G;
+    A.g = (float2 *)g;
+    A.nsub_x = (nx + 15) / 16;
+    A.nsub = A.nsub_x * ((ny + 15) / 16);
+    const size_t need = adj_workspace(n, ny, nx, exact, &A.bands);
+    cudaStream_t st = (cudaStream_t)stream;
+    Scratch S;
+    if (int rc = S.acquire(work, work_bytes, need, st)) return rc;
+    A.part = (float2 *)S.ptr;
+    const dim3 grid((n + ADJ_PTS - 1) / ADJ_PTS, A.bands);
+    if (exact) k_cgh_adj<true><<<grid, 256, 0, st>>>(A);
+    else k_cgh_adj<false><<<grid, 256, 0, st>>>(A);
+    count_launch();
+    if (int rc = check_launch(exact ? "k_cgh_adj<exact>" : "k_cgh_adj<fresnel>")) return rc;
+    k_cgh_adj_reduce<<<(n + 255) / 256, 256, 0, st>>>(A);
+    count_launch();
+    return check_launch("k_cgh_adj_reduce");
+}
+
 } // namespace olg
 
 using namespace olg;
+
+extern "C" size_t olg_cgh_adjoint_workspace_bytes(int n_points, int ny, int nx, int exact)
+{
+    if (n_points <= 0 || ny <= 0 || nx <= 0) return 0;
+    return adj_workspace(n_points, ny, nx, exact != 0, nullptr);
+}
+
+extern "C" int olg_cgh_fresnel_adjoint_c64(const float *points, int n_points, const void *G, void *g, int ny, int nx,
+                                           double py, double px, double lambda, int flags, void *work,
+                                           size_t work_bytes, olg_stream_t stream)
+{
+    return cgh_adjoint(false, points, n_points, G, g, ny, nx, py, px, lambda, flags, work, work_bytes, stream);
+}
+
+extern "C" int olg_cgh_exact_adjoint_c64(const float *points, int n_points, const void *G, void *g, int ny, int nx,
+                                         double py, double px, double lambda, int flags, void *work, size_t work_bytes,
+                                         olg_stream_t stream)
+{
+    return cgh_adjoint(true, points, n_points, G, g, ny, nx, py, px, lambda, flags, work, work_bytes, stream);
+}
 
 extern "C" int olg_cgh_fresnel_c64(const float *points, const float *amp, const float *phase0, int n_points, void *U,
                                    float *phase_out, int ny, int nx, double py, double px, double lambda, int flags,

@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <map>
 #include <mutex>
 
 #include "common.cuh"
@@ -375,7 +376,7 @@ namespace {
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::atomic<double> g_tail_weight{1.2};
 std::mutex g_encode_mu;
-int *g_err_flag[64] = {};
+std::map<unsigned long long, int *> g_err_flag; // per context
 
 int get_encode()
 {
@@ -391,11 +392,10 @@ int get_encode()
 
 int err_flag(int **out)
 {
-    int dev = 0;
-    if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-    if (dev < 0 || dev >= 64) return fail(OLG_ERR_INVALID_ARG, "device index out of range");
+    unsigned long long ctx = 0;
+    if (int rc = context_id(&ctx)) return rc;
     std::lock_guard<std::mutex> lk(g_encode_mu);
-    if (!g_err_flag[dev]) {
+    if (!g_err_flag.count(ctx)) {
         int *f = nullptr;
         cudaError_t e = cudaMalloc(&f, sizeof(int));
         if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (error flag)");
@@ -404,9 +404,9 @@ int err_flag(int **out)
             cudaFree(f);
             return cuda_fail(e, "cudaMemset (error flag)");
         }
-        g_err_flag[dev] = f;
+        g_err_flag[ctx] = f;
     }
-    *out = g_err_flag[dev];
+    *out = g_err_flag[ctx];
     return OLG_OK;
 }
 
@@ -499,23 +499,27 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
     P.tiles = (int)tiles;
     P.U = (float2 *)U;
     P.err = err;
-    // per device, once: the shared-memory opt-in and the SM count
-    static std::atomic<int> sm_count[64];
-    int dev = 0;
-    if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-    if (dev < 0 || dev >= 64) return fail(OLG_ERR_INVALID_ARG, "device index out of range");
-    if (!sm_count[dev]) {
+    // per context, once: the shared-memory opt-in and the SM count
+    static std::map<unsigned long long, int> sm_count;
+    unsigned long long ctx = 0;
+    if (int rc = context_id(&ctx)) return rc;
+    int nsm = 0;
+    {
         std::lock_guard<std::mutex> lk(g_encode_mu);
-        if (!sm_count[dev]) {
-            cudaError_t e = cudaFuncSetAttribute(k_cgh_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM);
+        auto it = sm_count.find(ctx);
+        if (it == sm_count.end()) {
+            int dev = 0;
+            cudaError_t e = cudaGetDevice(&dev);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+            e = cudaFuncSetAttribute(k_cgh_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM);
             if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm)");
             int n = 0;
             e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(SM count)");
-            sm_count[dev] = n;
+            it = sm_count.emplace(ctx, n).first;
         }
+        nsm = it->second;
     }
-    const int nsm = sm_count[dev];
     const double tw = g_tail_weight.load(std::memory_order_relaxed);
     // SMs left over after one CTA per tile (one CTA per SM: ~197 KB of shared
     // memory) take the K tails: with e extra CTAs each holds `per` tails.  A

@@ -2,9 +2,11 @@
 // messages, launch counter, stream-ordered scratch.
 #include <atomic>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <string>
 
-#include <mutex>
+#include <cuda.h>
 
 #include "common.cuh"
 
@@ -12,6 +14,10 @@ namespace olg {
 
 static thread_local std::string t_err;
 static std::atomic<unsigned long long> g_launches{0};
+static std::atomic<long long> g_wait_budget{4000000000LL};
+static std::atomic<int> g_fail_allocs{0};
+
+long long wait_budget_cycles() { return g_wait_budget.load(std::memory_order_relaxed); }
 
 void set_error(const std::string &msg) { t_err = msg; }
 
@@ -35,33 +41,75 @@ int check_launch(const char *what)
 
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+namespace {
+using PFN_ctx_current = CUresult (*)(CUcontext *);
+using PFN_ctx_id = CUresult (*)(CUcontext, unsigned long long *);
+std::once_flag g_ctx_once;
+PFN_ctx_current g_ctx_current = nullptr;
+PFN_ctx_id g_ctx_id = nullptr;
+
+void load_ctx_entry_points()
+{
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        g_ctx_current = (PFN_ctx_current)fn;
+    fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        g_ctx_id = (PFN_ctx_id)fn;
+}
+} // namespace
+
+int context_id(unsigned long long *id)
+{
+    std::call_once(g_ctx_once, load_ctx_entry_points);
+    if (!g_ctx_current || !g_ctx_id) return fail(OLG_ERR_CUDA, "cuCtxGetCurrent / cuCtxGetId unavailable");
+    CUcontext c = nullptr;
+    if (g_ctx_current(&c) != CUDA_SUCCESS) return fail(OLG_ERR_CUDA, "cuCtxGetCurrent failed");
+    if (!c) {
+        // no context current on this thread yet: let the runtime make the
+        // current device's primary context current
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaSetDevice(dev);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+        if (g_ctx_current(&c) != CUDA_SUCCESS || !c) return fail(OLG_ERR_CUDA, "no current CUDA context");
+    }
+    if (g_ctx_id(c, id) != CUDA_SUCCESS) return fail(OLG_ERR_CUDA, "cuCtxGetId failed");
+    return OLG_OK;
+}
+
 // The library's own stream-ordered pool per device.  It keeps up to 8 GiB of
 // freed scratch mapped between calls: the default pool returns everything at
 // each synchronisation, and re-mapping a few hundred MB per call (the WRP pair
 // lists) cost more than the kernels that use it.  Leaves the device's default
 // pool untouched.
+// Pools are keyed on the context (a reset device gets a new pool).
 static cudaMemPool_t scratch_pool()
 {
     static std::mutex mu;
-    static cudaMemPool_t pools[64] = {};
+    static std::map<unsigned long long, cudaMemPool_t> pools;
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    unsigned long long ctx = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || context_id(&ctx) != OLG_OK) return nullptr;
     std::lock_guard<std::mutex> lk(mu);
-    if (!pools[dev]) {
-        cudaMemPoolProps props{};
-        props.allocType = cudaMemAllocationTypePinned;
-        props.location.type = cudaMemLocationTypeDevice;
-        props.location.id = dev;
-        cudaMemPool_t p = nullptr;
-        if (cudaMemPoolCreate(&p, &props) == cudaSuccess) {
-            unsigned long long keep = 8ull << 30;
-            cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
-            pools[dev] = p;
-        } else if (cudaDeviceGetDefaultMemPool(&p, dev) == cudaSuccess) {
-            pools[dev] = p;
-        }
+    auto it = pools.find(ctx);
+    if (it != pools.end()) return it->second;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) == cudaSuccess) {
+        unsigned long long keep = 8ull << 30;
+        cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    } else if (cudaDeviceGetDefaultMemPool(&p, dev) != cudaSuccess) {
+        return nullptr;
     }
-    return pools[dev];
+    pools.emplace(ctx, p);
+    return p;
 }
 
 int Scratch::acquire(void *work, size_t work_bytes, size_t need, cudaStream_t s)
@@ -75,7 +123,16 @@ int Scratch::acquire(void *work, size_t work_bytes, size_t need, cudaStream_t s)
         owned = false;
         return OLG_OK;
     }
-    cudaError_t e = cudaMallocFromPoolAsync(&ptr, need, scratch_pool(), s);
+    // host-side fault injection (olg_inject_alloc_failures): fail this
+    // allocation as an out-of-memory would, before touching the device
+    for (int k = g_fail_allocs.load(); k > 0;)
+        if (g_fail_allocs.compare_exchange_weak(k, k - 1)) {
+            ptr = nullptr;
+            return fail(OLG_ERR_NOMEM, "injected allocation failure (olg_inject_alloc_failures)");
+        }
+    cudaMemPool_t pool = scratch_pool();
+    if (!pool) return fail(OLG_ERR_CUDA, std::string("no scratch memory pool: ") + t_err);
+    cudaError_t e = cudaMallocFromPoolAsync(&ptr, need, pool, s);
     if (e != cudaSuccess) {
         ptr = nullptr;
         return cuda_fail(e, "cudaMallocFromPoolAsync (scratch)");
@@ -110,6 +167,17 @@ extern "C" const char *olg_status_string(int status)
 extern "C" const char *olg_last_error(void) { return olg::t_err.c_str(); }
 
 extern "C" unsigned long long olg_launch_count(void) { return olg::g_launches.load(); }
+
+extern "C" long long olg_wait_budget_cycles(long long cycles)
+{
+    if (cycles > 0) return olg::g_wait_budget.exchange(cycles);
+    return olg::g_wait_budget.load();
+}
+
+extern "C" int olg_inject_alloc_failures(int n)
+{
+    return olg::g_fail_allocs.exchange(n > 0 ? n : 0);
+}
 
 extern "C" int olg_host_device_pointer(const void *host, void **dev)
 {

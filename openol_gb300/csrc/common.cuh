@@ -18,6 +18,19 @@ void count_launch(unsigned n = 1);
 // Check the last launch; returns OLG_OK or OLG_ERR_CUDA with a message.
 int check_launch(const char *what);
 
+// Identifier of the calling thread's current CUDA context (the runtime's
+// primary context of the current device, made current if none is).  Ids are
+// unique over the process: a context destroyed by cudaDeviceReset and created
+// again gets a new one.  Host-side caches of device state (uploaded tables,
+// symbol addresses, allocations, function attributes) are keyed on it, so a
+// re-created context never inherits pointers or "already done" flags that
+// belonged to its predecessor.
+int context_id(unsigned long long *id);
+
+// Budget of one bounded device-side wait, in SM clock cycles (default 4e9,
+// about 2 s at 2 GHz); olg_wait_budget_cycles sets it.
+long long wait_budget_cycles();
+
 // Stream-ordered scratch: caller memory when given, else cudaMallocAsync.
 struct Scratch {
     void *ptr = nullptr;

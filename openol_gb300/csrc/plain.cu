@@ -139,14 +139,14 @@ struct Plan {
     float2 *b1 = nullptr, *b2 = nullptr;
 };
 std::mutex g_mu;
-std::map<std::pair<int, std::pair<int, int>>, Plan> g_plans;
+std::map<std::pair<unsigned long long, std::pair<int, int>>, Plan> g_plans; // (context, (ny, nx))
 
 int get_plan(int ny, int nx, Plan **out)
 {
-    int dev = 0;
-    if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    unsigned long long ctx = 0;
+    if (int rc = context_id(&ctx)) return rc;
     std::lock_guard<std::mutex> lk(g_mu);
-    auto key = std::make_pair(dev, std::make_pair(ny, nx));
+    auto key = std::make_pair(ctx, std::make_pair(ny, nx));
     auto it = g_plans.find(key);
     if (it == g_plans.end()) {
         Plan p;

@@ -292,15 +292,15 @@ __global__ void __launch_bounds__(MR_NT, 1) k_tilt_cols_inv(TiltArgs T, MrPlan p
 namespace {
 
 std::mutex g_mr_mu;
-std::map<std::pair<int, int>, float2 *> g_mr_tw; // (device, N) -> exp(-2 pi i m / N)
+std::map<std::pair<unsigned long long, int>, float2 *> g_mr_tw; // (context, N) -> exp(-2 pi i m / N)
 
 int mr_table(int N, const float2 **out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    unsigned long long ctx = 0;
+    if (int rc = context_id(&ctx)) return rc;
+    cudaError_t e = cudaSuccess;
     std::lock_guard<std::mutex> lk(g_mr_mu);
-    auto it = g_mr_tw.find({dev, N});
+    auto it = g_mr_tw.find({ctx, N});
     if (it == g_mr_tw.end()) {
         std::vector<float2> t(N);
         for (int m = 0; m < N; ++m) {
@@ -315,7 +315,7 @@ int mr_table(int N, const float2 **out)
             cudaFree(d);
             return cuda_fail(e, "twiddle table upload");
         }
-        it = g_mr_tw.emplace(std::make_pair(dev, N), d).first;
+        it = g_mr_tw.emplace(std::make_pair(ctx, N), d).first;
     }
     *out = it->second;
     return OLG_OK;

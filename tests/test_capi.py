@@ -114,6 +114,32 @@ def test_wrp_plane_z():
             assert np.float32(got) == _plane_z_ref(window, ny, nx, p, p, lam, zmin, s)
 
 
+def test_fault_knobs_without_gpu():
+    """The wait budget and the injected allocation failures are host state."""
+    L = _lib.lib()
+    b = L.olg_wait_budget_cycles(0)
+    assert b == 4000000000
+    assert L.olg_wait_budget_cycles(12345) == b and L.olg_wait_budget_cycles(0) == 12345
+    assert L.olg_wait_budget_cycles(b) == 12345
+    assert L.olg_inject_alloc_failures(2) == 0
+    assert L.olg_inject_alloc_failures(-3) == 2   # negative counts clear
+    assert L.olg_inject_alloc_failures(0) == 0
+    assert L.olg_batch_plan_raise_target(None, 0, 0, 1) == -1
+
+
+def test_cgh_adjoint_validation_without_gpu():
+    L = _lib.lib()
+    buf = (C.c_char * 64)()
+    base = (C.addressof(buf) + 15) // 16 * 16
+    adj = L.olg_cgh_fresnel_adjoint_c64
+    assert adj(base, -1, base, base, 8, 8, 8e-6, 8e-6, 532e-9, 0, None, 0, None) == -1   # bad point count
+    assert adj(None, 5, base, base, 8, 8, 8e-6, 8e-6, 532e-9, 0, None, 0, None) == -1    # null points
+    assert adj(base, 5, base + 4, base, 8, 8, 8e-6, 8e-6, 532e-9, 0, None, 0, None) == -1  # misaligned G
+    assert L.olg_cgh_exact_adjoint_c64(base, 5, base, base, 8, 8, 8e-6, 0.0, 532e-9, 0, None, 0, None) == -1
+    assert adj(base, 0, base, base, 8, 8, 8e-6, 8e-6, 532e-9, 0, None, 0, None) == 0     # nothing to do
+    assert L.olg_cgh_adjoint_workspace_bytes(0, 8, 8, 0) == 0
+
+
 def test_argument_validation_without_gpu():
     L = _lib.lib()
     # rejected before any device work

@@ -23,7 +23,9 @@ def _noalloc(u_in, u_out, dy, dx, lam, z, flags=0):
                                                torch.cuda.current_stream().cuda_stream)
 
 
-@pytest.mark.parametrize("shape,z", [((1024, 1024), 0.05), ((256, 512), -0.03)])
+# 256 x 4096 has the widest padded rows, hence the largest scratch layout
+# (about 16.1 of the 17 MiB)
+@pytest.mark.parametrize("shape,z", [((1024, 1024), 0.05), ((256, 512), -0.03), ((256, 4096), 0.02)])
 def test_noalloc_matches_allocating_entry_point(shape, z):
     rng = np.random.default_rng(shape[0] + shape[1])
     u0 = ((rng.random(shape) < 0.5) * np.exp(2j * np.pi * rng.random(shape))).astype(np.complex64)
@@ -48,3 +50,13 @@ def test_noalloc_rejects_fields_beyond_its_scratch():
     rc = _noalloc(big, big, 8e-6, 8e-6, 532e-9, 0.05)
     assert rc == -4  # OLG_ERR_WORKSPACE
     assert b"1048576" in _lib.lib().olg_last_error()
+
+
+def test_noalloc_rejects_mixed_radix_sizes():
+    """24 x 40 is a valid size for olg_asm_prop_c64 (mixed-radix passes), but
+    those passes build a twiddle table on first use, so the allocation-free
+    entry point takes power-of-two sizes only."""
+    u = torch.zeros((24, 40), dtype=torch.complex64, device="cuda")
+    rc = _noalloc(u, u, 8e-6, 8e-6, 532e-9, 0.05)
+    assert rc == -2  # OLG_ERR_UNSUPPORTED_SIZE
+    assert b"power-of-two" in _lib.lib().olg_last_error()
