@@ -351,6 +351,11 @@ int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, const float 
  * one of their K blocks relative to a tile CTA's (default 1.2; 0 turns the
  * split off).  Sets w when 0 <= w <= 16 and returns the previous value. */
 double olg_cgh_gemm_tail_weight(double w);
+/* Autotuner of that split (project-written; the reference has none): times
+ * the GEMM for an n_points x ny x nx hologram at a few tail weights (0, 1.0 ..
+ * 1.6; operands built once and reused, L2 flushed before every timed GEMM;
+ * synchronises `stream`) and keeps the fastest for the rest of the process. */
+int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg_stream_t stream);
 /* Synchronises the device and reports (OLG_ERR_CUDA) whether any tensor-core
  * kernel of this library gave up on a bounded wait; clear != 0 resets the flag. */
 int olg_device_fault_check(int clear);

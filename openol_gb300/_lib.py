@@ -74,6 +74,7 @@ SIGNATURES = {
     "olg_cgh_exact_c64": (_i, [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d, _i, _p]),
     "olg_cgh_adjoint_workspace_bytes": (_sz, [_i, _i, _i, _i]),
     "olg_wait_budget_cycles": (C.c_longlong, [C.c_longlong]),
+    "olg_autotune_cgh_gemm": (_i, [_i, _i, _i, _i, _p]),
     "olg_inject_alloc_failures": (_i, [_i]),
     "olg_batch_plan_raise_target": (_i, [_p, _i, _i, _i]),
     "olg_cgh_fresnel_adjoint_c64": (_i, [_p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),

@@ -109,6 +109,13 @@ def cgh_fresnel_gemm(gobj, U, *, ny, nx, py, px, lam, amp=None, phase0=None, acc
     return U
 
 
+def autotune_cgh_gemm(n_points, ny, nx, reps=5, stream=None):
+    """Time the GEMM's K-tail split for this hologram shape (olg_autotune_cgh_gemm)
+    and keep the fastest; returns the chosen tail weight."""
+    call("olg_autotune_cgh_gemm", int(n_points), int(ny), int(nx), int(reps), _stream(stream))
+    return float(lib().olg_cgh_gemm_tail_weight(-1.0))
+
+
 def cgh_gemm_workspace(n_points, ny, nx, device="cuda"):
     return torch.empty(int(lib().olg_cgh_gemm_workspace_bytes(n_points, ny, nx)), dtype=torch.uint8, device=device)
 

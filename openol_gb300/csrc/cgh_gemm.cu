@@ -33,6 +33,7 @@
 #include <cmath>
 #include <map>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "tc.cuh"
@@ -553,6 +554,81 @@ extern "C" double olg_cgh_gemm_tail_weight(double w)
 {
     if (w >= 0.0 && w <= 16.0) return g_tail_weight.exchange(w);
     return g_tail_weight.load();
+}
+
+// Times the GEMM on the caller's hologram shape and point count for a few
+// K-tail weights (the work split between tile CTAs and the spare SMs' tail
+// CTAs) and keeps the fastest.  Operands are built once (a unit-amplitude
+// cloud spread over the hologram at 0.1 m; the split depends on the shape,
+// not on the values) and reused; every timed GEMM starts from a cold L2.
+extern "C" int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg_stream_t stream)
+{
+    if (n_points <= 0 || ny <= 0 || nx <= 0 || ny > 4096 || nx > 4096)
+        return fail(OLG_ERR_INVALID_ARG, "autotuning needs n_points > 0 and ny, nx in [1, 4096]");
+    if (reps < 1) reps = 5;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t wb = olg_cgh_gemm_workspace_bytes(n_points, ny, nx);
+    Scratch ws, pts, U, flush;
+    if (int rc = ws.acquire(nullptr, 0, wb, st)) return rc;
+    if (int rc = pts.acquire(nullptr, 0, sizeof(float) * 3 * (size_t)n_points, st)) return rc;
+    if (int rc = U.acquire(nullptr, 0, sizeof(float2) * (size_t)ny * nx, st)) return rc;
+    const size_t flush_bytes = (size_t)256 << 20;
+    if (int rc = flush.acquire(nullptr, 0, flush_bytes, st)) return rc;
+    std::vector<float> h(3 * (size_t)n_points);
+    for (int j = 0; j < n_points; ++j) {
+        h[3 * j] = (float)(8e-6 * nx * ((j * 0.6180339887) - std::floor(j * 0.6180339887)));
+        h[3 * j + 1] = (float)(8e-6 * ny * ((j * 0.7548776662) - std::floor(j * 0.7548776662)));
+        h[3 * j + 2] = (float)(0.1 + 1e-3 * ((j * 0.5698402910) - std::floor(j * 0.5698402910)));
+    }
+    cudaError_t e = cudaMemcpyAsync(pts.ptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (autotune points)");
+    const double keep = g_tail_weight.load();
+    auto run = [&](int flags) {
+        return olg_cgh_fresnel_gemm_c64((const float *)pts.ptr, nullptr, nullptr, n_points, U.ptr, ny, nx, 8e-6,
+                                        8e-6, 532e-9, flags, ws.ptr, wb, stream);
+    };
+    if (int rc = run(0)) return rc; // builds the operands
+    struct Events {
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~Events()
+        {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } ev;
+    if ((e = cudaEventCreate(&ev.a)) != cudaSuccess || (e = cudaEventCreate(&ev.b)) != cudaSuccess)
+        return cuda_fail(e, "cudaEventCreate");
+    const double cand[] = {0.0, 1.0, 1.1, 1.2, 1.3, 1.45, 1.6};
+    double best_w = keep;
+    float best = 1e30f;
+    for (double w : cand) {
+        g_tail_weight.store(w);
+        float tot = 0.f;
+        for (int r = 0; r < reps; ++r) {
+            if ((e = cudaMemsetAsync(flush.ptr, r & 0xff, flush_bytes, st)) != cudaSuccess ||
+                (e = cudaEventRecord(ev.a, st)) != cudaSuccess) {
+                g_tail_weight.store(keep);
+                return cuda_fail(e, "autotune timing");
+            }
+            if (int rc = run(OLG_REUSE_OPERANDS)) {
+                g_tail_weight.store(keep);
+                return rc;
+            }
+            float t = 0.f;
+            if ((e = cudaEventRecord(ev.b, st)) != cudaSuccess || (e = cudaEventSynchronize(ev.b)) != cudaSuccess ||
+                (e = cudaEventElapsedTime(&t, ev.a, ev.b)) != cudaSuccess) {
+                g_tail_weight.store(keep);
+                return cuda_fail(e, "autotune timing");
+            }
+            tot += t;
+        }
+        if (tot < best) {
+            best = tot;
+            best_w = w;
+        }
+    }
+    g_tail_weight.store(best_w);
+    return OLG_OK;
 }
 
 extern "C" int olg_device_fault_check(int clear)

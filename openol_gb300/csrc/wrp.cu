@@ -189,22 +189,46 @@ __global__ void __launch_bounds__(WNT) k_wrp_tile(WrpParams P)
             const float lim = b.z * 1.0001f;
             const bool reach = WIN == 0 ? ex * ex + ey * ey <= lim : (2.f * ex <= lim && 2.f * ey <= lim);
             if (!reach) continue;
+            // warp-uniform: does the window hold the whole strip, with a 1e-4
+            // relative margin over the float rounding of the per-pixel test?
+            // Then every pixel's test is true and none is evaluated.
+            const float fx = fmaxf(fabsf(xl - b.x), fabsf(xr - b.x)), fy = fmaxf(fabsf(yl - b.y), fabsf(yr - b.y));
+            const float inner = b.z * 0.9999f;
+            const bool full = WIN == 0 ? fx * fx + fy * fy <= inner : (2.f * fx <= inner && 2.f * fy <= inner);
             const float4 a = cst[i][0];
+            const float base = fmaf(a.y, dw, a.x);
+            if (full) {
+#pragma unroll
+                for (int pr = 0; pr < 2; ++pr) {
+                    const float2 cyc = __ffma2_rn(f2(a.z), dhp[pr], __ffma2_rn(f2(a.w), q2p[pr], f2(base)));
+                    const float2 r = __fadd2_rn(__fadd2_rn(cyc, f2(12582912.0f)), f2(-12582912.0f));
+                    const float2 ang = __fmul2_rn(__ffma2_rn(r, f2(-1.0f), cyc), f2(6.283185307179586f));
+                    float sa, ca, sb, cb;
+                    __sincosf(ang.x, &sa, &ca);
+                    __sincosf(ang.y, &sb, &cb);
+                    part[2 * pr] = __ffma2_rn(f2(b.w), make_float2(ca, sa), part[2 * pr]);
+                    part[2 * pr + 1] = __ffma2_rn(f2(b.w), make_float2(cb, sb), part[2 * pr + 1]);
+                }
+                continue;
+            }
             const float ddx = __fsub_rn(pw, b.x);
             const float ddx2 = __fmul_rn(ddx, ddx);
             const bool xin = __fmul_rn(fabsf(ddx), 2.0f) <= b.z;
-            const float base = fmaf(a.y, dw, a.x);
 #pragma unroll
             for (int pr = 0; pr < 2; ++pr) {
-                // the window test in scalar rounded operations (never contracted)
-                const float dya = __fsub_rn(php[pr].x, b.y), dyb = __fsub_rn(php[pr].y, b.y);
+                // the window test on the paired pipe, each operation rounded
+                // separately (the _rn intrinsics are never contracted), so each
+                // lane decides as the reference's float code does
+                const float2 dy = __fadd2_rn(php[pr], f2(-b.y));
                 bool in0, in1;
                 if (WIN == 0) {
-                    in0 = __fadd_rn(ddx2, __fmul_rn(dya, dya)) < b.z;
-                    in1 = __fadd_rn(ddx2, __fmul_rn(dyb, dyb)) < b.z;
+                    const float2 t = __fadd2_rn(f2(ddx2), __fmul2_rn(dy, dy));
+                    in0 = t.x < b.z;
+                    in1 = t.y < b.z;
                 } else {
-                    in0 = xin && __fmul_rn(fabsf(dya), 2.0f) <= b.z;
-                    in1 = xin && __fmul_rn(fabsf(dyb), 2.0f) <= b.z;
+                    const float2 ay = __fmul2_rn(make_float2(fabsf(dy.x), fabsf(dy.y)), f2(2.0f));
+                    in0 = xin && ay.x <= b.z;
+                    in1 = xin && ay.y <= b.z;
                 }
                 if (!__any_sync(0xffffffffu, in0 || in1)) continue;
                 const float wa = in0 ? b.w : 0.f, wb = in1 ? b.w : 0.f;
