@@ -20,6 +20,12 @@
 //   ref_gpu_harness wrp PTS OUT n ny nx p lambda plane_z window plimit
 //       window 0: WRPStep1 (golcgh.h:369-389), 1: WRPStep1_D (golcgh.h:470-491);
 //       plimit > 0 selects the p_limit overloads.
+//   ref_gpu_harness time-asm|time-fresnel|time-arss ny nx p lambda z reps
+//   ref_gpu_harness time-cgh ny nx n p lambda reps
+//   ref_gpu_harness time-wrp N n p lambda reps
+//       the reference's own gAsmProp / gFresnelProp / ARSSFresnelProp (s = 0.5),
+//       gCgh (gCghShared) and WRPMethod timed on the GPU (mean ms per call).
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -31,11 +37,12 @@
 
 // golclass.h names std:: inside its own namespace `cuda`; it must come before
 // any header that declares cuda::std (thrust, libcu++), or those names bind
-// to cuda::std.  golcgh.h includes it first; golprop.h pulls in thrust and
-// uses the CPU transfer functions of olprop.h.
-#include "golcgh.h"
+// to cuda::std.  golprop.h pulls in thrust and uses the CPU transfer
+// functions of olprop.h; golcgh.h's WRPStep2 calls golprop.h's templates.
+#include "golclass.h"
 #include "olprop.h"
 #include "golprop.h"
+#include "golcgh.h"
 
 namespace {
 
@@ -139,6 +146,112 @@ int run_wrp(int argc, char **argv)
     return dump(U, (size_t)ny * nx, out) ? 0 : 5;
 }
 
+// ---------------------------------------------------------------- timing
+// The reference's own GPU calls on the GPU they run on, for comparison with
+// this project's kernels on the same GB300.  Each mode prints one line
+// "<mode> <mean ms per call> <calls>"; every call is the reference's full
+// wrapper (its allocations, plans and synchronisations included), timed with
+// CUDA events after two untimed calls.
+struct Lcg {
+    unsigned long long s;
+    float next() { s = s * 6364136223846793005ULL + 1442695040888963407ULL; return (float)((s >> 40) * (1.0 / 16777216.0)); }
+};
+
+template <typename F>
+double time_calls(int reps, F &&fn)
+{
+    fn();
+    fn();
+    cudaDeviceSynchronize();
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a);
+    for (int r = 0; r < reps; ++r) fn();
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms / reps;
+}
+
+cuda::unique_ptr<cf[]> random_field(int ny, int nx, unsigned long long seed)
+{
+    Lcg g{seed};
+    std::vector<cf> h((size_t)ny * nx);
+    for (auto &v : h) {
+        const float a = g.next() < 0.5f ? 1.f : 0.f, ph = 6.2831853f * g.next();
+        v = cf(a * std::cos(ph), a * std::sin(ph));
+    }
+    auto d = cuda::make_unique<cf[]>(h.size());
+    upload(d, h);
+    return d;
+}
+
+// point cloud: n points uniform in a box of edge `box` centred at
+// (cx, cy, cz), or, with depth > 0, uniform over [cx +- box/2] x [cy +- box/2]
+// x [cz, cz + depth]
+ol::gObject<float> cloud(int n, float cx, float cy, float cz, float box, float depth, unsigned long long seed)
+{
+    Lcg g{seed};
+    ol::Object<float> o(n);
+    for (int j = 0; j < n; ++j) {
+        const float x = cx + (g.next() - 0.5f) * box, y = cy + (g.next() - 0.5f) * box;
+        const float z = depth > 0 ? cz + g.next() * depth : cz + (g.next() - 0.5f) * box;
+        o[j] = ol::Vect3<float>(x, y, z);
+    }
+    return ol::Object2cuda<float>(o);
+}
+
+int run_time(int argc, char **argv)
+{
+    const std::string mode = argv[1];
+    if (mode == "time-asm" || mode == "time-fresnel" || mode == "time-arss") {
+        // ny nx p lambda z reps
+        if (argc != 8) return 2;
+        const int ny = std::atoi(argv[2]), nx = std::atoi(argv[3]), reps = std::atoi(argv[7]);
+        const float p = std::strtof(argv[4], nullptr), lam = std::strtof(argv[5], nullptr);
+        const float z = std::strtof(argv[6], nullptr);
+        if (ny < 16 || nx < 16 || ny > 4096 || nx > 4096 || reps < 1) return 2;
+        auto u = random_field(ny, nx, 7);
+        auto v = cuda::make_unique<cf[]>((size_t)ny * nx);
+        double ms;
+        if (mode == "time-asm") ms = time_calls(reps, [&] { ol::gAsmProp(u, ny, nx, p, p, lam, z); });
+        else if (mode == "time-fresnel") ms = time_calls(reps, [&] { ol::gFresnelProp(u, ny, nx, p, p, lam, z); });
+        else ms = time_calls(reps, [&] { ol::ARSSFresnelProp(u, v, ny, nx, p, p, lam, z, 0.5f); });
+        std::printf("%s %.6f %d\n", mode.c_str(), ms, reps);
+        return cudaDeviceSynchronize() == cudaSuccess ? 0 : 6;
+    }
+    if (mode == "time-cgh") {
+        // ny nx n p lambda reps: the points in a 5 mm box at z = 100 mm over the hologram centre
+        if (argc != 8) return 2;
+        const int ny = std::atoi(argv[2]), nx = std::atoi(argv[3]), n = std::atoi(argv[4]), reps = std::atoi(argv[7]);
+        const float p = std::strtof(argv[5], nullptr), lam = std::strtof(argv[6], nullptr);
+        if (ny < 1 || nx < 1 || ny > 8192 || nx > 8192 || n < 1 || n > 10000000 || reps < 1) return 2;
+        auto obj = cloud(n, nx / 2 * p, ny / 2 * p, 0.1f, 5e-3f, 0.f, 11);
+        auto U = cuda::make_unique<cf[]>((size_t)ny * nx);
+        const double ms = time_calls(reps, [&] { ol::gCgh(obj, U, ny, nx, p, lam); });
+        std::printf("%s %.6f %d\n", mode.c_str(), ms, reps);
+        return cudaDeviceSynchronize() == cudaSuccess ? 0 : 6;
+    }
+    if (mode == "time-wrp") {
+        // N n p lambda reps: n points over 10 x 10 mm, 1..5 mm behind zmin, WRPMethod (plane 0.9 zmin)
+        if (argc != 7) return 2;
+        const int N = std::atoi(argv[2]), n = std::atoi(argv[3]), reps = std::atoi(argv[6]);
+        const float p = std::strtof(argv[4], nullptr), lam = std::strtof(argv[5], nullptr);
+        if (N < 16 || N > 4096 || n < 1 || n > 10000000 || reps < 1) return 2;
+        const float zmin = 0.15f;
+        auto obj = cloud(n, N / 2 * p, N / 2 * p, zmin + 1e-3f, 10e-3f, 4e-3f, 13);
+        auto U = cuda::make_unique<cf[]>((size_t)N * N);
+        const double ms = time_calls(reps, [&] { ol::WRPMethod(obj, U, N, N, p, lam, zmin); });
+        std::printf("%s %.6f %d\n", mode.c_str(), ms, reps);
+        return cudaDeviceSynchronize() == cudaSuccess ? 0 : 6;
+    }
+    return 2;
+}
+
 } // namespace
 
 int main(int argc, char **argv)
@@ -150,6 +263,7 @@ int main(int argc, char **argv)
     int rc = 2;
     if (!std::strcmp(argv[1], "arss")) rc = run_arss(argc, argv);
     else if (!std::strcmp(argv[1], "wrp")) rc = run_wrp(argc, argv);
+    else if (!std::strncmp(argv[1], "time-", 5)) rc = run_time(argc, argv);
     if (rc) std::fprintf(stderr, "ref_gpu_harness %s: status %d\n", argv[1], rc);
     return rc;
 }
