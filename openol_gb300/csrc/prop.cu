@@ -347,14 +347,18 @@ int setup_arss(const void *u_src, void *u_dst, int ny, int nx, double dy, double
     if (int rc = mr_prepare(P)) return rc;
     const int NX = 2 * nx, NY = 2 * ny;
     const double np = (double)NX * (double)NY;
-    // windows, golprop.h:849-852, 891-892, 928-931 (-1: none)
+    // windows, golprop.h:849-852, 891-892, 928-931 (-1: none).  A computed
+    // limit <= 0 is an empty window (the reference's |m| >= lim then holds for
+    // every m; s < 0 makes the pre-chirp limits negative), so limits are
+    // clamped at 0 and never reach the "none" value.
     int hlim_u = -1, wlim_u = -1, lim_h = -1, hlim_c = -1, wlim_c = -1;
     if (windows) {
-        hlim_u = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dy)) / dy);
-        wlim_u = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dx)) / dx);
-        lim_h = (int)floor_lim(std::fabs(lambda * z * 0.5 / (dx * s)) / dx);
-        hlim_c = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dy)) / dy);
-        wlim_c = (int)floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dx)) / dx);
+        auto win = [](long v) { return (int)std::max(v, 0L); };
+        hlim_u = win(floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dy)) / dy));
+        wlim_u = win(floor_lim((lambda * std::fabs(z) * 0.5 / (s * std::fabs(s - 1) * dx)) / dx));
+        lim_h = win(floor_lim(std::fabs(lambda * z * 0.5 / (dx * s)) / dx));
+        hlim_c = win(floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dy)) / dy));
+        wlim_c = win(floor_lim((lambda * std::fabs(z) * 0.5 / (std::fabs(1 - s) * dx)) / dx));
     }
     const bool adj = (flags & OLG_CONJ) != 0;
     const double lz2 = 2.0 * lambda * z;
