@@ -106,7 +106,13 @@ __device__ __forceinline__ float2 asm_tf(const PropParams &P, int fx, int fy)
 {
     const float fx2 = (float)(fx * fx), fy2 = (float)(fy * fy);
     const float t = P.tx * fx2 + P.ty * fy2;
-    const float s = sqrtf(1.0f - t);
+    // s enters only through q = t / (1 + s), so its relative error reaches the
+    // phase scaled by t / (1 + s) ~ 1e-2: the approximate square root (about
+    // 1 ulp) moves the phase by < 1e-6 cycles at z / lambda ~ 3e5, where the
+    // correctly rounded sqrtf costs a multi-instruction sequence per element.
+    // A negative argument (evanescent t > 1) still gives NaN.
+    float s;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(s) : "f"(1.0f - t));
     const float q = __fdividef(t, 1.0f + s); // 1 + s in [1, 2]: the fast divide is within 2 ulp
     const float g = 0.5f * q * q;
     float cyc = P.c0 - frac_mul(P.ax_hi, P.ax_lo, fx2) - frac_mul(P.ay_hi, P.ay_lo, fy2) - P.zl * g;
