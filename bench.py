@@ -62,6 +62,22 @@ TILT_DESC = ("tilt 1024x1024 padded 2048x2048, p=8um, lambda=532nm, z=50mm, Tilt
 ADAM = dict(n=2048, p=6.4e-6, lam=532e-9, planes=8, z0=0.08, dz=0.01, lr=0.05, seed=20261203 + 4)
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# kernels each roofline covers, from ncu captures of this bench's own timed
+# region (--ncu-range); the profile file named beside each holds the command.
+TRAFFIC = {
+    "cgh": (544.8e6 + 17.4e6, "k_cgh_gemm, profiles/cgh_gemm_1920x1080_10k.md"),
+    "asm": ((8.5 + 16.9 + 16.8) * 1e6, "the three passes, profiles/asm_1024_kernels.md (S stays in L2)"),
+    "wrp": ((134.3 + 204.7 + 268.6 + 211.7 + 268.6 + 99.8) * 1e6,
+            "the three 8192-point passes of step 2, profiles/asm_4096_to_8192_wrp_step2.md"),
+}
+
+
+def traffic(name):
+    t = TRAFFIC.get(name)
+    return (t[0], t[1]) if t else (None, None)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -499,7 +515,8 @@ def wl_cgh(x, K, W, cpu):
                 "d2h_bytes_per_step": c["ny"] * c["nx"] * 8},
         "gpu_launches": int(launches),
         "roofline": {"bound": "tensor", "achieved": ach_tf, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                     "frac": ach_tf / pk["bf16_tflops"], "traffic": None,
+                     "frac": ach_tf / pk["bf16_tflops"], "traffic": traffic("cgh")[0],
+                     "traffic_source": traffic("cgh")[1],
                      "note": f"k_cgh_gemm alone ({ms_g:.3f} ms): 24 M N K issued f16 flop (3 split products x "
                              f"4 real GEMMs), useful 8 M N K; peak = {pk_kind} dense bf16 (f16 same rate)"},
         "exact_kernel_sfu": {"achieved": sfu_gops, "peak": peak_gops, "unit": "Gop/s (MUFU)",
@@ -591,7 +608,8 @@ def wl_asm(x, K, W, cpu):
                 "d2h_bytes_per_step": u0.nbytes, "form": e2e_form},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach / pk["hbm_gbs"], "traffic": None,
+                     "frac": ach / pk["hbm_gbs"], "traffic": traffic("asm")[0],
+                     "traffic_source": traffic("asm")[1],
                      "note": f"80 n bytes per propagation (n = 1024^2) over the 3-pass propagation time; "
                              f"peak {pk_kind}"},
         "forms": {"fused": {"props/s": 1e3 / statistics.mean(ms), "ms": statistics.mean(ms)},
@@ -669,7 +687,8 @@ def wl_wrp(x, K, W, cpu):
                 "d2h_bytes_per_step": N * N},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach / pk["hbm_gbs"], "traffic": None,
+                     "frac": ach / pk["hbm_gbs"], "traffic": traffic("wrp")[0],
+                     "traffic_source": traffic("wrp")[1],
                      "note": f"step 2 (4096^2 -> 8192^2 ASM, {statistics.mean(ms2):.3f} ms): 80 n bytes; "
                              f"peak {pk_kind}"},
         "forms": {"step1_ms": statistics.mean(ms1), "step2_ms": statistics.mean(ms2),

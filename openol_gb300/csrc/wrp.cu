@@ -132,6 +132,7 @@ template <int WIN>
 __global__ void __launch_bounds__(WNT) k_wrp_tile(WrpParams P)
 {
     __shared__ float4 cst[WNB][2]; // {c0, ax, ay, b} {x, y, Rtest, A}
+    __shared__ int cls[WNB];       // per point, 2 bits per warp strip: reaches it, holds it whole
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int t = blockIdx.x;
     const int tx_t = t % P.tiles_x, ty_t = t / P.tiles_x;
@@ -150,9 +151,8 @@ __global__ void __launch_bounds__(WNT) k_wrp_tile(WrpParams P)
         dhp[k] = make_float2((float)ra - 7.5f, (float)rb - 7.5f);
         q2p[k] = make_float2(dw * dw + dhp[k].x * dhp[k].x, dw * dw + dhp[k].y * dhp[k].y);
     }
-    // the warp's strip in metres
+    // the tile's columns in metres (the strips' x range)
     const float xl = __fmul_rn(P.p, (float)(tx_t * WT)), xr = __fmul_rn(P.p, (float)(tx_t * WT + WT - 1));
-    const float yl = __fmul_rn(P.p, (float)(ty_t * WT + 8 * warp)), yr = __fmul_rn(P.p, (float)(ty_t * WT + 8 * warp + 7));
     const int beg = P.offset[t], cnt = P.offset[t + 1] - beg;
     float2 acc[4]; // (re, im) of rows r0, r0 + 2, r0 + 4, r0 + 6
 #pragma unroll
@@ -175,26 +175,45 @@ __global__ void __launch_bounds__(WNT) k_wrp_tile(WrpParams P)
             const float Rt = WIN == 0 ? __fmul_rn(R, R) : R;
             c1 = make_float4(x, y, Rt, 1.0f / fabsf(dz.hi + dz.lo));
         }
+        // Classify this point against both warps' 16 x 8 strips once, here,
+        // instead of in every warp's inner loop.  Bit 2s: the window can reach
+        // strip s (a conservative cull with a 1e-4 relative margin; the float
+        // test decides every pixel it keeps).  Bit 2s + 1: the window holds the
+        // whole strip with a 1e-4 margin below its float rounding, so every
+        // pixel's test would be true and none is evaluated (float subtraction
+        // and squaring are monotone, so no pixel's rounded distance exceeds
+        // the strip corner's).
+        int cl = 0;
+        if (k < cnt) {
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                const float yl = __fmul_rn(P.p, (float)(ty_t * WT + 8 * s));
+                const float yr = __fmul_rn(P.p, (float)(ty_t * WT + 8 * s + 7));
+                const float ex = fmaxf(fmaxf(xl - c1.x, c1.x - xr), 0.f), ey = fmaxf(fmaxf(yl - c1.y, c1.y - yr), 0.f);
+                const float lim = c1.z * 1.0001f;
+                const bool reach = WIN == 0 ? ex * ex + ey * ey <= lim : (2.f * ex <= lim && 2.f * ey <= lim);
+                const float fx = fmaxf(fabsf(xl - c1.x), fabsf(xr - c1.x));
+                const float fy = fmaxf(fabsf(yl - c1.y), fabsf(yr - c1.y));
+                const float inner = c1.z * 0.9999f;
+                const bool full = WIN == 0 ? fx * fx + fy * fy <= inner : (2.f * fx <= inner && 2.f * fy <= inner);
+                cl |= (reach ? 1 : 0) << (2 * s);
+                cl |= (reach && full ? 2 : 0) << (2 * s);
+            }
+        }
         cst[tid][0] = c0;
         cst[tid][1] = c1;
+        cls[tid] = cl;
         __syncthreads();
         const int m = min(WNB, cnt - b0);
         float2 part[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) part[q] = make_float2(0.f, 0.f);
         for (int i = 0; i < m; ++i) {
+            // warp-uniform class of this point for this warp's strip
+            const int cl = (cls[i] >> (2 * warp)) & 3;
+            if (!cl) continue;
+            const bool full = cl & 2;
             const float4 b = cst[i][1];
-            // warp-uniform: can the window reach the strip at all?
-            const float ex = fmaxf(fmaxf(xl - b.x, b.x - xr), 0.f), ey = fmaxf(fmaxf(yl - b.y, b.y - yr), 0.f);
-            const float lim = b.z * 1.0001f;
-            const bool reach = WIN == 0 ? ex * ex + ey * ey <= lim : (2.f * ex <= lim && 2.f * ey <= lim);
-            if (!reach) continue;
-            // warp-uniform: does the window hold the whole strip, with a 1e-4
-            // relative margin over the float rounding of the per-pixel test?
-            // Then every pixel's test is true and none is evaluated.
-            const float fx = fmaxf(fabsf(xl - b.x), fabsf(xr - b.x)), fy = fmaxf(fabsf(yl - b.y), fabsf(yr - b.y));
-            const float inner = b.z * 0.9999f;
-            const bool full = WIN == 0 ? fx * fx + fy * fy <= inner : (2.f * fx <= inner && 2.f * fy <= inner);
             const float4 a = cst[i][0];
             const float base = fmaf(a.y, dw, a.x);
             if (full) {
