@@ -356,8 +356,9 @@ double olg_cgh_gemm_tail_weight(double w);
  * 1.6; operands built once and reused, L2 flushed before every timed GEMM;
  * synchronises `stream`) and keeps the fastest for the rest of the process. */
 int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg_stream_t stream);
-/* Synchronises the device and reports (OLG_ERR_CUDA) whether any tensor-core
- * kernel of this library gave up on a bounded wait; clear != 0 resets the flag. */
+/* Synchronises the device and reports (OLG_ERR_CUDA) whether a kernel of this
+ * library with mbarrier waits (the tensor-core GEMM, the TMA-staged column
+ * pass) gave up on a bounded wait; clear != 0 resets the flag. */
 int olg_device_fault_check(int clear);
 
 /* ------------------------------------------------------------------- WRP */

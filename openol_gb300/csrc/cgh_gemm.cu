@@ -374,42 +374,8 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
 // ------------------------------------------------------------------ host
 namespace {
 
-PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::atomic<double> g_tail_weight{1.2};
 std::mutex g_encode_mu;
-std::map<unsigned long long, int *> g_err_flag; // per context
-
-int get_encode()
-{
-    std::lock_guard<std::mutex> lk(g_encode_mu);
-    if (g_encode) return OLG_OK;
-    void *fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-    if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess) return fail(OLG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-    return OLG_OK;
-}
-
-int err_flag(int **out)
-{
-    unsigned long long ctx = 0;
-    if (int rc = context_id(&ctx)) return rc;
-    std::lock_guard<std::mutex> lk(g_encode_mu);
-    if (!g_err_flag.count(ctx)) {
-        int *f = nullptr;
-        cudaError_t e = cudaMalloc(&f, sizeof(int));
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (error flag)");
-        e = cudaMemset(f, 0, sizeof(int));
-        if (e != cudaSuccess) {
-            cudaFree(f);
-            return cuda_fail(e, "cudaMemset (error flag)");
-        }
-        g_err_flag[ctx] = f;
-    }
-    *out = g_err_flag[ctx];
-    return OLG_OK;
-}
 
 int make_map(CUtensorMap *m, void *base, uint64_t rows, uint64_t kp, uint32_t box_rows)
 {
@@ -417,7 +383,9 @@ int make_map(CUtensorMap *m, void *base, uint64_t rows, uint64_t kp, uint32_t bo
     cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
     cuuint32_t box[2] = {(cuuint32_t)GB_K, box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims, strides, box, estr,
+    PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
+    if (int rc = tensor_map_encoder(&enc)) return rc;
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims, strides, box, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? OLG_OK : fail(OLG_ERR_CUDA, "cuTensorMapEncodeTiled failed");
@@ -455,9 +423,8 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
     if (n_points < 0 || ny <= 0 || nx <= 0 || nx > (1 << 20) || ny > (1 << 20)) return fail(OLG_ERR_INVALID_ARG, "bad sizes");
     if (nx > 4096 || ny > 4096) return fail(OLG_ERR_UNSUPPORTED_SIZE, "hologram side must be <= 4096 (exact w^2 in float)");
     if (!(px > 0) || !(py > 0) || !(lambda > 0)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
-    if (int rc = get_encode()) return rc;
     int *err = nullptr;
-    if (int rc = err_flag(&err)) return rc;
+    if (int rc = device_fault_word(&err)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     int kp = 0;
     size_t off[5];
@@ -634,11 +601,11 @@ extern "C" int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg
 extern "C" int olg_device_fault_check(int clear)
 {
     int *err = nullptr;
-    if (int rc = err_flag(&err)) return rc;
+    if (int rc = device_fault_word(&err)) return rc;
     int h = 0;
     cudaError_t e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "reading the device fault flag");
     if (clear && h) cudaMemset(err, 0, sizeof(int));
-    if (h) return fail(OLG_ERR_CUDA, "a tensor-core kernel gave up on a bounded wait");
+    if (h) return fail(OLG_ERR_CUDA, "a kernel gave up on a bounded wait (tensor-core GEMM or TMA-staged column pass)");
     return OLG_OK;
 }

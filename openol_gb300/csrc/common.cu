@@ -62,6 +62,49 @@ void load_ctx_entry_points()
 }
 } // namespace
 
+namespace {
+std::mutex g_encode_mu;
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::map<unsigned long long, int *> g_fault_word; // per context
+} // namespace
+
+int tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000 *out)
+{
+    std::lock_guard<std::mutex> lk(g_encode_mu);
+    if (!g_encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        const cudaError_t e =
+            cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
+            return fail(OLG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    *out = g_encode;
+    return OLG_OK;
+}
+
+int device_fault_word(int **out)
+{
+    unsigned long long ctx = 0;
+    if (int rc = context_id(&ctx)) return rc;
+    std::lock_guard<std::mutex> lk(g_encode_mu);
+    auto it = g_fault_word.find(ctx);
+    if (it == g_fault_word.end()) {
+        int *f = nullptr;
+        cudaError_t e = cudaMalloc(&f, sizeof(int));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (fault word)");
+        e = cudaMemset(f, 0, sizeof(int));
+        if (e != cudaSuccess) {
+            cudaFree(f);
+            return cuda_fail(e, "cudaMemset (fault word)");
+        }
+        it = g_fault_word.emplace(ctx, f).first;
+    }
+    *out = it->second;
+    return OLG_OK;
+}
+
 int context_id(unsigned long long *id)
 {
     std::call_once(g_ctx_once, load_ctx_entry_points);

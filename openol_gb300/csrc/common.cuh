@@ -1,5 +1,7 @@
 // common.cuh -- shared helpers for the libolgb300 kernels (sm_103a).
 #pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -30,6 +32,14 @@ int context_id(unsigned long long *id);
 // Budget of one bounded device-side wait, in SM clock cycles (default 4e9,
 // about 2 s at 2 GHz); olg_wait_budget_cycles sets it.
 long long wait_budget_cycles();
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda).
+int tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000 *out);
+
+// Device word, one per CUDA context, that kernels with bounded waits set
+// when a wait runs out; olg_device_fault_check reads and clears it.
+int device_fault_word(int **out);
 
 // Stream-ordered scratch: caller memory when given, else cudaMallocAsync.
 struct Scratch {

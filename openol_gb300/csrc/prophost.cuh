@@ -32,6 +32,8 @@ extern std::atomic<int> g_variant[3][14];
 int rows_fwd_pass_pow2(const PropParams &P, cudaStream_t st); // prop_rows_fwd.cu
 int rows_inv_pass_pow2(const PropParams &P, cudaStream_t st); // prop_rows_inv.cu
 int cols_pass_pow2(const PropParams &P, cudaStream_t st);     // prop_cols.cu
+// the persistent TMA-staged column pass, padded heights 2048..8192 (prop_cols_tma.cu)
+int cols_pass_tma(const PropParams &P, cudaStream_t st);
 int chirp_axis_pow2(const ChirpAxis &A, cudaStream_t st);     // prop_aux.cu
 // forward pass 3 (OP_SEED) and adjoint pass 1 of one plane, fused; padded
 // widths 256..8192 (prop_aux.cu)

@@ -736,7 +736,10 @@ template <> struct ColVar<7> : Shape<64, 2048, 8, true> {};
 // register-capped shapes: two / four CTAs per SM for more resident warps
 template <> struct ColVar<8> : Shape<512, 8192, 2> {};
 template <> struct ColVar<9> : Shape<256, 4096, 4> {};
-constexpr int N_COL_VARIANTS = 10;
+// variant 10: the persistent TMA-staged column pass (prop_cols_tma.cu),
+// padded heights 2048..8192
+constexpr int COL_VARIANT_TMA = 10;
+constexpr int N_COL_VARIANTS = 11;
 
 template <int N, class V>
 struct RowShape {
@@ -967,6 +970,7 @@ bool col_variant_valid(int i)
     case 7: return ColShape<N, ColVar<7>>::valid;
     case 8: return ColShape<N, ColVar<8>>::valid;
     case 9: return ColShape<N, ColVar<9>>::valid;
+    case COL_VARIANT_TMA: return N >= 2048 && N <= 8192;
     default: return false;
     }
 }
@@ -1020,6 +1024,9 @@ int launch_cols(const PropParams &P, cudaStream_t st)
         case 7: return launch_cols_v<N, 7>(P, st);
         case 8: return launch_cols_v<N, 8>(P, st);
         case 9: return launch_cols_v<N, 9>(P, st);
+        case COL_VARIANT_TMA:
+            if constexpr (N >= 2048) return cols_pass_tma(P, st);
+            else return fail(OLG_ERR_INVALID_ARG, "TMA column pass: padded heights 2048..8192");
         default: return launch_cols_v<N, 0>(P, st);
         }
     } else {

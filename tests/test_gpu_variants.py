@@ -12,7 +12,7 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("shape", [(128, 256), (512, 512), (2048, 1024), (64, 4096), (4096, 64)])
+@pytest.mark.parametrize("shape", [(128, 256), (512, 512), (1024, 512), (2048, 1024), (64, 4096), (4096, 64)])
 def test_every_launch_variant_matches_oracle(shape):
     ny, nx = shape
     rng = np.random.default_rng(ny + nx)
