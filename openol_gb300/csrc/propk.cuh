@@ -736,10 +736,13 @@ template <> struct ColVar<7> : Shape<64, 2048, 8, true> {};
 // register-capped shapes: two / four CTAs per SM for more resident warps
 template <> struct ColVar<8> : Shape<512, 8192, 2> {};
 template <> struct ColVar<9> : Shape<256, 4096, 4> {};
+// 1024 threads, one butterfly each: twice the resident warps of ColVar<1> at
+// the same 64 KB-per-column tile (64 registers, no spills up to 8192)
+template <> struct ColVar<11> : Shape<1024, 16384, 1> {};
 // variant 10: the persistent TMA-staged column pass (prop_cols_tma.cu),
 // padded heights 2048..8192
 constexpr int COL_VARIANT_TMA = 10;
-constexpr int N_COL_VARIANTS = 11;
+constexpr int N_COL_VARIANTS = 12;
 
 template <int N, class V>
 struct RowShape {
@@ -971,6 +974,7 @@ bool col_variant_valid(int i)
     case 8: return ColShape<N, ColVar<8>>::valid;
     case 9: return ColShape<N, ColVar<9>>::valid;
     case COL_VARIANT_TMA: return N >= 2048 && N <= 8192;
+    case 11: return ColShape<N, ColVar<11>>::valid;
     default: return false;
     }
 }
@@ -1027,6 +1031,7 @@ int launch_cols(const PropParams &P, cudaStream_t st)
         case COL_VARIANT_TMA:
             if constexpr (N >= 2048) return cols_pass_tma(P, st);
             else return fail(OLG_ERR_INVALID_ARG, "TMA column pass: padded heights 2048..8192");
+        case 11: return launch_cols_v<N, 11>(P, st);
         default: return launch_cols_v<N, 0>(P, st);
         }
     } else {
