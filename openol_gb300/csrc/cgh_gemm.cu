@@ -17,13 +17,15 @@
 // k_cgh_gemm_prep  per point, FP64: expansion coefficients of the x / y phases
 // k_cgh_gemm_ops   builds A_hi/A_lo/B_hi/B_lo (f16, K-contiguous, zero padded),
 //                  phases range-reduced exactly (frac_mul), MUFU sin/cos
-// k_cgh_gemm       warp-specialised tcgen05 GEMM, one CTA per tile plus CTAs on
+// k_cgh_gemm<BN>   warp-specialised tcgen05 GEMM, one CTA per tile plus CTAs on
 //                  the spare SMs that take the tiles' K tails: warp 0 issues TMA loads into a
-//                  4-stage ring (128 x 64 A and 256 x 64 B f16 tiles, 128-byte
-//                  swizzle), warp 1 owns TMEM (two 256-column f32 accumulators)
-//                  and issues the 128 x 256 x 16 MMAs chunk by chunk, warps 2-9
-//                  add each finished chunk into f32 registers and add every
-//                  finished piece of a tile into the complex64 output.
+//                  4-stage ring (128 x 64 A and BN x 64 B f16 tiles, 128-byte
+//                  swizzle), warp 1 owns TMEM (two f32 accumulators of BN
+//                  columns) and issues the 128 x BN x 16 MMAs chunk by chunk,
+//                  warps 2-9 add each finished chunk into f32 registers and add
+//                  every finished piece of a tile into the complex64 output.
+//                  BN in {128, ..., 256} is the N tile that pads nx least
+//                  (1920 = 8 x 240).
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
@@ -40,10 +42,17 @@
 
 namespace olg {
 
-constexpr int GB_M = 128, GB_N = 256, GB_K = 64, GB_STAGES = 4;
+constexpr int GB_M = 128, GB_K = 64, GB_STAGES = 4;
 constexpr int GB_A_BYTES = GB_M * GB_K * 2;
-constexpr int GB_B_BYTES = GB_N * GB_K * 2;
-constexpr int GB_SMEM = GB_STAGES * (GB_A_BYTES + GB_B_BYTES) + 1024 + 256;
+// N tile widths (multiples of 16 up to 256, the kind::f16 limit at M = 128):
+// the host takes the one whose tiles cover nx with the least padding
+// (1920 = 8 x 240 exactly, where 256 would pad to 2048).
+template <int BN>
+struct GemmTile {
+    static_assert(BN % 16 == 0 && BN >= 128 && BN <= 256, "N tile");
+    static constexpr int B_BYTES = BN * GB_K * 2;           // a multiple of 1024: SW128 stages stay aligned
+    static constexpr int SMEM = GB_STAGES * (GB_A_BYTES + B_BYTES) + 1024 + 256;
+};
 constexpr long long GB_WAIT = 4000000000LL; // ~2 s of SM clock per wait
 
 struct PointCoef {
@@ -149,11 +158,12 @@ __global__ void k_cgh_gemm_ops(GemmOps G)
 
 struct GemmParams {
     int m2, n, kblocks; // rows of D (2 ny), columns (nx), K blocks of 64 per segment
-    int tiles_n;        // 256-column tiles across D
-    int tiles;          // 128 x 256 tiles of D
+    int tiles_n;        // N tiles across D
+    int tiles;          // 128 x BN tiles of D
     int split;          // K blocks (of 3 kblocks) a tile's own CTA does
     int extra;          // CTAs beyond `tiles` that do the rest [split, 3 kblocks)
-    float2 *U;          // added to with float2 atomics (zeroed first unless accumulating)
+    int vec4;           // U is 16-byte aligned and n even: two complex values per atomic
+    float2 *U;          // added to with atomics (zeroed first unless accumulating)
     int *err;
 };
 
@@ -163,8 +173,8 @@ struct GemmParams {
 // that every SM gets about the same tensor work.  The tile CTAs walk K in
 // lockstep (their A / B blocks are shared through L2), and the extra CTAs'
 // K range is a small slice of the operands that L2 holds.  Each piece (tile,
-// K range) is one accumulation, added into U with float2 atomics when it ends;
-// a tile's two pieces add in either order.
+// K range) is one accumulation, added into U with atomics when it ends; a
+// tile's two pieces add in either order.
 __device__ __forceinline__ int gemm_pieces(const GemmParams &P)
 {
     if ((int)blockIdx.x < P.tiles) return 1;
@@ -185,23 +195,97 @@ __device__ __forceinline__ void gemm_piece(const GemmParams &P, int p, int total
 }
 
 // Accumulation within a piece: the MMA warp writes chunks of GB_CHUNK
-// K-blocks alternately into two 256-column TMEM accumulators; the 8 epilogue
+// K-blocks alternately into two TMEM accumulators (BN columns each); the 8 epilogue
 // warps add every finished chunk into f32 registers (rounded adds) while the
 // next chunk runs, so the tensor pipe's own accumulation never spans more
 // than GB_CHUNK x 64 x 3 products.
 constexpr int GB_CHUNK = 8;
 constexpr int GB_EPI_WARPS = 8;
 constexpr int GB_THREADS = 64 + 32 * GB_EPI_WARPS;
+constexpr uint32_t GB_TMEM_COLS = 512; // two accumulators, at columns 0 and 256
 
+// Epilogue warps: warp w drains TMEM lanes [32 (w % 4), +32) of columns
+// [128 half, min(BN, 128 half + 128)), half = (w - 2) / 4, in chunks of 16
+// (every TMEM load starts on a 16-column boundary).  PAIR keeps two loads in
+// flight per wait; at 168 registers per thread that compiles without spills
+// for BN = 224 and 240 only (the other widths spill 20-44 bytes paired; 192
+// spills 32 bytes either way).
+template <bool PAIR>
+__device__ __forceinline__ void drain_cols(uint32_t base, int nch, float (&acc)[128])
+{
+#pragma unroll
+    for (int cc = 0; cc < 8; cc += PAIR ? 2 : 1) {
+        if (PAIR && cc + 1 < nch) {
+            uint32_t r0[16], r1[16];
+            tmem_ld_async(base + 16 * cc, r0);
+            tmem_ld_async(base + 16 * cc + 16, r1);
+            tmem_wait_ld();
+            tmem_regs_ready(r0);
+            tmem_regs_ready(r1);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                acc[16 * cc + i] += __uint_as_float(r0[i]);
+                acc[16 * cc + 16 + i] += __uint_as_float(r1[i]);
+            }
+        } else if (cc < nch) {
+            uint32_t r0[16];
+            tmem_ld_async(base + 16 * cc, r0);
+            tmem_wait_ld();
+            tmem_regs_ready(r0);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) acc[16 * cc + i] += __uint_as_float(r0[i]);
+        }
+    }
+}
+
+// Add this warp's columns into U.  Lanes 2i / 2i + 1 hold the Re / Im rows of
+// one hologram row h: in each 16-column chunk the even lane adds the first 8
+// columns and the odd lane the last 8, each forming complex values from its
+// own accumulator and its partner's (shuffled).
+__device__ __forceinline__ void store_cols(const GemmParams &P, const float (&acc)[128], int nch, bool store,
+                                           bool odd, int h, int cbase)
+{
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) {
+        if (cc >= nch) break; // warp-uniform
+        float o[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) o[i] = __shfl_xor_sync(0xffffffffu, acc[16 * cc + i], 1);
+        if (!store) continue;
+        const int cb = cbase + 16 * cc + (odd ? 8 : 0);
+        float2 *dst = P.U + (size_t)h * P.n + cb;
+        if (P.vec4 && cb + 8 <= P.n) {
+#pragma unroll
+            for (int i = 0; i < 8; i += 2) {
+                const float4 v = odd ? make_float4(o[8 + i], acc[16 * cc + 8 + i], o[9 + i], acc[16 * cc + 9 + i])
+                                     : make_float4(acc[16 * cc + i], o[i], acc[16 * cc + i + 1], o[i + 1]);
+                atomicAdd(reinterpret_cast<float4 *>(dst + i), v);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                if (cb + i >= P.n) break;
+                const float re = odd ? o[8 + i] : acc[16 * cc + i];
+                const float im = odd ? acc[16 * cc + 8 + i] : o[i];
+                atomicAdd(dst + i, make_float2(re, im));
+            }
+        }
+    }
+}
+
+// 320 threads: ten warps over four SM sub-partitions (three on two of them)
+// cap the registers at 168 per thread.
+template <int BN>
 __global__ void __launch_bounds__(GB_THREADS, 1)
     k_cgh_gemm(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, GemmParams P)
 {
+    using T = GemmTile<BN>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
     uint8_t *sB = smem + GB_STAGES * GB_A_BYTES;
-    uint64_t *full = (uint64_t *)(sB + GB_STAGES * GB_B_BYTES);
+    uint64_t *full = (uint64_t *)(sB + GB_STAGES * T::B_BYTES);
     uint64_t *empty = full + GB_STAGES;
     uint64_t *tfull = empty + GB_STAGES; // [2]
     uint64_t *tfree = tfull + 2;         // [2]
@@ -225,7 +309,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
         fence_mbar_init();
     }
     if (warp == 1) {
-        tmem_alloc(smem_u32(tmem_slot), 2 * GB_N);
+        tmem_alloc(smem_u32(tmem_slot), GB_TMEM_COLS);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -239,7 +323,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
             for (int p = 0; p < np && !*fault; ++p) {
                 int t, k0, k1;
                 gemm_piece(P, p, total, t, k0, k1);
-                const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * GB_N;
+                const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * BN;
                 for (int kb = k0; kb < k1 && !*fault; ++kb, ++i) {
                     const int s = i % GB_STAGES;
                     const uint32_t ph = (uint32_t)(i / GB_STAGES) & 1u;
@@ -250,9 +334,9 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                     const int seg = kb / P.kblocks, kk = (kb % P.kblocks) * GB_K;
                     const CUtensorMap *ma = seg < 2 ? &tAh : &tAl;
                     const CUtensorMap *mb = seg == 1 ? &tBl : &tBh;
-                    mbar_expect_tx(smem_u32(full + s), GB_A_BYTES + GB_B_BYTES);
+                    mbar_expect_tx(smem_u32(full + s), GB_A_BYTES + T::B_BYTES);
                     tma_load_2d(smem_u32(sA + s * GB_A_BYTES), ma, smem_u32(full + s), kk, m0);
-                    tma_load_2d(smem_u32(sB + s * GB_B_BYTES), mb, smem_u32(full + s), kk, n0);
+                    tma_load_2d(smem_u32(sB + s * T::B_BYTES), mb, smem_u32(full + s), kk, n0);
                     issued = i + 1;
                 }
             }
@@ -262,7 +346,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_f16_f32(GB_M, GB_N);
+            constexpr uint32_t idesc = idesc_f16_f32(GB_M, BN);
             int c = 0, i = 0; // chunk and stage counters over all pieces
             for (int p = 0; p < np && !*fault; ++p) {
                 int t, k0, k1;
@@ -274,7 +358,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t d = tmem + (uint32_t)(b * GB_N);
+                    const uint32_t d = tmem + (uint32_t)(b * 256);
                     const int kend = min(k1, kb + GB_CHUNK);
                     for (int kc = kb; kc < kend; ++kc, ++i) {
                         const int s = i % GB_STAGES;
@@ -283,7 +367,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                             break;
                         }
                         tc_fence_after();
-                        const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * GB_B_BYTES);
+                        const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * T::B_BYTES);
 #pragma unroll
                         for (int k = 0; k < GB_K / 16; ++k)
                             umma_f16(d, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), idesc,
@@ -296,8 +380,8 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
             }
         }
     } else {
-        // epilogue: warp w drains TMEM lanes [32 (w % 4), +32), columns [128 half, +128)
         const int q = warp & 3, half = (warp - 2) >> 2;
+        const int nch = max(0, min(128, BN - 128 * half)) / 16;
         bool ok = true;
         int c = 0;
         for (int p = 0; p < np && ok; ++p) {
@@ -317,57 +401,22 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                     break;
                 }
                 tc_fence_after();
-                const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * GB_N + 128 * half);
-#pragma unroll
-                for (int cc = 0; cc < 8; ++cc) {
-                    float v[16];
-                    tmem_ld16(base + 16 * cc, v);
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) acc[16 * cc + i] += v[i];
-                }
+                drain_cols<BN == 224 || BN == 240>(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * 256 + 128 * half),
+                                                   nch, acc);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0)
                     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tfree + b)) : "memory");
                 kb = min(k1, kb + GB_CHUNK);
             }
-            const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * GB_N;
+            const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * BN;
             const int row = m0 + 32 * q + lane; // row of D
-            const int h = row >> 1;
-            const bool odd = row & 1;
-            const bool store = ok && row < P.m2;
-#pragma unroll
-            for (int cc = 0; cc < 8; ++cc) {
-                float o[16];
-#pragma unroll
-                for (int i = 0; i < 16; ++i) o[i] = __shfl_xor_sync(0xffffffffu, acc[16 * cc + i], 1);
-                if (!store) continue;
-                // even lane holds Re of row h, odd lane Im: even adds columns +0..7, odd +8..15
-                const int cb = n0 + 128 * half + 16 * cc + (odd ? 8 : 0);
-                float2 *dst = P.U + (size_t)h * P.n + cb;
-                if ((P.n & 1) == 0 && cb + 8 <= P.n) {
-                    // two complex values per 16-byte atomic (cb and n even: aligned)
-#pragma unroll
-                    for (int i = 0; i < 8; i += 2) {
-                        const float4 v = odd ? make_float4(o[8 + i], acc[16 * cc + 8 + i], o[9 + i], acc[16 * cc + 9 + i])
-                                             : make_float4(acc[16 * cc + i], o[i], acc[16 * cc + i + 1], o[i + 1]);
-                        atomicAdd(reinterpret_cast<float4 *>(dst + i), v);
-                    }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        if (cb + i >= P.n) break;
-                        const float re = odd ? o[8 + i] : acc[16 * cc + i];
-                        const float im = odd ? acc[16 * cc + 8 + i] : o[i];
-                        atomicAdd(dst + i, make_float2(re, im));
-                    }
-                }
-            }
+            store_cols(P, acc, nch, ok && row < P.m2, row & 1, row >> 1, n0 + 128 * half);
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 1) tmem_dealloc(tmem, 2 * GB_N);
+    if (warp == 1) tmem_dealloc(tmem, GB_TMEM_COLS);
     if (threadIdx.x == 0 && *fault) atomicExch(P.err, 1);
 }
 
@@ -389,6 +438,36 @@ int make_map(CUtensorMap *m, void *base, uint64_t rows, uint64_t kp, uint32_t bo
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? OLG_OK : fail(OLG_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+}
+
+// N tile width for a hologram nx wide: the fewest padded columns, ties to
+// the wider tile.
+int pick_bn(int nx)
+{
+    const int cand[] = {256, 240, 224, 192, 160, 128};
+    int best = 256;
+    long long pad = 1LL << 40;
+    for (int bn : cand) {
+        const long long cover = (long long)((nx + bn - 1) / bn) * bn;
+        if (cover < pad) {
+            pad = cover;
+            best = bn;
+        }
+    }
+    return best;
+}
+
+int gemm_smem_optin()
+{
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaFuncSetAttribute(k_cgh_gemm<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<256>::SMEM)) ||
+        (e = cudaFuncSetAttribute(k_cgh_gemm<240>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<240>::SMEM)) ||
+        (e = cudaFuncSetAttribute(k_cgh_gemm<224>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<224>::SMEM)) ||
+        (e = cudaFuncSetAttribute(k_cgh_gemm<192>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<192>::SMEM)) ||
+        (e = cudaFuncSetAttribute(k_cgh_gemm<160>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<160>::SMEM)) ||
+        (e = cudaFuncSetAttribute(k_cgh_gemm<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<128>::SMEM)))
+        return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm)");
+    return OLG_OK;
 }
 
 size_t gemm_layout(int n, int ny, int nx, int *kp_out, size_t off[5])
@@ -423,6 +502,7 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
     if (n_points < 0 || ny <= 0 || nx <= 0 || nx > (1 << 20) || ny > (1 << 20)) return fail(OLG_ERR_INVALID_ARG, "bad sizes");
     if (nx > 4096 || ny > 4096) return fail(OLG_ERR_UNSUPPORTED_SIZE, "hologram side must be <= 4096 (exact w^2 in float)");
     if (!(px > 0) || !(py > 0) || !(lambda > 0)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if ((uintptr_t)U % 8) return fail(OLG_ERR_INVALID_ARG, "U must be 8-byte aligned (complex64)");
     int *err = nullptr;
     if (int rc = device_fault_word(&err)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
@@ -456,16 +536,18 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
     CUtensorMap mAh, mAl, mBh, mBl;
     if (int rc = make_map(&mAh, G.a_hi, 2 * (uint64_t)ny, kp, GB_M)) return rc;
     if (int rc = make_map(&mAl, G.a_lo, 2 * (uint64_t)ny, kp, GB_M)) return rc;
-    if (int rc = make_map(&mBh, G.b_hi, nx, kp, GB_N)) return rc;
-    if (int rc = make_map(&mBl, G.b_lo, nx, kp, GB_N)) return rc;
+    const int bn = pick_bn(nx);
+    if (int rc = make_map(&mBh, G.b_hi, nx, kp, bn)) return rc;
+    if (int rc = make_map(&mBl, G.b_lo, nx, kp, bn)) return rc;
     GemmParams P{};
     P.m2 = 2 * ny;
     P.n = nx;
     P.kblocks = kp / GB_K;
-    P.tiles_n = (nx + GB_N - 1) / GB_N;
+    P.tiles_n = (nx + bn - 1) / bn;
     const long long tiles = (long long)P.tiles_n * ((2 * ny + GB_M - 1) / GB_M);
     P.tiles = (int)tiles;
     P.U = (float2 *)U;
+    P.vec4 = ((uintptr_t)U % 16 == 0 && nx % 2 == 0) ? 1 : 0;
     P.err = err;
     // per context, once: the shared-memory opt-in and the SM count
     static std::map<unsigned long long, int> sm_count;
@@ -479,8 +561,7 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
             int dev = 0;
             cudaError_t e = cudaGetDevice(&dev);
             if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-            e = cudaFuncSetAttribute(k_cgh_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, GB_SMEM);
-            if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm)");
+            if (int rc = gemm_smem_optin()) return rc;
             int n = 0;
             e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(SM count)");
@@ -512,7 +593,14 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
     }
     const int grid = (int)tiles + P.extra;
-    k_cgh_gemm<<<grid, GB_THREADS, GB_SMEM, st>>>(mAh, mAl, mBh, mBl, P);
+    switch (bn) {
+    case 256: k_cgh_gemm<256><<<grid, GB_THREADS, GemmTile<256>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
+    case 240: k_cgh_gemm<240><<<grid, GB_THREADS, GemmTile<240>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
+    case 224: k_cgh_gemm<224><<<grid, GB_THREADS, GemmTile<224>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
+    case 192: k_cgh_gemm<192><<<grid, GB_THREADS, GemmTile<192>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
+    case 160: k_cgh_gemm<160><<<grid, GB_THREADS, GemmTile<160>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
+    default: k_cgh_gemm<128><<<grid, GB_THREADS, GemmTile<128>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
+    }
     count_launch();
     return check_launch("k_cgh_gemm");
 }

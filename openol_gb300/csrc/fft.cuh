@@ -21,6 +21,16 @@ constexpr int FFT_MAX = 8192;
 
 __host__ __device__ constexpr int padded_len(int n) { return n + (n >> 4); }
 __device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+// pidx is affine along the index sets the transforms walk, so addresses can be
+// formed as one base plus compile-time offsets:
+//   pidx(j + r M) = pidx(j) + r pstride<M>()   (M a multiple of 16)
+//   pidx(16 j + k) = 17 j + k                  (0 <= k < 16)
+template <int M>
+__host__ __device__ constexpr int pstride()
+{
+    static_assert(M % 16 == 0 && M > 0, "pidx is affine only on multiples of 16");
+    return M + M / 16;
+}
 
 template <int DIR>
 __device__ __forceinline__ float2 twid(const float2 *__restrict__ table, int m)
@@ -176,8 +186,15 @@ __device__ __forceinline__ void fft_stage(float2 *s, int ss, const float2 *__res
         if (GUARD && b >= BT) continue;
         const int q = COLS ? (b % NSEQ) : (b / B);
         const int j = COLS ? (b / NSEQ) : (b % B);
+        if constexpr (B % 16 == 0) {
+            const int a0 = saddr<N, NSEQ, COLS>(q, j, ss);
+            constexpr int LS = pstride<B>() * (COLS ? NSEQ : 1);
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[t][r] = s[saddr<N, NSEQ, COLS>(q, j + r * B, ss)];
+            for (int r = 0; r < R; ++r) v[t][r] = s[a0 + r * LS];
+        } else { // short transforms (N < 256)
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[t][r] = s[saddr<N, NSEQ, COLS>(q, j + r * B, ss)];
+        }
         if constexpr (NS > 1) {
             const int k = j & (NS - 1);
             constexpr int STEP = FFT_MAX / (NS * R);
@@ -194,8 +211,16 @@ __device__ __forceinline__ void fft_stage(float2 *s, int ss, const float2 *__res
         const int j = COLS ? (b / NSEQ) : (b % B);
         const int k = j & (NS - 1);
         const int base = (j / NS) * NS * R + k;
+        if constexpr (NS % 16 == 0 || (NS == 1 && R == 16)) {
+            // NS == 1 with radix 16: base = 16 j, offsets r < 16 stay in one 16-block
+            const int a0 = saddr<N, NSEQ, COLS>(q, base, ss);
+            constexpr int SS = (NS == 1 ? 1 : pstride<(NS % 16 == 0 ? NS : 16)>()) * (COLS ? NSEQ : 1);
 #pragma unroll
-        for (int r = 0; r < R; ++r) s[saddr<N, NSEQ, COLS>(q, base + r * NS, ss)] = v[t][outpos<R>(r)];
+            for (int r = 0; r < R; ++r) s[a0 + r * SS] = v[t][outpos<R>(r)];
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) s[saddr<N, NSEQ, COLS>(q, base + r * NS, ss)] = v[t][outpos<R>(r)];
+        }
     }
     __syncthreads();
 }

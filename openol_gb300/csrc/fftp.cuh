@@ -272,8 +272,10 @@ __device__ __forceinline__ void cp_fft_stage(float4 *s, int ss, const float4 *__
         if (GUARD && b >= BT) continue;
         const int q = COLS ? (b % NSP) : (b / B);
         const int j = COLS ? (b / NSP) : (b % B);
+        const int a0 = cp_saddr<N, NSP, COLS>(q, j, ss);
+        constexpr int LS = pstride<B>() * (COLS ? NSP : 1);
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[t][r] = cp_ld(s + cp_saddr<N, NSP, COLS>(q, j + r * B, ss));
+        for (int r = 0; r < R; ++r) v[t][r] = cp_ld(s + a0 + r * LS);
         if constexpr (NS > 1) {
             const int k = j & (NS - 1);
             constexpr int STEP = FFT_MAX / (NS * R);
@@ -290,8 +292,11 @@ __device__ __forceinline__ void cp_fft_stage(float4 *s, int ss, const float4 *__
         const int j = COLS ? (b / NSP) : (b % B);
         const int k = j & (NS - 1);
         const int base = (j / NS) * NS * R + k;
+        const int a0 = cp_saddr<N, NSP, COLS>(q, base, ss);
+        static_assert(NS % 16 == 0, "middle stages start at NS = 16");
+        constexpr int SS = pstride<NS>() * (COLS ? NSP : 1);
 #pragma unroll
-        for (int r = 0; r < R; ++r) cp_st(s + cp_saddr<N, NSP, COLS>(q, base + r * NS, ss), v[t][outpos<R>(r)]);
+        for (int r = 0; r < R; ++r) cp_st(s + a0 + r * SS, v[t][outpos<R>(r)]);
     }
     __syncthreads();
 }

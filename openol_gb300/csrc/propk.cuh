@@ -226,7 +226,7 @@ __device__ __forceinline__ void rows_fwd_body(const PropParams &P, int r0, float
         for (int r = 4; r < 12; ++r) v[r] = h < P.ny ? load_in(P, h, j + (r - 4) * B) : make_float2(0.f, 0.f);
         dft16_in_mid<-1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[q * SS + 17 * j + k] = v[outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, -1, NT, false, NSEQ>(sm, SS, g_tw, tid);
@@ -235,7 +235,7 @@ __device__ __forceinline__ void rows_fwd_body(const PropParams &P, int r0, float
         const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j) + r * pstride<B>()];
         last_twiddle<N, -1>(v, j, g_tw);
         dft<16, -1>(v);
         if (h < P.ny) {
@@ -259,7 +259,7 @@ __device__ __forceinline__ void rows_inv_body(const PropParams &P, int r0, float
             v[r] = h < P.ny ? __ldcg(P.S + (size_t)h * N + j + r * B) : make_float2(0.f, 0.f);
         dft<16, +1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[q * SS + 17 * j + k] = v[outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, +1, NT, false, NSEQ>(sm, SS, g_tw, tid);
@@ -268,7 +268,7 @@ __device__ __forceinline__ void rows_inv_body(const PropParams &P, int r0, float
         const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j) + r * pstride<B>()];
         last_twiddle<N, +1>(v, j, g_tw);
         dft16_out_mid<+1>(v);
         if (h >= P.ny) continue;
@@ -298,7 +298,7 @@ __device__ __forceinline__ void cols_body(const PropParams &P, int c0, float2 *s
             v[r] = kx < NX ? __ldcg(P.S + (size_t)(j + (r - 4) * B) * NX + kx) : make_float2(0.f, 0.f);
         dft16_in_mid<-1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = v[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[17 * C * j + c + k * C] = v[outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, -1, NT, true, C>(sm, 0, g_tw, tid);
@@ -308,7 +308,7 @@ __device__ __forceinline__ void cols_body(const PropParams &P, int c0, float2 *s
     for (int t = 0; t < BPT; ++t) {
         const int b = tid + t * NT, c = b % C, j = b / C;
 #pragma unroll
-        for (int r = 0; r < 16; ++r) vv[t][r] = sm[pidx(j + r * B) * C + c];
+        for (int r = 0; r < 16; ++r) vv[t][r] = sm[pidx(j) * C + c + r * (pstride<B>() * C)];
     }
     __syncthreads();
 #pragma unroll
@@ -321,7 +321,7 @@ __device__ __forceinline__ void cols_body(const PropParams &P, int c0, float2 *s
         for (int k = 0; k < 16; ++k) w[k] = kx < NX ? cmul(vv[t][outpos<16>(k)], tf_at(P, j + k * B, kx, N)) : vv[t][outpos<16>(k)];
         dft<16, +1>(w);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = w[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[17 * C * j + c + k * C] = w[outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, +1, NT, true, C>(sm, 0, g_tw, tid);
@@ -331,7 +331,7 @@ __device__ __forceinline__ void cols_body(const PropParams &P, int c0, float2 *s
         const int b = tid + t * NT, c = b % C, j = b / C, kx = c0 + c;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j + r * B) * C + c];
+        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j) * C + c + r * (pstride<B>() * C)];
         last_twiddle<N, +1>(v, j, g_tw);
         dft16_out_mid<+1>(v);
         if (kx < NX) {
@@ -372,7 +372,7 @@ __device__ __forceinline__ void rows_fwd_body_persist(const PropParams &P, float
             for (int r = 4; r < 12; ++r) v[r] = nv[t][r - 4];
             dft16_in_mid<-1>(v);
 #pragma unroll
-            for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+            for (int k = 0; k < 16; ++k) sm[q * SS + 17 * j + k] = v[outpos<16>(k)];
         }
         fetch(g + gridDim.x);
         __syncthreads();
@@ -382,7 +382,7 @@ __device__ __forceinline__ void rows_fwd_body_persist(const PropParams &P, float
             const int b = tid + t * NT, q = b / B, j = b % B, h = g * NSEQ + q;
             float2 v[16];
 #pragma unroll
-            for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+            for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j) + r * pstride<B>()];
             last_twiddle<N, -1>(v, j, g_tw);
             dft<16, -1>(v);
             if (h < P.ny) {
@@ -421,7 +421,7 @@ __device__ __forceinline__ void rows_inv_body_persist(const PropParams &P, float
             for (int r = 0; r < 16; ++r) v[r] = nv[t][r];
             dft<16, +1>(v);
 #pragma unroll
-            for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+            for (int k = 0; k < 16; ++k) sm[q * SS + 17 * j + k] = v[outpos<16>(k)];
         }
         fetch(g + gridDim.x);
         __syncthreads();
@@ -431,7 +431,7 @@ __device__ __forceinline__ void rows_inv_body_persist(const PropParams &P, float
             const int b = tid + t * NT, q = b / B, j = b % B, h = g * NSEQ + q;
             float2 v[16];
 #pragma unroll
-            for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+            for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j) + r * pstride<B>()];
             last_twiddle<N, +1>(v, j, g_tw);
             dft16_out_mid<+1>(v);
             if (h < P.ny) {
@@ -466,7 +466,7 @@ __device__ __forceinline__ void rows_seed_body(const PropParams &P, int r0, floa
             v[r] = h < P.ny ? __ldcg(P.S + (size_t)h * N + j + r * B) : make_float2(0.f, 0.f);
         dft<16, +1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = v[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[q * SS + 17 * j + k] = v[outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, +1, NT, false, NSEQ>(sm, SS, g_tw, tid);
@@ -475,7 +475,7 @@ __device__ __forceinline__ void rows_seed_body(const PropParams &P, int r0, floa
         const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j) + r * pstride<B>()];
         last_twiddle<N, +1>(v, j, g_tw);
         dft16_out_mid<+1>(v);
 #pragma unroll
@@ -497,7 +497,7 @@ __device__ __forceinline__ void rows_seed_body(const PropParams &P, int r0, floa
         const int b = tid + t * NT, q = b / B, j = b % B;
         dft16_in_mid<-1>(u[t]);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[q * SS + pidx(j * 16 + k)] = u[t][outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[q * SS + 17 * j + k] = u[t][outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, -1, NT, false, NSEQ>(sm, SS, g_tw, tid);
@@ -506,7 +506,7 @@ __device__ __forceinline__ void rows_seed_body(const PropParams &P, int r0, floa
         const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + q;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j) + r * pstride<B>()];
         last_twiddle<N, -1>(v, j, g_tw);
         dft<16, -1>(v);
         if (h < P.ny) {
@@ -557,7 +557,7 @@ __device__ __forceinline__ void rows_fwd_body_p(const PropParams &P, int r0, flo
         }
         cp_dft16_in_mid<-1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) cp_st(sm + q * SS + pidx(j * 16 + k), v[outpos<16>(k)]);
+        for (int k = 0; k < 16; ++k) cp_st(sm + q * SS + 17 * j + k, v[outpos<16>(k)]);
     }
     __syncthreads();
     cp_mid_stages<N, -1, NT, false, NSP>(sm, SS, g_tw4, tid);
@@ -566,7 +566,7 @@ __device__ __forceinline__ void rows_fwd_body_p(const PropParams &P, int r0, flo
         const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + 2 * q;
         cpair v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = cp_ld(sm + q * SS + pidx(j + r * B));
+        for (int r = 0; r < 16; ++r) v[r] = cp_ld(sm + q * SS + pidx(j) + r * pstride<B>());
         cp_last_twiddle<N, -1>(v, j, g_tw4);
         cp_dft<16, -1>(v);
         if (h < P.ny) {
@@ -598,7 +598,7 @@ __device__ __forceinline__ void rows_inv_body_p(const PropParams &P, int r0, flo
         }
         cp_dft<16, +1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) cp_st(sm + q * SS + pidx(j * 16 + k), v[outpos<16>(k)]);
+        for (int k = 0; k < 16; ++k) cp_st(sm + q * SS + 17 * j + k, v[outpos<16>(k)]);
     }
     __syncthreads();
     cp_mid_stages<N, +1, NT, false, NSP>(sm, SS, g_tw4, tid);
@@ -607,7 +607,7 @@ __device__ __forceinline__ void rows_inv_body_p(const PropParams &P, int r0, flo
         const int b = tid + t * NT, q = b / B, j = b % B, h = r0 + 2 * q;
         cpair v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = cp_ld(sm + q * SS + pidx(j + r * B));
+        for (int r = 0; r < 16; ++r) v[r] = cp_ld(sm + q * SS + pidx(j) + r * pstride<B>());
         cp_last_twiddle<N, +1>(v, j, g_tw4);
         cp_dft16_out_mid<+1>(v);
         if (h < P.ny) {
@@ -641,7 +641,7 @@ __device__ __forceinline__ void cols_body_p(const PropParams &P, int c0, float4 
         }
         cp_dft16_in_mid<-1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) cp_st(sm + pidx(j * 16 + k) * CP + c, v[outpos<16>(k)]);
+        for (int k = 0; k < 16; ++k) cp_st(sm + 17 * CP * j + c + k * CP, v[outpos<16>(k)]);
     }
     __syncthreads();
     cp_mid_stages<N, -1, NT, true, CP>(sm, 0, g_tw4, tid);
@@ -651,7 +651,7 @@ __device__ __forceinline__ void cols_body_p(const PropParams &P, int c0, float4 
     for (int t = 0; t < BPT; ++t) {
         const int b = tid + t * NT, c = b % CP, j = b / CP;
 #pragma unroll
-        for (int r = 0; r < 16; ++r) vv[t][r] = cp_ld(sm + pidx(j + r * B) * CP + c);
+        for (int r = 0; r < 16; ++r) vv[t][r] = cp_ld(sm + pidx(j) * CP + c + r * (pstride<B>() * CP));
     }
     __syncthreads();
 #pragma unroll
@@ -674,7 +674,7 @@ __device__ __forceinline__ void cols_body_p(const PropParams &P, int c0, float4 
         }
         cp_dft<16, +1>(w);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) cp_st(sm + pidx(j * 16 + k) * CP + c, w[outpos<16>(k)]);
+        for (int k = 0; k < 16; ++k) cp_st(sm + 17 * CP * j + c + k * CP, w[outpos<16>(k)]);
     }
     __syncthreads();
     cp_mid_stages<N, +1, NT, true, CP>(sm, 0, g_tw4, tid);
@@ -684,7 +684,7 @@ __device__ __forceinline__ void cols_body_p(const PropParams &P, int c0, float4 
         const int b = tid + t * NT, c = b % CP, j = b / CP, kx = c0 + 2 * c;
         cpair v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = cp_ld(sm + pidx(j + r * B) * CP + c);
+        for (int r = 0; r < 16; ++r) v[r] = cp_ld(sm + pidx(j) * CP + c + r * (pstride<B>() * CP));
         cp_last_twiddle<N, +1>(v, j, g_tw4);
         cp_dft16_out_mid<+1>(v);
         if (kx < NX) {

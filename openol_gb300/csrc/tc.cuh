@@ -73,19 +73,25 @@ __device__ __forceinline__ void umma_commit(uint32_t mbar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
 
-// 32 lanes x 16 consecutive 32-bit TMEM columns -> 16 registers per thread
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+// TMEM -> registers, 32 lanes x 16 consecutive 32-bit columns per load.
+// Issue several loads, then one tmem_wait_ld, then tmem_regs_ready on each
+// destination.  The last step is an empty asm that
+// redefines the registers after the wait, so no use of them can be scheduled
+// before it.
+__device__ __forceinline__ void tmem_ld_async(uint32_t taddr, uint32_t (&r)[16])
 {
-    uint32_t r[16];
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
                  "%14, %15}, [%16];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
                    "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
                    "=r"(r[15])
                  : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_regs_ready(uint32_t (&r)[16])
+{
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(r[i]));
 }
 
 // Shared-memory matrix descriptor, K-major operand in the 128-byte swizzle

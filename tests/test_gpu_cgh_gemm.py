@@ -20,7 +20,10 @@ def host(t):
     return t.cpu().numpy().astype(np.complex128)
 
 
-@pytest.mark.parametrize("ny,nx,n", [(64, 96, 300), (37, 53, 1), (130, 260, 1000), (16, 16, 0)])
+# nx picks the N tile (fewest padded columns): 96, 53, 16 -> 128, 260 -> 160,
+# 384 -> 192, 448 -> 224, 512 -> 256 (1920 -> 240 in the workload test)
+@pytest.mark.parametrize("ny,nx,n", [(64, 96, 300), (37, 53, 1), (130, 260, 1000), (16, 16, 0),
+                                     (30, 384, 120), (24, 448, 150), (40, 512, 200)])
 def test_gemm_vs_oracle(ny, nx, n):
     rng = np.random.default_rng(ny * nx + n)
     p, lam = 8e-6, 532e-9
@@ -39,6 +42,22 @@ def test_gemm_vs_oracle(ny, nx, n):
     ref = O.cgh_fresnel(pts.astype(np.float64), ny, nx, p, p, lam, amp=amp.astype(np.float64),
                         phase0=ph.astype(np.float64))
     assert rel_l2(G, ref) < TOL
+
+
+def test_gemm_output_8_byte_aligned():
+    """An output that is 8- but not 16-byte aligned takes the one-complex
+    atomics (the paired ones need 16-byte alignment)."""
+    ny, nx, n, p, lam = 24, 64, 90, 8e-6, 532e-9
+    rng = np.random.default_rng(3)
+    pts = np.stack([rng.random(n) * nx * p, rng.random(n) * ny * p, 0.02 + rng.random(n) * 0.01], 1).astype(np.float32)
+    buf = torch.zeros(ny * nx + 1, dtype=torch.complex64, device="cuda")
+    U = buf[1:].view(ny, nx)
+    assert U.data_ptr() % 16 == 8
+    og.cgh_fresnel_gemm(og.gObject(pts), U, ny=ny, nx=nx, py=p, px=p, lam=lam)
+    og.device_fault_check()
+    assert buf[0].item() == 0
+    ref = O.cgh_fresnel(pts.astype(np.float64), ny, nx, p, p, lam)
+    assert rel_l2(host(U), ref) < TOL
 
 
 def test_gemm_workload_vs_direct_and_oracle():
