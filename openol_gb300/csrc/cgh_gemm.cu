@@ -14,9 +14,11 @@
 // (three K segments of one accumulation).  Issued tensor work 3 x 2 x 2M N 2K
 // = 24 M N K flop for 8 M N K useful.
 //
-// k_cgh_gemm_prep  per point, FP64: expansion coefficients of the x / y phases
-// k_cgh_gemm_ops   builds A_hi/A_lo/B_hi/B_lo (f16, K-contiguous, zero padded),
-//                  phases range-reduced exactly (frac_mul), MUFU sin/cos
+// k_cgh_gemm_prep  per point, FP64: the x / y phase polynomials as 64-bit
+//                  fixed-point fractions of a cycle
+// k_cgh_gemm_ops   builds A_hi/A_lo/B_hi/B_lo (f16, K-contiguous, zero padded):
+//                  phases stepped row to row exactly in 64-bit integers,
+//                  MUFU sin/cos
 // k_cgh_gemm<BN>   warp-specialised tcgen05 GEMM, one CTA per tile plus CTAs on
 //                  the spare SMs that take the tiles' K tails: warp 0 issues TMA loads into a
 //                  4-stage ring (128 x 64 A and BN x 64 B f16 tiles, 128-byte
@@ -55,10 +57,15 @@ struct GemmTile {
 };
 constexpr long long GB_WAIT = 4000000000LL; // ~2 s of SM clock per wait
 
+// Per point, the Fresnel phases of the B rows (w) and the A rows (h) as 64-bit
+// fixed-point fractions of a cycle (unit 2^-64):  cycles(w) = ax w^2 - bx w + gx
+// reduces mod 1 exactly in integer arithmetic (w is an integer, so the
+// integer parts of ax and bx drop out), and consecutive rows follow
+// P(w + 1) = P(w) + D(w), D(w + 1) = D(w) + 2 ax with no rounding at all.
 struct PointCoef {
-    float ax_hi, ax_lo, bx_hi, bx_lo, gx; // cycles(w) = ax w^2 - bx w + gx
-    float ay_hi, ay_lo, by_hi, by_lo, gy;
-    float cr, ci;                         // a_j e^{i phi_j}
+    unsigned long long ax, bx, gx; // frac(k2 px^2), frac(2 k2 px x), frac(k2 x^2), times 2^64
+    unsigned long long ay, by, gy;
+    float cr, ci;                  // a_j e^{i phi_j}
 };
 
 struct GemmOps {
@@ -69,6 +76,20 @@ struct GemmOps {
     __half *a_hi, *a_lo, *b_hi, *b_lo;
 };
 
+// frac(v) scaled to 2^64.  A double's 53 significant bits sit at or above
+// bit 0 of the result for |v| < 2^11 cycles, so the scaling and the
+// conversion are exact.
+__device__ __forceinline__ unsigned long long frac64(double v)
+{
+    double f = v - floor(v);
+    if (!(f < 1.0)) f = 0.0; // v - floor(v) can round up to 1 for tiny negative v
+    return __double2ull_rz(f * 18446744073709551616.0);
+}
+
+// 64 threads per CTA: the ~10^4 points spread over every SM (the FP64 work
+// per point is a few dozen operations).
+constexpr int PREP_THREADS = 64;
+
 __global__ void k_cgh_gemm_prep(GemmOps G)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -76,38 +97,46 @@ __global__ void k_cgh_gemm_prep(GemmOps G)
     const double x = G.pts[3 * j], y = G.pts[3 * j + 1], z = G.pts[3 * j + 2];
     const double k2 = 1.0 / (2.0 * G.lambda * z); // cycles per m^2
     PointCoef c;
-    auto put = [](double v, float &hi, float &lo) {
-        hi = (float)v;
-        lo = (float)(v - (double)hi);
-    };
-    put(k2 * G.px * G.px, c.ax_hi, c.ax_lo);
-    put(2.0 * k2 * G.px * x, c.bx_hi, c.bx_lo);
-    double g = k2 * x * x;
-    c.gx = (float)(g - rint(g));
-    put(k2 * G.py * G.py, c.ay_hi, c.ay_lo);
-    put(2.0 * k2 * G.py * y, c.by_hi, c.by_lo);
-    g = k2 * y * y;
-    c.gy = (float)(g - rint(g));
-    const double a = G.amp ? (double)G.amp[j] : 1.0;
-    const double ph = G.ph0 ? (double)G.ph0[j] : 0.0;
-    c.cr = (float)(a * cos(ph));
-    c.ci = (float)(a * sin(ph));
+    c.ax = frac64(k2 * G.px * G.px);
+    c.bx = frac64(2.0 * k2 * G.px * x);
+    c.gx = frac64(k2 * x * x);
+    c.ay = frac64(k2 * G.py * G.py);
+    c.by = frac64(2.0 * k2 * G.py * y);
+    c.gy = frac64(k2 * y * y);
+    // the complex amplitude is stored in FP32: FP32 sincosf (about 1 ulp) suffices
+    const float a = G.amp ? G.amp[j] : 1.f;
+    float sn = 0.f, cs = 1.f;
+    if (G.ph0) sincosf(G.ph0[j], &sn, &cs);
+    c.cr = a * cs;
+    c.ci = a * sn;
     G.coef[j] = c;
 }
 
-__device__ __forceinline__ void split2(float v, __half &hi, __half &lo)
+// exp(2 pi i P / 2^64): the top 32 bits as a signed fraction of a cycle in
+// [-1/2, 1/2), then MUFU sin / cos (about 4e-7 absolute there, below the
+// f16 hi + lo representation's 2^-22).
+__device__ __forceinline__ float2 cis_fixed(unsigned long long P)
 {
-    hi = __float2half_rn(v);
-    lo = __float2half_rn(v - __half2float(hi));
+    const float rad = (float)(int)(unsigned)(P >> 32) * 1.4629180792671596e-09f; // 2 pi / 2^32
+    float s, c;
+    __sincosf(rad, &s, &c);
+    return make_float2(c, s);
+}
+
+// f16 hi + lo of both components (packed conversions)
+__device__ __forceinline__ void split2(float2 v, unsigned &hi, unsigned &lo)
+{
+    const __half2 h = __float22half2_rn(v);
+    const float2 b = __half22float2(h);
+    const __half2 l = __float22half2_rn(make_float2(v.x - b.x, v.y - b.y));
+    hi = *reinterpret_cast<const unsigned *>(&h);
+    lo = *reinterpret_cast<const unsigned *>(&l);
 }
 
 // grid.x = point j (one per thread), grid.y = block of OPS_ROWS operand rows
-// (the nx rows of B, then the ny row pairs of A).  Each thread keeps its
-// point's coefficients in registers across the rows; for each row a warp
-// writes 32 consecutive points (128 contiguous bytes per f16 plane).
-// Phases are reduced exactly to [-0.5, 0.5] cycles (frac_mul on the FP64
-// coefficients) before the MUFU sin/cos, whose error there (~4e-7) is below
-// the f16 hi + lo representation (2^-22 relative).
+// (the nx rows of B, then the ny row pairs of A).  Each thread walks its rows
+// with the exact fixed-point recurrence; for each row a warp writes 32
+// consecutive points (128 contiguous bytes per f16 plane).
 constexpr int OPS_ROWS = 16;
 
 __global__ void k_cgh_gemm_ops(GemmOps G)
@@ -118,40 +147,46 @@ __global__ void k_cgh_gemm_ops(GemmOps G)
     PointCoef c{};
     if (live) c = G.coef[j];
     const int r0 = blockIdx.y * OPS_ROWS, r1 = min(r0 + OPS_ROWS, G.nx + G.ny);
-    for (int r = r0; r < r1; ++r) {
-        const bool isB = r < G.nx;
-        float re = 0.f, im = 0.f;
-        if (live) {
-            float s, co;
-            if (isB) {
-                const float w = (float)r;
-                const float cyc = frac_mul(c.ax_hi, c.ax_lo, w * w) - frac_mul(c.bx_hi, c.bx_lo, w) + c.gx;
-                __sincosf(6.283185307179586f * wrap_cycles(cyc), &s, &co);
-                re = co;
-                im = s;
-            } else {
-                const float h = (float)(r - G.nx);
-                const float cyc = frac_mul(c.ay_hi, c.ay_lo, h * h) - frac_mul(c.by_hi, c.by_lo, h) + c.gy;
-                __sincosf(6.283185307179586f * wrap_cycles(cyc), &s, &co);
-                re = c.cr * co - c.ci * s;
-                im = c.cr * s + c.ci * co;
-            }
-        }
-        __half hr, lr, hm, lm;
-        split2(re, hr, lr);
-        split2(im, hm, lm);
-        if (isB) {
+    // B rows: X[w, j] = exp(2 pi i cycles_x(w))
+    const int b1 = min(r1, G.nx);
+    if (r0 < b1) {
+        const unsigned long long w0 = (unsigned long long)r0;
+        unsigned long long P = c.ax * (w0 * w0) - c.bx * w0 + c.gx;
+        unsigned long long D = c.ax * (2 * w0 + 1) - c.bx;
+        const unsigned long long A2 = c.ax << 1;
+        for (int r = r0; r < b1; ++r) {
+            unsigned hi = 0u, lo = 0u;
+            if (live) split2(cis_fixed(P), hi, lo);
             const size_t o = (size_t)r * G.kp + 2 * j;
-            *reinterpret_cast<__half2 *>(G.b_hi + o) = __halves2half2(hr, hm);
-            *reinterpret_cast<__half2 *>(G.b_lo + o) = __halves2half2(lr, lm);
-        } else {
-            // row 2h: [re, -im] per point, row 2h + 1: [im, re]
+            *reinterpret_cast<unsigned *>(G.b_hi + o) = hi;
+            *reinterpret_cast<unsigned *>(G.b_lo + o) = lo;
+            P += D;
+            D += A2;
+        }
+    }
+    // A rows: Y'[h, j] = a_j e^{i phi_j} exp(2 pi i cycles_y(h)); row 2h holds
+    // [re, -im] per point, row 2h + 1 [im, re]
+    const int a0 = max(r0, G.nx);
+    if (a0 < r1) {
+        const unsigned long long h0 = (unsigned long long)(a0 - G.nx);
+        unsigned long long P = c.ay * (h0 * h0) - c.by * h0 + c.gy;
+        unsigned long long D = c.ay * (2 * h0 + 1) - c.by;
+        const unsigned long long A2 = c.ay << 1;
+        for (int r = a0; r < r1; ++r) {
+            unsigned hi = 0u, lo = 0u;
+            if (live) {
+                const float2 e = cis_fixed(P);
+                split2(make_float2(c.cr * e.x - c.ci * e.y, c.cr * e.y + c.ci * e.x), hi, lo);
+            }
             const int h = r - G.nx;
             const size_t o0 = (size_t)(2 * h) * G.kp + 2 * j, o1 = o0 + G.kp;
-            *reinterpret_cast<__half2 *>(G.a_hi + o0) = __halves2half2(hr, __hneg(hm));
-            *reinterpret_cast<__half2 *>(G.a_lo + o0) = __halves2half2(lr, __hneg(lm));
-            *reinterpret_cast<__half2 *>(G.a_hi + o1) = __halves2half2(hm, hr);
-            *reinterpret_cast<__half2 *>(G.a_lo + o1) = __halves2half2(lm, lr);
+            // the high 16 bits hold the imaginary half
+            *reinterpret_cast<unsigned *>(G.a_hi + o0) = hi ^ 0x80000000u;
+            *reinterpret_cast<unsigned *>(G.a_lo + o0) = lo ^ 0x80000000u;
+            *reinterpret_cast<unsigned *>(G.a_hi + o1) = __byte_perm(hi, 0u, 0x1032);
+            *reinterpret_cast<unsigned *>(G.a_lo + o1) = __byte_perm(lo, 0u, 0x1032);
+            P += D;
+            D += A2;
         }
     }
 }
@@ -523,7 +558,7 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
     const bool reuse = (flags & OLG_REUSE_OPERANDS) != 0;
     if (reuse && !work) return fail(OLG_ERR_INVALID_ARG, "OLG_REUSE_OPERANDS needs the caller's workspace");
     if (n_points > 0 && !reuse) {
-        k_cgh_gemm_prep<<<(n_points + 255) / 256, 256, 0, st>>>(G);
+        k_cgh_gemm_prep<<<(n_points + PREP_THREADS - 1) / PREP_THREADS, PREP_THREADS, 0, st>>>(G);
         count_launch();
         if (int rc = check_launch("k_cgh_gemm_prep")) return rc;
     }
