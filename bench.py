@@ -434,7 +434,7 @@ def wl_cgh(x, K, W, cpu):
     def step_exact():
         og.cgh_exact(obj, U, ny=c["ny"], nx=c["nx"], py=c["p"], px=c["p"], lam=c["lam"], amp=a, phase0=f)
 
-    tail_w = og.autotune_cgh_gemm(c["n"], c["ny"], c["nx"])
+    gemm_pairs, tail_w = og.autotune_cgh_gemm(c["n"], c["ny"], c["nx"])
     gws = og.cgh_gemm_workspace(c["n"], c["ny"], c["nx"])
 
     def step_gemm():
@@ -509,7 +509,7 @@ def wl_cgh(x, K, W, cpu):
         "dtype": "f16x3 split products, f32 accumulate",
         "config": {"workload": "cgh 1920x1080, 10000 points, p=8um, lambda=532nm, 5mm box at z=100mm",
                    "form": chosen, "l2": "flushed between steps (256 MiB write)",
-                   "gemm_tail_weight": tail_w},
+                   "gemm_tail_weight": tail_w, "gemm_tiles": "two-SM 256xBN" if gemm_pairs else "single-SM 128xBN"},
         "e2e": {"value": ws * units / (t_e2e * 1e-3), "unit": "point.pixel/s",
                 "h2d_bytes_per_step": pts.nbytes + amp.nbytes + ph.nbytes,
                 "d2h_bytes_per_step": c["ny"] * c["nx"] * 8},

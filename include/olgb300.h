@@ -346,15 +346,29 @@ int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, const float 
                              int ny, int nx, double py, double px, double lambda, int flags, void *work,
                              size_t work_bytes, olg_stream_t stream);
 /* Tuning hook of the GEMM's work split (no counterpart in the reference):
- * when a hologram has fewer 128 x 256 output tiles than the GPU has SMs, the
- * spare SMs take the last part of every tile's K range, and w is the cost of
- * one of their K blocks relative to a tile CTA's (default 1.2; 0 turns the
- * split off).  Sets w when 0 <= w <= 16 and returns the previous value. */
+ * when a hologram has fewer output tiles than the GPU has tile units (SMs, or
+ * SM pairs), the spare units take the last part of every tile's K range, and
+ * w is the cost of one of their K blocks relative to a tile unit's (default
+ * 1.2; 0 turns the split off).  Sets w when 0 <= w <= 16 and returns the
+ * previous value. */
 double olg_cgh_gemm_tail_weight(double w);
-/* Autotuner of that split (project-written; the reference has none): times
- * the GEMM for an n_points x ny x nx hologram at a few tail weights (0, 1.0 ..
- * 1.6; operands built once and reused, L2 flushed before every timed GEMM;
- * synchronises `stream`) and keeps the fastest for the rest of the process. */
+/* Accumulation length of the GEMM (no counterpart in the reference): K
+ * blocks of 64 (x 3 split products) summed in the tensor core's f32
+ * accumulator before each partial sum is added into f32 registers (default
+ * 8).  Longer chunks hand accumulators to the epilogue less often; shorter
+ * ones keep the tensor-core sums shorter.  Sets it for 1 <= kblocks <= 64
+ * and returns the previous value; other values only return it. */
+int olg_cgh_gemm_chunk(int kblocks);
+/* Tile form of the GEMM (no counterpart in the reference): 1 = 256 x BN tiles
+ * on pairs of SMs (a two-CTA cluster sharing each MMA), 0 = 128 x BN tiles on
+ * single SMs (the default).  Sets the form when on is 0 or 1 and returns
+ * the previous one; any other value only returns the current one. */
+int olg_cgh_gemm_pairs(int on);
+/* Autotuner of the tile form and that split (project-written; the reference
+ * has none): times the GEMM for an n_points x ny x nx hologram in both forms
+ * at a few tail weights (0, 1.0 .. 1.6; operands built once and reused, L2
+ * flushed before every timed GEMM; synchronises `stream`) and keeps the
+ * fastest for the rest of the process. */
 int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg_stream_t stream);
 /* Synchronises the device and reports (OLG_ERR_CUDA) whether a kernel of this
  * library with mbarrier waits (the tensor-core GEMM, the TMA-staged column

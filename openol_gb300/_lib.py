@@ -48,6 +48,8 @@ SIGNATURES = {
     "olg_asm_prop_noalloc_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _p]),
     "olg_tilted_workspace_bytes": (_sz, [_i, _i]),
     "olg_cgh_gemm_tail_weight": (_d, [_d]),
+    "olg_cgh_gemm_pairs": (_i, [_i]),
+    "olg_cgh_gemm_chunk": (_i, [_i]),
     "olg_tilted_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _i, _i, _i, _p, _sz, _p]),
     "olg_fresnel_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _i, _i, _p, _sz, _p]),
     "olg_arss_prop_c64": (_i, [_p, _p, _i, _i, _d, _d, _d, _d, _d, _d, _d, _i, _p, _sz, _p]),

@@ -110,10 +110,16 @@ def cgh_fresnel_gemm(gobj, U, *, ny, nx, py, px, lam, amp=None, phase0=None, acc
 
 
 def autotune_cgh_gemm(n_points, ny, nx, reps=5, stream=None):
-    """Time the GEMM's K-tail split for this hologram shape (olg_autotune_cgh_gemm)
-    and keep the fastest; returns the chosen tail weight."""
+    """Time the GEMM's tile form and K-tail split for this hologram shape
+    (olg_autotune_cgh_gemm) and keep the fastest; returns (pairs, tail weight)."""
     call("olg_autotune_cgh_gemm", int(n_points), int(ny), int(nx), int(reps), _stream(stream))
-    return float(lib().olg_cgh_gemm_tail_weight(-1.0))
+    return int(lib().olg_cgh_gemm_pairs(-1)), float(lib().olg_cgh_gemm_tail_weight(-1.0))
+
+
+def cgh_gemm_pairs(on=None):
+    """Tile form of the GEMM (olg_cgh_gemm_pairs): True = two-SM pairs,
+    False = single-SM tiles; None only reads it.  Returns the previous form."""
+    return bool(lib().olg_cgh_gemm_pairs(-1 if on is None else int(bool(on))))
 
 
 def cgh_gemm_workspace(n_points, ny, nx, device="cuda"):

@@ -198,6 +198,7 @@ struct GemmParams {
     int split;          // K blocks (of 3 kblocks) a tile's own CTA does
     int extra;          // CTAs beyond `tiles` that do the rest [split, 3 kblocks)
     int vec4;           // U is 16-byte aligned and n even: two complex values per atomic
+    int chunk;          // K blocks per TMEM accumulation before the f32 register add
     float2 *U;          // added to with atomics (zeroed first unless accumulating)
     int *err;
 };
@@ -210,31 +211,31 @@ struct GemmParams {
 // K range is a small slice of the operands that L2 holds.  Each piece (tile,
 // K range) is one accumulation, added into U with atomics when it ends; a
 // tile's two pieces add in either order.
-__device__ __forceinline__ int gemm_pieces(const GemmParams &P)
+// `u` is the CTA (single-SM tiles) or the CTA pair (two-SM tiles).
+__device__ __forceinline__ int gemm_pieces(const GemmParams &P, int u)
 {
-    if ((int)blockIdx.x < P.tiles) return 1;
-    const int e = blockIdx.x - P.tiles;
+    if (u < P.tiles) return 1;
+    const int e = u - P.tiles;
     return e < P.tiles ? (P.tiles - e + P.extra - 1) / P.extra : 0;
 }
-__device__ __forceinline__ void gemm_piece(const GemmParams &P, int p, int total, int &t, int &k0, int &k1)
+__device__ __forceinline__ void gemm_piece(const GemmParams &P, int u, int p, int total, int &t, int &k0, int &k1)
 {
-    if ((int)blockIdx.x < P.tiles) {
-        t = blockIdx.x;
+    if (u < P.tiles) {
+        t = u;
         k0 = 0;
         k1 = P.split;
     } else {
-        t = (int)blockIdx.x - P.tiles + p * P.extra;
+        t = u - P.tiles + p * P.extra;
         k0 = P.split;
         k1 = total;
     }
 }
 
-// Accumulation within a piece: the MMA warp writes chunks of GB_CHUNK
+// Accumulation within a piece: the MMA warp writes chunks of P.chunk
 // K-blocks alternately into two TMEM accumulators (BN columns each); the 8 epilogue
 // warps add every finished chunk into f32 registers (rounded adds) while the
 // next chunk runs, so the tensor pipe's own accumulation never spans more
-// than GB_CHUNK x 64 x 3 products.
-constexpr int GB_CHUNK = 8;
+// than P.chunk x 64 x 3 products (default 8: 1536 products).
 constexpr int GB_EPI_WARPS = 8;
 constexpr int GB_THREADS = 64 + 32 * GB_EPI_WARPS;
 constexpr uint32_t GB_TMEM_COLS = 512; // two accumulators, at columns 0 and 256
@@ -329,7 +330,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int total = 3 * P.kblocks; // K blocks per tile
-    const int np = gemm_pieces(P);
+    const int np = gemm_pieces(P, blockIdx.x);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < GB_STAGES; ++s) {
@@ -357,7 +358,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
             int i = 0, issued = 0;
             for (int p = 0; p < np && !*fault; ++p) {
                 int t, k0, k1;
-                gemm_piece(P, p, total, t, k0, k1);
+                gemm_piece(P, blockIdx.x, p, total, t, k0, k1);
                 const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * BN;
                 for (int kb = k0; kb < k1 && !*fault; ++kb, ++i) {
                     const int s = i % GB_STAGES;
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
             int c = 0, i = 0; // chunk and stage counters over all pieces
             for (int p = 0; p < np && !*fault; ++p) {
                 int t, k0, k1;
-                gemm_piece(P, p, total, t, k0, k1);
+                gemm_piece(P, blockIdx.x, p, total, t, k0, k1);
                 for (int kb = k0; kb < k1 && !*fault; ++c) {
                     const int b = c & 1;
                     if (c >= 2 && !mbar_wait(smem_u32(tfree + b), (uint32_t)((c >> 1) - 1) & 1u, GB_WAIT)) {
@@ -394,7 +395,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                     }
                     tc_fence_after();
                     const uint32_t d = tmem + (uint32_t)(b * 256);
-                    const int kend = min(k1, kb + GB_CHUNK);
+                    const int kend = min(k1, kb + P.chunk);
                     for (int kc = kb; kc < kend; ++kc, ++i) {
                         const int s = i % GB_STAGES;
                         if (!mbar_wait(smem_u32(full + s), (uint32_t)(i / GB_STAGES) & 1u, GB_WAIT)) {
@@ -421,7 +422,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
         int c = 0;
         for (int p = 0; p < np && ok; ++p) {
             int t, k0, k1;
-            gemm_piece(P, p, total, t, k0, k1);
+            gemm_piece(P, blockIdx.x, p, total, t, k0, k1);
             float acc[128];
 #pragma unroll
             for (int i = 0; i < 128; ++i) acc[i] = 0.f;
@@ -442,7 +443,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                 __syncwarp();
                 if (lane == 0)
                     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tfree + b)) : "memory");
-                kb = min(k1, kb + GB_CHUNK);
+                kb = min(k1, kb + P.chunk);
             }
             const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * BN;
             const int row = m0 + 32 * q + lane; // row of D
@@ -455,10 +456,196 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
     if (threadIdx.x == 0 && *fault) atomicExch(P.err, 1);
 }
 
+// ------------------------------------------------- two-SM tiles (CTA pairs)
+// The same GEMM with 256 x BN tiles on a cluster of two CTAs (cta_group::2).
+// CTA r of the pair loads A rows [128 r, +128) and B rows [BN/2 r, +BN/2) of
+// the tile into its own shared memory; the even CTA issues the M = 256 MMAs,
+// which read both CTAs' halves, and each CTA's TMEM receives its own 128 rows
+// of D.  Each SM then stages 31 KB per K block for the same tensor work that
+// takes 46 KB on a single-SM 128 x 240 tile, so shared memory (TMA writes
+// plus MMA operand reads) is lighter, and the smaller stages fit a 6-deep
+// ring.  Measured on 1920 x 1080 x 10^4: the same issued-flop rate as the
+// single-SM form (~1.5 PFLOP/s), so there the single-SM form's finer M
+// padding (2176 vs 2304 rows of D) wins; the autotuner picks per shape.
+//
+// Barriers: full[s] of the even CTA counts both CTAs' TMA bytes (its
+// producer posts the expected total; the odd CTA's loads complete on it
+// through its cluster address); empty[s] and tfull[b] live in both CTAs and
+// receive the MMA commits by multicast; tfree[b] of the even CTA collects the
+// 16 epilogue warps of the pair.  Every wait is bounded, and both CTAs meet
+// at a cluster barrier before TMEM is released and either exits, so no CTA
+// leaves while its peer may still touch its shared memory.
+constexpr int G2_STAGES = 6;
+template <int BN>
+struct Gemm2Tile {
+    static_assert(BN % 16 == 0 && BN >= 128 && BN <= 256, "N tile");
+    static constexpr int BH = BN / 2;                  // B rows per CTA (a multiple of 8)
+    static constexpr int B_BYTES = BH * GB_K * 2;      // a multiple of 1024
+    static constexpr int STAGE = GB_A_BYTES + B_BYTES; // bytes one CTA loads per K block
+    // + B_BYTES of slack at the end: every B descriptor's reach, even a whole
+    // BN-row tile from the last stage, stays inside the allocation
+    static constexpr int SMEM = G2_STAGES * STAGE + 1024 + 256 + B_BYTES;
+};
+
+template <int BN>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_THREADS, 1)
+    k_cgh_gemm2(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
+                const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, GemmParams P)
+{
+    using T = Gemm2Tile<BN>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + G2_STAGES * GB_A_BYTES;
+    uint64_t *full = (uint64_t *)(sB + G2_STAGES * T::B_BYTES);
+    uint64_t *empty = full + G2_STAGES;
+    uint64_t *tfull = empty + G2_STAGES; // [2]
+    uint64_t *tfree = tfull + 2;         // [2]
+    uint32_t *tmem_slot = (uint32_t *)(tfree + 2);
+    volatile int *fault = (volatile int *)(tmem_slot + 1);
+
+    const uint32_t rank = cluster_ctarank();
+    const bool lead = rank == 0;
+    const int pair = blockIdx.x >> 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int total = 3 * P.kblocks;
+    const int np = gemm_pieces(P, pair);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < G2_STAGES; ++s) {
+            mbar_init(smem_u32(full + s), 1);
+            mbar_init(smem_u32(empty + s), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(tfull + b), 1);
+            mbar_init(smem_u32(tfree + b), 2 * GB_EPI_WARPS);
+        }
+        *fault = 0;
+        fence_mbar_init();
+    }
+    if (warp == 1) {
+        tmem_alloc_pair(smem_u32(tmem_slot), GB_TMEM_COLS);
+        tmem_relinquish_pair();
+    }
+    tc_fence_before();
+    cluster_sync(); // both CTAs' barriers initialised and TMEM allocated
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            const uint32_t full_lead = mapa_shared(smem_u32(full), 0);
+            int i = 0, issued = 0;
+            for (int p = 0; p < np && !*fault; ++p) {
+                int t, k0, k1;
+                gemm_piece(P, pair, p, total, t, k0, k1);
+                const int m0 = (t / P.tiles_n) * (2 * GB_M) + (int)rank * GB_M;
+                const int n0 = (t % P.tiles_n) * BN + (int)rank * T::BH;
+                for (int kb = k0; kb < k1 && !*fault; ++kb, ++i) {
+                    const int s = i % G2_STAGES;
+                    const uint32_t ph = (uint32_t)(i / G2_STAGES) & 1u;
+                    if (!mbar_wait(smem_u32(empty + s), ph ^ 1u, GB_WAIT)) {
+                        *fault = 1;
+                        break;
+                    }
+                    const int seg = kb / P.kblocks, kk = (kb % P.kblocks) * GB_K;
+                    const CUtensorMap *ma = seg < 2 ? &tAh : &tAl;
+                    const CUtensorMap *mb = seg == 1 ? &tBl : &tBh;
+                    if (lead) mbar_expect_tx(smem_u32(full + s), 2 * T::STAGE);
+                    tma_load_2d_pair(smem_u32(sA + s * GB_A_BYTES), ma, full_lead + 8u * s, kk, m0);
+                    tma_load_2d_pair(smem_u32(sB + s * T::B_BYTES), mb, full_lead + 8u * s, kk, n0);
+                    issued = i + 1;
+                }
+            }
+            // the even CTA's full barriers track both CTAs' copies: never
+            // leave with any in flight
+            if (lead)
+                for (int j = issued > G2_STAGES ? issued - G2_STAGES : 0; j < issued; ++j)
+                    mbar_wait(smem_u32(full + j % G2_STAGES), (uint32_t)(j / G2_STAGES) & 1u, GB_WAIT);
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && lead) {
+            constexpr uint32_t idesc = idesc_f16_f32(2 * GB_M, BN);
+            int c = 0, i = 0;
+            for (int p = 0; p < np && !*fault; ++p) {
+                int t, k0, k1;
+                gemm_piece(P, pair, p, total, t, k0, k1);
+                for (int kb = k0; kb < k1 && !*fault; ++c) {
+                    const int b = c & 1;
+                    if (c >= 2 && !mbar_wait(smem_u32(tfree + b), (uint32_t)((c >> 1) - 1) & 1u, GB_WAIT)) {
+                        *fault = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d = tmem + (uint32_t)(b * 256);
+                    const int kend = min(k1, kb + P.chunk);
+                    for (int kc = kb; kc < kend; ++kc, ++i) {
+                        const int s = i % G2_STAGES;
+                        if (!mbar_wait(smem_u32(full + s), (uint32_t)(i / G2_STAGES) & 1u, GB_WAIT)) {
+                            *fault = 1;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * T::B_BYTES);
+#pragma unroll
+                        for (int k = 0; k < GB_K / 16; ++k)
+                            umma_f16_pair(d, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), idesc,
+                                          (kc > kb || k > 0) ? 1u : 0u);
+                        umma_commit_pair(smem_u32(empty + s), 3);
+                    }
+                    umma_commit_pair(smem_u32(tfull + b), 3);
+                    kb = kend;
+                }
+            }
+        }
+    } else {
+        const int q = warp & 3, half = (warp - 2) >> 2;
+        const int nch = max(0, min(128, BN - 128 * half)) / 16;
+        const uint32_t tfree_lead = mapa_shared(smem_u32(tfree), 0);
+        bool ok = true;
+        int c = 0;
+        for (int p = 0; p < np && ok; ++p) {
+            int t, k0, k1;
+            gemm_piece(P, pair, p, total, t, k0, k1);
+            float acc[128];
+#pragma unroll
+            for (int i = 0; i < 128; ++i) acc[i] = 0.f;
+            for (int kb = k0; kb < k1; ++c) {
+                const int b = c & 1;
+                if (!mbar_wait(smem_u32(tfull + b), (uint32_t)(c >> 1) & 1u, GB_WAIT)) {
+                    *fault = 1;
+                    ok = false;
+                }
+                if (!ok || *fault) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                drain_cols<BN == 224 || BN == 240>(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * 256 + 128 * half),
+                                                   nch, acc);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive_remote(tfree_lead + 8u * b);
+                kb = min(k1, kb + P.chunk);
+            }
+            const int m0 = (t / P.tiles_n) * (2 * GB_M) + (int)rank * GB_M, n0 = (t % P.tiles_n) * BN;
+            const int row = m0 + 32 * q + lane; // row of D
+            store_cols(P, acc, nch, ok && row < P.m2, row & 1, row >> 1, n0 + 128 * half);
+        }
+    }
+    __syncwarp();
+    tc_fence_before();
+    cluster_sync(); // neither CTA releases TMEM or exits while its peer still works
+    if (warp == 1) tmem_dealloc_pair(tmem, GB_TMEM_COLS);
+    if (threadIdx.x == 0 && *fault) atomicExch(P.err, 1);
+}
+
 // ------------------------------------------------------------------ host
 namespace {
 
 std::atomic<double> g_tail_weight{1.2};
+std::atomic<int> g_pairs{0}; // single-SM tiles unless switched (or autotuned) to pairs
+std::atomic<int> g_chunk{8};
 std::mutex g_encode_mu;
 
 int make_map(CUtensorMap *m, void *base, uint64_t rows, uint64_t kp, uint32_t box_rows)
@@ -492,17 +679,73 @@ int pick_bn(int nx)
     return best;
 }
 
-int gemm_smem_optin()
+constexpr int BN_LIST[] = {256, 240, 224, 192, 160, 128};
+int bn_index(int bn)
 {
-    cudaError_t e = cudaSuccess;
-    if ((e = cudaFuncSetAttribute(k_cgh_gemm<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<256>::SMEM)) ||
-        (e = cudaFuncSetAttribute(k_cgh_gemm<240>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<240>::SMEM)) ||
-        (e = cudaFuncSetAttribute(k_cgh_gemm<224>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<224>::SMEM)) ||
-        (e = cudaFuncSetAttribute(k_cgh_gemm<192>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<192>::SMEM)) ||
-        (e = cudaFuncSetAttribute(k_cgh_gemm<160>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<160>::SMEM)) ||
-        (e = cudaFuncSetAttribute(k_cgh_gemm<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<128>::SMEM)))
-        return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm)");
+    for (int i = 0; i < 6; ++i)
+        if (BN_LIST[i] == bn) return i;
+    return 5;
+}
+
+// one tile width: both kernels' shared-memory opt-in, and how many CTA pairs
+// can be resident at once
+template <int BN>
+int gemm_setup(int *pairs)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_cgh_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmTile<BN>::SMEM);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm)");
+    e = cudaFuncSetAttribute(k_cgh_gemm2<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Gemm2Tile<BN>::SMEM);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_cgh_gemm2)");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2, 1, 1);
+    cfg.blockDim = dim3(GB_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = Gemm2Tile<BN>::SMEM;
+    e = cudaOccupancyMaxActiveClusters(pairs, k_cgh_gemm2<BN>, &cfg);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveClusters(k_cgh_gemm2)");
     return OLG_OK;
+}
+
+struct GemmDevice {
+    int nsm = 0;
+    int pairs[6] = {};
+};
+
+// per context, once: the opt-ins, the SM count and the resident pair counts
+int gemm_device(GemmDevice *out)
+{
+    static std::map<unsigned long long, GemmDevice> cache;
+    unsigned long long ctx = 0;
+    if (int rc = context_id(&ctx)) return rc;
+    std::lock_guard<std::mutex> lk(g_encode_mu);
+    auto it = cache.find(ctx);
+    if (it == cache.end()) {
+        GemmDevice d;
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+        e = cudaDeviceGetAttribute(&d.nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(SM count)");
+        int rc = gemm_setup<256>(&d.pairs[0]);
+        if (!rc) rc = gemm_setup<240>(&d.pairs[1]);
+        if (!rc) rc = gemm_setup<224>(&d.pairs[2]);
+        if (!rc) rc = gemm_setup<192>(&d.pairs[3]);
+        if (!rc) rc = gemm_setup<160>(&d.pairs[4]);
+        if (!rc) rc = gemm_setup<128>(&d.pairs[5]);
+        if (rc) return rc;
+        it = cache.emplace(ctx, d).first;
+    }
+    *out = it->second;
+    return OLG_OK;
+}
+
+template <int BN>
+void launch_gemm(bool pair, int units, const CUtensorMap &a_hi, const CUtensorMap &a_lo, const CUtensorMap &b_hi,
+                 const CUtensorMap &b_lo, const GemmParams &P, cudaStream_t st)
+{
+    if (pair)
+        k_cgh_gemm2<BN><<<2 * units, GB_THREADS, Gemm2Tile<BN>::SMEM, st>>>(a_hi, a_lo, b_hi, b_lo, P);
+    else
+        k_cgh_gemm<BN><<<units, GB_THREADS, GemmTile<BN>::SMEM, st>>>(a_hi, a_lo, b_hi, b_lo, P);
 }
 
 size_t gemm_layout(int n, int ny, int nx, int *kp_out, size_t off[5])
@@ -568,53 +811,40 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
         count_launch();
         if (int rc = check_launch("k_cgh_gemm_ops")) return rc;
     }
+    const int bn = pick_bn(nx);
+    const bool pair = g_pairs.load(std::memory_order_relaxed) != 0;
+    GemmDevice dev{};
+    if (int rc = gemm_device(&dev)) return rc;
+    const int units_max = pair ? dev.pairs[bn_index(bn)] : dev.nsm; // CTAs or CTA pairs resident at once
+    if (units_max < 1) return fail(OLG_ERR_CUDA, "k_cgh_gemm: no resident CTA (pair) fits");
     CUtensorMap mAh, mAl, mBh, mBl;
     if (int rc = make_map(&mAh, G.a_hi, 2 * (uint64_t)ny, kp, GB_M)) return rc;
     if (int rc = make_map(&mAl, G.a_lo, 2 * (uint64_t)ny, kp, GB_M)) return rc;
-    const int bn = pick_bn(nx);
-    if (int rc = make_map(&mBh, G.b_hi, nx, kp, bn)) return rc;
-    if (int rc = make_map(&mBl, G.b_lo, nx, kp, bn)) return rc;
+    if (int rc = make_map(&mBh, G.b_hi, nx, kp, pair ? bn / 2 : bn)) return rc;
+    if (int rc = make_map(&mBl, G.b_lo, nx, kp, pair ? bn / 2 : bn)) return rc;
     GemmParams P{};
     P.m2 = 2 * ny;
     P.n = nx;
     P.kblocks = kp / GB_K;
     P.tiles_n = (nx + bn - 1) / bn;
-    const long long tiles = (long long)P.tiles_n * ((2 * ny + GB_M - 1) / GB_M);
+    const int tile_m = pair ? 2 * GB_M : GB_M;
+    const long long tiles = (long long)P.tiles_n * ((2 * ny + tile_m - 1) / tile_m);
     P.tiles = (int)tiles;
     P.U = (float2 *)U;
     P.vec4 = ((uintptr_t)U % 16 == 0 && nx % 2 == 0) ? 1 : 0;
+    P.chunk = g_chunk.load(std::memory_order_relaxed);
     P.err = err;
-    // per context, once: the shared-memory opt-in and the SM count
-    static std::map<unsigned long long, int> sm_count;
-    unsigned long long ctx = 0;
-    if (int rc = context_id(&ctx)) return rc;
-    int nsm = 0;
-    {
-        std::lock_guard<std::mutex> lk(g_encode_mu);
-        auto it = sm_count.find(ctx);
-        if (it == sm_count.end()) {
-            int dev = 0;
-            cudaError_t e = cudaGetDevice(&dev);
-            if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-            if (int rc = gemm_smem_optin()) return rc;
-            int n = 0;
-            e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-            if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(SM count)");
-            it = sm_count.emplace(ctx, n).first;
-        }
-        nsm = it->second;
-    }
     const double tw = g_tail_weight.load(std::memory_order_relaxed);
-    // SMs left over after one CTA per tile (one CTA per SM: ~197 KB of shared
-    // memory) take the K tails: with e extra CTAs each holds `per` tails.  A
-    // tail K block costs g_tail_weight tile K blocks (its operands are not
-    // shared in L2 with other CTAs at the time), so split = total per w /
-    // (per w + 1) evens the two kinds of CTA; w <= 0 turns the split off.
+    // Units (CTAs, or CTA pairs) left over after one per tile take the K
+    // tails: with e extra units each holds `per` tails.  A tail K block costs
+    // g_tail_weight tile K blocks (its operands are not shared in L2 with
+    // other units at the time), so split = total per w / (per w + 1) evens
+    // the two kinds of unit; w <= 0 turns the split off.
     const int total = 3 * P.kblocks;
     P.split = total;
     P.extra = 0;
-    if (tiles < nsm && tw > 0.0) {
-        const int e = nsm - (int)tiles;
+    if (tiles < units_max && tw > 0.0) {
+        const int e = units_max - (int)tiles;
         const int per = ((int)tiles + e - 1) / e;
         const double pw = per * tw;
         const int split = (int)((double)total * pw / (pw + 1.0));
@@ -627,17 +857,29 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
         const cudaError_t e = cudaMemsetAsync(U, 0, sizeof(float2) * (size_t)ny * nx, st);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
     }
-    const int grid = (int)tiles + P.extra;
+    const int units = (int)tiles + P.extra;
     switch (bn) {
-    case 256: k_cgh_gemm<256><<<grid, GB_THREADS, GemmTile<256>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
-    case 240: k_cgh_gemm<240><<<grid, GB_THREADS, GemmTile<240>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
-    case 224: k_cgh_gemm<224><<<grid, GB_THREADS, GemmTile<224>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
-    case 192: k_cgh_gemm<192><<<grid, GB_THREADS, GemmTile<192>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
-    case 160: k_cgh_gemm<160><<<grid, GB_THREADS, GemmTile<160>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
-    default: k_cgh_gemm<128><<<grid, GB_THREADS, GemmTile<128>::SMEM, st>>>(mAh, mAl, mBh, mBl, P); break;
+    case 256: launch_gemm<256>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    case 240: launch_gemm<240>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    case 224: launch_gemm<224>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    case 192: launch_gemm<192>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    case 160: launch_gemm<160>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    default: launch_gemm<128>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
     }
     count_launch();
-    return check_launch("k_cgh_gemm");
+    return check_launch(pair ? "k_cgh_gemm2" : "k_cgh_gemm");
+}
+
+extern "C" int olg_cgh_gemm_chunk(int kblocks)
+{
+    if (kblocks >= 1 && kblocks <= 64) return g_chunk.exchange(kblocks);
+    return g_chunk.load();
+}
+
+extern "C" int olg_cgh_gemm_pairs(int on)
+{
+    if (on == 0 || on == 1) return g_pairs.exchange(on);
+    return g_pairs.load();
 }
 
 extern "C" double olg_cgh_gemm_tail_weight(double w)
@@ -646,11 +888,12 @@ extern "C" double olg_cgh_gemm_tail_weight(double w)
     return g_tail_weight.load();
 }
 
-// Times the GEMM on the caller's hologram shape and point count for a few
-// K-tail weights (the work split between tile CTAs and the spare SMs' tail
-// CTAs) and keeps the fastest.  Operands are built once (a unit-amplitude
-// cloud spread over the hologram at 0.1 m; the split depends on the shape,
-// not on the values) and reused; every timed GEMM starts from a cold L2.
+// Times the GEMM on the caller's hologram shape and point count for each
+// tile form (two-SM pairs, single-SM tiles) and a few K-tail weights (the
+// work split between tile units and the spare SMs' tail units), and keeps
+// the fastest.  Operands are built once (a unit-amplitude cloud spread over
+// the hologram at 0.1 m; the choice depends on the shape, not on the values)
+// and reused; every timed GEMM starts from a cold L2.
 extern "C" int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg_stream_t stream)
 {
     if (n_points <= 0 || ny <= 0 || nx <= 0 || ny > 4096 || nx > 4096)
@@ -673,11 +916,19 @@ extern "C" int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg
     cudaError_t e = cudaMemcpyAsync(pts.ptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (autotune points)");
     const double keep = g_tail_weight.load();
+    const int keep_pairs = g_pairs.load();
+    auto restore = [&] {
+        g_tail_weight.store(keep);
+        g_pairs.store(keep_pairs);
+    };
     auto run = [&](int flags) {
         return olg_cgh_fresnel_gemm_c64((const float *)pts.ptr, nullptr, nullptr, n_points, U.ptr, ny, nx, 8e-6,
                                         8e-6, 532e-9, flags, ws.ptr, wb, stream);
     };
-    if (int rc = run(0)) return rc; // builds the operands
+    if (int rc = run(0)) { // builds the operands
+        restore();
+        return rc;
+    }
     struct Events {
         cudaEvent_t a = nullptr, b = nullptr;
         ~Events()
@@ -690,34 +941,40 @@ extern "C" int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg
         return cuda_fail(e, "cudaEventCreate");
     const double cand[] = {0.0, 1.0, 1.1, 1.2, 1.3, 1.45, 1.6};
     double best_w = keep;
+    int best_p = keep_pairs;
     float best = 1e30f;
-    for (double w : cand) {
-        g_tail_weight.store(w);
-        float tot = 0.f;
-        for (int r = 0; r < reps; ++r) {
-            if ((e = cudaMemsetAsync(flush.ptr, r & 0xff, flush_bytes, st)) != cudaSuccess ||
-                (e = cudaEventRecord(ev.a, st)) != cudaSuccess) {
-                g_tail_weight.store(keep);
-                return cuda_fail(e, "autotune timing");
+    for (int pr = 1; pr >= 0; --pr) {
+        g_pairs.store(pr);
+        for (double w : cand) {
+            g_tail_weight.store(w);
+            float tot = 0.f;
+            for (int r = 0; r < reps; ++r) {
+                if ((e = cudaMemsetAsync(flush.ptr, r & 0xff, flush_bytes, st)) != cudaSuccess ||
+                    (e = cudaEventRecord(ev.a, st)) != cudaSuccess) {
+                    restore();
+                    return cuda_fail(e, "autotune timing");
+                }
+                if (int rc = run(OLG_REUSE_OPERANDS)) {
+                    restore();
+                    return rc;
+                }
+                float t = 0.f;
+                if ((e = cudaEventRecord(ev.b, st)) != cudaSuccess || (e = cudaEventSynchronize(ev.b)) != cudaSuccess ||
+                    (e = cudaEventElapsedTime(&t, ev.a, ev.b)) != cudaSuccess) {
+                    restore();
+                    return cuda_fail(e, "autotune timing");
+                }
+                tot += t;
             }
-            if (int rc = run(OLG_REUSE_OPERANDS)) {
-                g_tail_weight.store(keep);
-                return rc;
+            if (tot < best) {
+                best = tot;
+                best_w = w;
+                best_p = pr;
             }
-            float t = 0.f;
-            if ((e = cudaEventRecord(ev.b, st)) != cudaSuccess || (e = cudaEventSynchronize(ev.b)) != cudaSuccess ||
-                (e = cudaEventElapsedTime(&t, ev.a, ev.b)) != cudaSuccess) {
-                g_tail_weight.store(keep);
-                return cuda_fail(e, "autotune timing");
-            }
-            tot += t;
-        }
-        if (tot < best) {
-            best = tot;
-            best_w = w;
         }
     }
     g_tail_weight.store(best_w);
+    g_pairs.store(best_p);
     return OLG_OK;
 }
 

@@ -94,6 +94,73 @@ __device__ __forceinline__ void tmem_regs_ready(uint32_t (&r)[16])
     for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(r[i]));
 }
 
+// ------------------------------------------------ CTA pairs (cta_group::2)
+// A cluster of two CTAs shares one MMA: the even CTA issues M = 256 MMAs whose
+// A rows 0-127 and first half of B sit in its own shared memory and rows
+// 128-255 and the second half of B at the same offsets in its peer; each CTA's
+// TMEM holds its own 128 rows of D.
+
+__device__ __forceinline__ uint32_t cluster_ctarank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// all threads of both CTAs: barrier with release / acquire at cluster scope
+__device__ __forceinline__ void cluster_sync()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// the shared::cluster address of the same variable in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t a, uint32_t rank)
+{
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+// arrive on an mbarrier given by its shared::cluster address (default
+// .release.cta semantics: the arriving warp's own tcgen05 loads have already
+// completed, tcgen05.wait::ld, so no cluster-scope fence is needed)
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr)
+{
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+// TMA load into this CTA's shared memory, completing on an mbarrier in either
+// CTA of the pair (`mbar` a shared::cluster address)
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap *map, uint32_t mbar, int x, int y)
+{
+    asm volatile("cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+                 ::"r"(dst), "l"((uint64_t)map), "r"(mbar), "r"(x), "r"(y)
+                 : "memory");
+}
+// executed by one warp in each CTA of the pair
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t slot, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish_pair()
+{
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void umma_f16_pair(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                 ::"r"(d), "l"(a), "l"(b), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+// arrive once on `mbar` (same offset) in every CTA of `mask` when this thread's
+// earlier MMAs have completed
+__device__ __forceinline__ void umma_commit_pair(uint32_t mbar, uint16_t mask)
+{
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                 ::"r"(mbar), "h"(mask)
+                 : "memory");
+}
+
 // Shared-memory matrix descriptor, K-major operand in the 128-byte swizzle
 // layout TMA writes with CU_TENSOR_MAP_SWIZZLE_128B: rows of 128 B (64 f16),
 // 8-row groups 1024 B apart (stride byte offset), descriptor version 1,

@@ -76,6 +76,18 @@ def test_tuning_knobs_without_gpu():
     assert L.olg_cgh_gemm_tail_weight(2.0) == w
     assert L.olg_cgh_gemm_tail_weight(99.0) == 2.0
     assert L.olg_cgh_gemm_tail_weight(w) == 2.0
+    # GEMM tile form: 0 / 1 set it, anything else only reads it
+    f = L.olg_cgh_gemm_pairs(-1)
+    assert f == 0
+    assert L.olg_cgh_gemm_pairs(1) == 0
+    assert L.olg_cgh_gemm_pairs(7) == 1
+    assert L.olg_cgh_gemm_pairs(f) == 1
+    # GEMM accumulation chunk: 1..64 K blocks
+    ch = L.olg_cgh_gemm_chunk(-1)
+    assert ch == 8
+    assert L.olg_cgh_gemm_chunk(16) == 8
+    assert L.olg_cgh_gemm_chunk(0) == 16 and L.olg_cgh_gemm_chunk(65) == 16
+    assert L.olg_cgh_gemm_chunk(ch) == 16
 
 
 def test_auto_checks_match_reference_float_and_double(golden):

@@ -15,6 +15,15 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-5
 
 
+@pytest.fixture(params=[True, False], ids=["pairs", "single"], autouse=True)
+def tile_form(request):
+    """Every test runs on both tile forms: two-SM 256 x BN tiles (CTA pairs
+    sharing each MMA) and single-SM 128 x BN tiles."""
+    prev = og.cgh_gemm_pairs(request.param)
+    yield request.param
+    og.cgh_gemm_pairs(prev)
+
+
 def host(t):
     torch.cuda.synchronize()
     return t.cpu().numpy().astype(np.complex128)
