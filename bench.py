@@ -66,9 +66,9 @@ ADAM = dict(n=2048, p=6.4e-6, lam=532e-9, planes=8, z0=0.08, dz=0.01, lr=0.05, s
 # kernels each roofline covers, from ncu captures of this bench's own timed
 # region (--ncu-range); the profile file named beside each holds the command.
 TRAFFIC = {
-    "cgh": (544.8e6 + 17.4e6, "k_cgh_gemm, profiles/cgh_gemm_1920x1080_10k.md"),
+    "cgh": (553.6e6 + 15.6e6, "k_cgh_gemm, profiles/cgh_gemm_1920x1080_10k.md"),
     "asm": ((8.5 + 16.9 + 16.8) * 1e6, "the three passes, profiles/asm_1024_kernels.md (S stays in L2)"),
-    "wrp": ((134.3 + 204.7 + 268.6 + 211.7 + 268.6 + 99.8) * 1e6,
+    "wrp": ((134.4 + 205.0 + 268.5 + 211.6 + 268.5 + 99.1) * 1e6,
             "the three 8192-point passes of step 2, profiles/asm_4096_to_8192_wrp_step2.md"),
 }
 
