@@ -256,6 +256,18 @@ typedef struct olg_batch_plan_s *olg_batch_plan;
 int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_batch_plan *plan);
 int olg_batch_execute(olg_batch_plan plan, olg_stream_t stream);
 int olg_batch_execute_serial(olg_batch_plan plan, olg_stream_t stream);
+/* The plan's fields from host buffers and back (the reference's host-field
+ * calls copy in and out around every propagation): host_in[i] (ny x nx
+ * complex64) is copied into field i's `in`, the plan runs, and field i's `out`
+ * is copied into host_out[i].  The copies in, the propagations and the copies
+ * out are pipelined over two copy streams owned by the plan and `stream`:
+ * the persistent kernel's fields arrive first and it starts at once, each
+ * large field's passes start when that field has arrived, and each result
+ * leaves when it is computed.  Ordered on `stream` like olg_batch_execute
+ * (synchronize it before reading host_out).  Pinned host buffers give
+ * asynchronous copies; pageable ones work but copy synchronously. */
+int olg_batch_execute_host(olg_batch_plan plan, const void *const *host_in, void *const *host_out,
+                           olg_stream_t stream);
 /* Synchronous: OLG_ERR_CUDA if an item of the last execution gave up on its bounded wait. */
 int olg_batch_check(olg_batch_plan plan);
 /* For tests of the bounded waits (no counterpart in the reference): raises by

@@ -65,6 +65,7 @@ SIGNATURES = {
     "olg_batch_plan_direct_fields": (_i, [_p]),
     "olg_batch_execute": (_i, [_p, _p]),
     "olg_batch_execute_serial": (_i, [_p, _p]),
+    "olg_batch_execute_host": (_i, [_p, _p, _p, _p]),
     "olg_batch_check": (_i, [_p]),
     "olg_batch_plan_items": (_i, [_p]),
     "olg_batch_plan_destroy": (_i, [_p]),

@@ -43,6 +43,26 @@ class BatchPlan:
         for the large ones (capturable in a CUDA graph)."""
         call("olg_batch_execute", self._plan, _stream(stream))
 
+    def execute_host(self, host_in, host_out, stream=None):
+        """The plan's fields from host tensors and back (olg_batch_execute_host):
+        ``host_in[i]`` is copied into field i's input, the plan runs, and field i's
+        output is copied into ``host_out[i]``, with the copies in, the propagations
+        and the copies out pipelined over three streams.  Host tensors: CPU
+        complex64 of each field's shape, contiguous; pinned memory
+        (``pin_memory()``) for the copies to run asynchronously.  Ordered on
+        ``stream``: synchronize it before reading ``host_out``."""
+        if len(host_in) != self.n_fields or len(host_out) != self.n_fields:
+            raise ValueError("one host tensor per field, in and out")
+        for t in list(host_in) + list(host_out):
+            if t.is_cuda or t.dtype != torch.complex64 or not t.is_contiguous():
+                raise TypeError("host fields must be contiguous CPU complex64 tensors")
+        for t, d in zip(host_in, self._keep[0::2]):
+            if tuple(t.shape) != tuple(d.shape):
+                raise ValueError("host field shape differs from the plan's")
+        hin = (C.c_void_p * self.n_fields)(*[t.data_ptr() for t in host_in])
+        hout = (C.c_void_p * self.n_fields)(*[t.data_ptr() for t in host_out])
+        call("olg_batch_execute_host", self._plan, hin, hout, _stream(stream))
+
     def execute_serial(self, stream=None):
         """The same fields one after another through the single-field entry points."""
         call("olg_batch_execute_serial", self._plan, _stream(stream))

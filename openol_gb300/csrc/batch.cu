@@ -151,6 +151,9 @@ struct olg_batch_plan_s {
     size_t bytes = 0;
     BatchDev D{};
     size_t counters_off = 0, counters_bytes = 0;
+    // olg_batch_execute_host: copy streams and events, made on first use
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    std::vector<cudaEvent_t> ev; // entry, small inputs in, small done, out done, per field: in, computed
 };
 
 namespace olg {
@@ -353,6 +356,106 @@ extern "C" int olg_batch_execute(olg_batch_plan plan, olg_stream_t stream)
     return OLG_OK;
 }
 
+namespace olg {
+namespace {
+
+int host_pipeline_init(olg_batch_plan plan)
+{
+    if (plan->s_in) return OLG_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&plan->s_in, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&plan->s_out, cudaStreamNonBlocking);
+    const int n_ev = 4 + 2 * plan->n;
+    for (int i = 0; e == cudaSuccess && i < n_ev; ++i) {
+        cudaEvent_t v = nullptr;
+        e = cudaEventCreateWithFlags(&v, cudaEventDisableTiming);
+        if (e == cudaSuccess) plan->ev.push_back(v);
+    }
+    return e == cudaSuccess ? OLG_OK : cuda_fail(e, "creating the batch copy streams");
+}
+
+int copy_field(void *dst, const void *src, const olg_field &F, cudaMemcpyKind kind, cudaStream_t st)
+{
+    const cudaError_t e = cudaMemcpyAsync(dst, src, sizeof(float2) * (size_t)F.ny * F.nx, kind, st);
+    return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaMemcpyAsync (batch field)");
+}
+
+} // namespace
+} // namespace olg
+
+// Host fields in and out, pipelined over three streams.  The copy-in stream
+// brings every persistent-kernel field first, then the large fields one by
+// one; the caller's stream runs the persistent launch as soon as its fields
+// have arrived and each large field's passes as soon as that field has; the
+// copy-out stream returns each result as soon as it is computed.  So the
+// copies in, the propagations and the copies out overlap, and a step takes
+// about the longest of the three instead of their sum.  Both copy streams
+// first wait for the caller's stream, and the caller's stream waits for the
+// last copy out, so the call is ordered on `stream` like olg_batch_execute.
+extern "C" int olg_batch_execute_host(olg_batch_plan plan, const void *const *host_in, void *const *host_out,
+                                      olg_stream_t stream)
+{
+    if (!plan) return fail(OLG_ERR_INVALID_ARG, "null plan");
+    if (!host_in || !host_out) return fail(OLG_ERR_INVALID_ARG, "null host field arrays");
+    for (int i = 0; i < plan->n; ++i)
+        if (!host_in[i] || !host_out[i]) return fail(OLG_ERR_INVALID_ARG, "null host field");
+    if (int rc = host_pipeline_init(plan)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t *ev = plan->ev.data();
+    cudaEvent_t e_entry = ev[0], e_small_in = ev[1], e_small_done = ev[2], e_out_done = ev[3];
+    cudaEvent_t *e_in = ev + 4, *e_done = ev + 4 + plan->n;
+    auto ck = [](cudaError_t e, const char *what) { return e == cudaSuccess ? OLG_OK : cuda_fail(e, what); };
+    if (int rc = ck(cudaEventRecord(e_entry, st), "cudaEventRecord")) return rc;
+    if (int rc = ck(cudaStreamWaitEvent(plan->s_in, e_entry, 0), "cudaStreamWaitEvent")) return rc;
+    if (int rc = ck(cudaStreamWaitEvent(plan->s_out, e_entry, 0), "cudaStreamWaitEvent")) return rc;
+    // the persistent kernel's fields
+    for (int i = 0; i < plan->n; ++i)
+        if (!plan->direct[i])
+            if (int rc = copy_field((void *)plan->fields[i].in, host_in[i], plan->fields[i], cudaMemcpyHostToDevice,
+                                    plan->s_in))
+                return rc;
+    if (int rc = ck(cudaEventRecord(e_small_in, plan->s_in), "cudaEventRecord")) return rc;
+    // the large fields, in order
+    for (int i = 0; i < plan->n; ++i)
+        if (plan->direct[i]) {
+            if (int rc = copy_field((void *)plan->fields[i].in, host_in[i], plan->fields[i], cudaMemcpyHostToDevice,
+                                    plan->s_in))
+                return rc;
+            if (int rc = ck(cudaEventRecord(e_in[i], plan->s_in), "cudaEventRecord")) return rc;
+        }
+    // compute on the caller's stream: the persistent launch, then each large field
+    if (int rc = ck(cudaStreamWaitEvent(st, e_small_in, 0), "cudaStreamWaitEvent")) return rc;
+    cudaError_t e = cudaMemsetAsync(plan->D.done, 0, plan->counters_bytes, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(plan->D.head, 0, 2 * sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync (batch counters)");
+    if (plan->n_items > 0) {
+        plan->D.wait = wait_budget_cycles();
+        k_batch<<<plan->grid, BATCH_NT, BATCH_SMEM, st>>>(plan->D);
+        count_launch();
+        if (int rc = check_launch("k_batch")) return rc;
+    }
+    if (int rc = ck(cudaEventRecord(e_small_done, st), "cudaEventRecord")) return rc;
+    if (int rc = ck(cudaStreamWaitEvent(plan->s_out, e_small_done, 0), "cudaStreamWaitEvent")) return rc;
+    for (int i = 0; i < plan->n; ++i)
+        if (!plan->direct[i])
+            if (int rc = copy_field(host_out[i], plan->fields[i].out, plan->fields[i], cudaMemcpyDeviceToHost,
+                                    plan->s_out))
+                return rc;
+    for (int i = 0; i < plan->n; ++i)
+        if (plan->direct[i]) {
+            if (int rc = ck(cudaStreamWaitEvent(st, e_in[i], 0), "cudaStreamWaitEvent")) return rc;
+            if (int rc = batch_field_direct(plan, i, st)) return rc;
+            if (int rc = ck(cudaEventRecord(e_done[i], st), "cudaEventRecord")) return rc;
+            if (int rc = ck(cudaStreamWaitEvent(plan->s_out, e_done[i], 0), "cudaStreamWaitEvent")) return rc;
+            if (int rc = copy_field(host_out[i], plan->fields[i].out, plan->fields[i], cudaMemcpyDeviceToHost,
+                                    plan->s_out))
+                return rc;
+        }
+    // the caller's stream resumes after the last copy out (and the copy-in
+    // stream has finished before the last computation, which waited on it)
+    if (int rc = ck(cudaEventRecord(e_out_done, plan->s_out), "cudaEventRecord")) return rc;
+    return ck(cudaStreamWaitEvent(st, e_out_done, 0), "cudaStreamWaitEvent");
+}
+
 extern "C" int olg_batch_execute_serial(olg_batch_plan plan, olg_stream_t stream)
 {
     if (!plan) return fail(OLG_ERR_INVALID_ARG, "null plan");
@@ -404,6 +507,9 @@ extern "C" int olg_batch_plan_raise_target(olg_batch_plan plan, int field, int s
 extern "C" int olg_batch_plan_destroy(olg_batch_plan plan)
 {
     if (!plan) return OLG_OK;
+    for (cudaEvent_t v : plan->ev) cudaEventDestroy(v);
+    if (plan->s_in) cudaStreamDestroy(plan->s_in);
+    if (plan->s_out) cudaStreamDestroy(plan->s_out);
     cudaError_t e = cudaFree(plan->mem);
     delete plan;
     return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaFree (batch plan)");
