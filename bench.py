@@ -462,9 +462,16 @@ def wl_cgh(x, K, W, cpu):
     def step_adj_exact():
         og.cgh_exact_adjoint(obj, Gadj, gadj, ny=c["ny"], nx=c["nx"], py=c["p"], px=c["p"], lam=c["lam"], work=aws)
 
+    agws = og.cgh_adjoint_gemm_workspace(c["n"], c["ny"], c["nx"])
+
+    def step_adj_gemm():
+        og.cgh_fresnel_adjoint_gemm(obj, Gadj, gadj, ny=c["ny"], nx=c["nx"], py=c["p"], px=c["p"], lam=c["lam"],
+                                    work=agws)
+
     forms = {"fresnel_gemm": step_gemm, "fresnel_gemm_kernel_only": step_gemm_only,
              "fresnel_direct": step_fresnel, "exact": step_exact, "plain_simt": step_plain,
-             "fresnel_adjoint": step_adj_fresnel, "exact_adjoint": step_adj_exact}
+             "fresnel_adjoint": step_adj_fresnel, "fresnel_adjoint_gemm": step_adj_gemm,
+             "exact_adjoint": step_adj_exact}
     chosen = "fresnel_gemm"
     res = {}
     with ClockSampler(local) as clk:

@@ -340,6 +340,17 @@ int olg_cgh_exact_c64(const float *points, const float *amp, const float *phase0
  * adds into g.  Scratch: olg_cgh_adjoint_workspace_bytes (work == NULL:
  * stream-ordered pool). */
 size_t olg_cgh_adjoint_workspace_bytes(int n_points, int ny, int nx, int exact);
+/* The Fresnel adjoint above on the tensor cores: T = G conj(X) as the same
+ * split-FP16 tcgen05 GEMM as olg_cgh_fresnel_gemm_c64 (M = ny, N = n_points,
+ * K = nx; G scaled by a power of two so its f16 operands stay in [-1, 1]),
+ * then g_j = sum_h conj(Y[h, j]) T[h, j] summed over row bands in a fixed
+ * order (deterministic).  Same arguments and flags as
+ * olg_cgh_fresnel_adjoint_c64; nx, ny <= 4096.  Scratch:
+ * olg_cgh_adjoint_gemm_workspace_bytes (work == NULL: stream-ordered pool). */
+size_t olg_cgh_adjoint_gemm_workspace_bytes(int n_points, int ny, int nx);
+int olg_cgh_fresnel_adjoint_gemm_c64(const float *points, int n_points, const void *G, void *g, int ny, int nx,
+                                     double py, double px, double lambda, int flags, void *work, size_t work_bytes,
+                                     olg_stream_t stream);
 int olg_cgh_fresnel_adjoint_c64(const float *points, int n_points, const void *G, void *g, int ny, int nx, double py,
                                 double px, double lambda, int flags, void *work, size_t work_bytes,
                                 olg_stream_t stream);

@@ -81,6 +81,8 @@ SIGNATURES = {
     "olg_inject_alloc_failures": (_i, [_i]),
     "olg_batch_plan_raise_target": (_i, [_p, _i, _i, _i]),
     "olg_cgh_fresnel_adjoint_c64": (_i, [_p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_cgh_fresnel_adjoint_gemm_c64": (_i, [_p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_cgh_adjoint_gemm_workspace_bytes": (_sz, [_i, _i, _i]),
     "olg_cgh_exact_adjoint_c64": (_i, [_p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),
     "olg_cgh_gemm_workspace_bytes": (_sz, [_i, _i, _i]),
     "olg_cgh_fresnel_gemm_c64": (_i, [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),

@@ -90,6 +90,18 @@ def cgh_fresnel_adjoint(gobj, G, g=None, *, ny, nx, py, px, lam, accumulate=Fals
     return _cgh_adjoint("olg_cgh_fresnel_adjoint_c64", gobj, G, g, ny, nx, py, px, lam, accumulate, stream, work)
 
 
+def cgh_fresnel_adjoint_gemm(gobj, G, g=None, *, ny, nx, py, px, lam, accumulate=False, stream=None, work=None):
+    """The Fresnel adjoint on the tensor cores (olg_cgh_fresnel_adjoint_gemm_c64):
+    the same g_j as cgh_fresnel_adjoint, through T = G conj(X) as a split-FP16
+    tcgen05 GEMM and a per-point reduction over rows."""
+    return _cgh_adjoint("olg_cgh_fresnel_adjoint_gemm_c64", gobj, G, g, ny, nx, py, px, lam, accumulate, stream, work)
+
+
+def cgh_adjoint_gemm_workspace(n_points, ny, nx, device="cuda"):
+    return torch.empty(int(lib().olg_cgh_adjoint_gemm_workspace_bytes(n_points, ny, nx)), dtype=torch.uint8,
+                       device=device)
+
+
 def cgh_exact_adjoint(gobj, G, g=None, *, ny, nx, py, px, lam, accumulate=False, stream=None, work=None):
     """Adjoint of the exact spherical CGH (olg_cgh_exact_adjoint_c64):
     g_j = sum_{h,w} conj(exp(i k r_j) / r_j) G[h,w]."""

@@ -191,6 +191,135 @@ __global__ void k_cgh_gemm_ops(GemmOps G)
     }
 }
 
+// ------------------------------------------- adjoint (transposed sum)
+// g_j = sum_{h,w} conj(X[w, j] Y[h, j]) G[h, w] (unit-weight kernels) as
+//   T = G conj(X)          (M = ny, N = points, K = nx: the same GEMM)
+//   g_j = sum_h conj(Y[h, j]) T[h, j]   (a per-point reduction over h)
+// A holds G scaled by 2^-e (e from max |Re G|, |Im G|: the f16 operands stay
+// in [-1, 1]; the scale is undone exactly in the reduction), rows 2h / 2h + 1
+// as [re, -im] / [im, re] per column; B row j holds conj(X[., j]) as
+// [re, -im] per column, stepped along w with the fixed-point recurrence.
+
+// max over |Re G|, |Im G| into *mx (non-negative floats order as their bits)
+__global__ void k_cgh_absmax(const float2 *G, long long count, unsigned *mx)
+{
+    float m = 0.f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+        const float2 v = G[i];
+        m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mx, __float_as_uint(m));
+}
+
+// 2^-e with max = m 2^e, m in [0.5, 1); 1 for a zero or non-finite max
+__device__ __forceinline__ float adj_scale(unsigned mx)
+{
+    const float m = __uint_as_float(mx);
+    if (!(m > 0.f) || !(m < INFINITY)) return 1.f;
+    int e = 0;
+    frexpf(m, &e);
+    return ldexpf(1.f, -e);
+}
+
+// A: grid.x over K columns (kp / 2 of them, the padding written as zeros),
+// grid.y over rows h
+__global__ void k_cgh_adjt_aops(const float2 *G, int ny, int nx, int kp, const unsigned *mx, __half *a_hi,
+                                __half *a_lo)
+{
+    const int w = blockIdx.x * blockDim.x + threadIdx.x, h = blockIdx.y;
+    if (w >= kp / 2 || h >= ny) return;
+    unsigned hi = 0u, lo = 0u;
+    if (w < nx) {
+        const float s = adj_scale(*mx);
+        const float2 v = G[(size_t)h * nx + w];
+        split2(make_float2(v.x * s, v.y * s), hi, lo);
+    }
+    const size_t o0 = (size_t)(2 * h) * kp + 2 * w, o1 = o0 + kp;
+    *reinterpret_cast<unsigned *>(a_hi + o0) = hi ^ 0x80000000u;
+    *reinterpret_cast<unsigned *>(a_lo + o0) = lo ^ 0x80000000u;
+    *reinterpret_cast<unsigned *>(a_hi + o1) = __byte_perm(hi, 0u, 0x1032);
+    *reinterpret_cast<unsigned *>(a_lo + o1) = __byte_perm(lo, 0u, 0x1032);
+}
+
+// B: one thread per (point j, 16 columns from 16 blockIdx.y), 64 contiguous
+// bytes per f16 plane
+__global__ void k_cgh_adjt_bops(GemmOps G)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= G.n) return;
+    const int w0 = blockIdx.y * 16;
+    const PointCoef c = G.coef[j];
+    const unsigned long long u0 = (unsigned long long)w0;
+    unsigned long long P = c.ax * (u0 * u0) - c.bx * u0 + c.gx;
+    unsigned long long D = c.ax * (2 * u0 + 1) - c.bx;
+    const unsigned long long A2 = c.ax << 1;
+    unsigned hi[16], lo[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        hi[i] = 0u;
+        lo[i] = 0u;
+        if (w0 + i < G.nx) {
+            const float2 e = cis_fixed(P);
+            split2(make_float2(e.x, -e.y), hi[i], lo[i]);
+        }
+        P += D;
+        D += A2;
+    }
+    uint4 *dh = reinterpret_cast<uint4 *>(G.b_hi + (size_t)j * G.kp + 2 * w0);
+    uint4 *dl = reinterpret_cast<uint4 *>(G.b_lo + (size_t)j * G.kp + 2 * w0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        dh[q] = make_uint4(hi[4 * q], hi[4 * q + 1], hi[4 * q + 2], hi[4 * q + 3]);
+        dl[q] = make_uint4(lo[4 * q], lo[4 * q + 1], lo[4 * q + 2], lo[4 * q + 3]);
+    }
+}
+
+// part[b][j] = sum over the rows h of band b of conj(Y[h, j]) T[h, j]
+constexpr int ADJT_BAND = 64;
+__global__ void k_cgh_adjt_rows(const PointCoef *coef, const float2 *T, int n, int ny, float2 *part)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (j >= n) return;
+    const int h0 = b * ADJT_BAND, h1 = min(ny, h0 + ADJT_BAND);
+    const PointCoef c = coef[j];
+    const unsigned long long u0 = (unsigned long long)h0;
+    unsigned long long P = c.ay * (u0 * u0) - c.by * u0 + c.gy;
+    unsigned long long D = c.ay * (2 * u0 + 1) - c.by;
+    const unsigned long long A2 = c.ay << 1;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int h = h0; h < h1; ++h) {
+        const float2 e = cis_fixed(P), t = T[(size_t)h * n + j];
+        acc.x = fmaf(e.x, t.x, fmaf(e.y, t.y, acc.x)); // conj(e) t
+        acc.y = fmaf(e.x, t.y, fmaf(-e.y, t.x, acc.y));
+        P += D;
+        D += A2;
+    }
+    part[(size_t)b * n + j] = acc;
+}
+
+// g_j (+)= 2^e sum_b part[b][j], bands added in a fixed order
+__global__ void k_cgh_adjt_sum(const float2 *part, int bands, int n, const unsigned *mx, float2 *g, int accumulate)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    float2 s = make_float2(0.f, 0.f);
+    for (int b = 0; b < bands; ++b) {
+        const float2 v = part[(size_t)b * n + j];
+        s.x += v.x;
+        s.y += v.y;
+    }
+    const float inv = 1.f / adj_scale(*mx); // a power of two: exact
+    s.x *= inv;
+    s.y *= inv;
+    if (accumulate) {
+        const float2 o = g[j];
+        s.x += o.x;
+        s.y += o.y;
+    }
+    g[j] = s;
+}
+
 struct GemmParams {
     int m2, n, kblocks; // rows of D (2 ny), columns (nx), K blocks of 64 per segment
     int tiles_n;        // N tiles across D
@@ -761,7 +890,95 @@ size_t gemm_layout(int n, int ny, int nx, int *kp_out, size_t off[5])
     return o;
 }
 
+// adjoint workspace: coefficients, A hi/lo (2 ny x kp), B hi/lo (n x kp),
+// T (ny x n complex64), per-band partial sums, the max word
+size_t adjt_layout(int n, int ny, int nx, int *kp_out, int *bands_out, size_t off[8])
+{
+    const int kp = (int)align_up((size_t)2 * nx, GB_K);
+    const int bands = (ny + ADJT_BAND - 1) / ADJT_BAND;
+    const size_t np = (size_t)(n > 0 ? n : 1);
+    size_t o = 0;
+    off[0] = o; o += align_up(np * sizeof(PointCoef) + 16, 1024);
+    off[1] = o; o += align_up((size_t)2 * ny * kp * 2, 1024);
+    off[2] = o; o += align_up((size_t)2 * ny * kp * 2, 1024);
+    off[3] = o; o += align_up(np * kp * 2, 1024);
+    off[4] = o; o += align_up(np * kp * 2, 1024);
+    off[5] = o; o += align_up((size_t)ny * np * sizeof(float2), 1024);
+    off[6] = o; o += align_up((size_t)bands * np * sizeof(float2), 1024);
+    off[7] = o; o += 1024;
+    if (kp_out) *kp_out = kp;
+    if (bands_out) *bands_out = bands;
+    return o;
+}
+
 } // namespace
+
+// D = A B^T on the tensor cores into the complex64 field U ((m2 / 2) x n_cols,
+// row stride n_cols): A (m2 x kp) and B (n_cols x kp) split-f16 operands,
+// K-contiguous, three K segments (hi.hi, hi.lo, lo.hi).  Zeroes U first
+// unless accumulating.
+int gemm_run(const __half *a_hi, const __half *a_lo, const __half *b_hi, const __half *b_lo, int m2, int n_cols,
+             int kp, float2 *U, bool accumulate, int *err, cudaStream_t st)
+{
+    const int bn = pick_bn(n_cols);
+    const bool pair = g_pairs.load(std::memory_order_relaxed) != 0;
+    GemmDevice dev{};
+    if (int rc = gemm_device(&dev)) return rc;
+    const int units_max = pair ? dev.pairs[bn_index(bn)] : dev.nsm; // CTAs or CTA pairs resident at once
+    if (units_max < 1) return fail(OLG_ERR_CUDA, "k_cgh_gemm: no resident CTA (pair) fits");
+    CUtensorMap mAh, mAl, mBh, mBl;
+    if (int rc = make_map(&mAh, (void *)a_hi, (uint64_t)m2, kp, GB_M)) return rc;
+    if (int rc = make_map(&mAl, (void *)a_lo, (uint64_t)m2, kp, GB_M)) return rc;
+    if (int rc = make_map(&mBh, (void *)b_hi, (uint64_t)n_cols, kp, pair ? bn / 2 : bn)) return rc;
+    if (int rc = make_map(&mBl, (void *)b_lo, (uint64_t)n_cols, kp, pair ? bn / 2 : bn)) return rc;
+    GemmParams P{};
+    P.m2 = m2;
+    P.n = n_cols;
+    P.kblocks = kp / GB_K;
+    P.tiles_n = (n_cols + bn - 1) / bn;
+    const int tile_m = pair ? 2 * GB_M : GB_M;
+    const long long tiles = (long long)P.tiles_n * ((m2 + tile_m - 1) / tile_m);
+    P.tiles = (int)tiles;
+    P.U = U;
+    P.vec4 = ((uintptr_t)U % 16 == 0 && n_cols % 2 == 0) ? 1 : 0;
+    P.chunk = g_chunk.load(std::memory_order_relaxed);
+    P.err = err;
+    const double tw = g_tail_weight.load(std::memory_order_relaxed);
+    // Units (CTAs, or CTA pairs) left over after one per tile take the K
+    // tails: with e extra units each holds `per` tails.  A tail K block costs
+    // g_tail_weight tile K blocks (its operands are not shared in L2 with
+    // other units at the time), so split = total per w / (per w + 1) evens
+    // the two kinds of unit; w <= 0 turns the split off.
+    const int total = 3 * P.kblocks;
+    P.split = total;
+    P.extra = 0;
+    if (tiles < units_max && tw > 0.0) {
+        const int e = units_max - (int)tiles;
+        const int per = ((int)tiles + e - 1) / e;
+        const double pw = per * tw;
+        const int split = (int)((double)total * pw / (pw + 1.0));
+        if (split > 0 && split < total) {
+            P.split = split;
+            P.extra = std::min(e, (int)tiles);
+        }
+    }
+    if (!accumulate) {
+        const cudaError_t e = cudaMemsetAsync(U, 0, sizeof(float2) * (size_t)(m2 / 2) * n_cols, st);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    }
+    const int units = (int)tiles + P.extra;
+    switch (bn) {
+    case 256: launch_gemm<256>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    case 240: launch_gemm<240>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    case 224: launch_gemm<224>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    case 192: launch_gemm<192>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    case 160: launch_gemm<160>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    default: launch_gemm<128>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
+    }
+    count_launch();
+    return check_launch(pair ? "k_cgh_gemm2" : "k_cgh_gemm");
+}
+
 } // namespace olg
 
 using namespace olg;
@@ -811,63 +1028,72 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
         count_launch();
         if (int rc = check_launch("k_cgh_gemm_ops")) return rc;
     }
-    const int bn = pick_bn(nx);
-    const bool pair = g_pairs.load(std::memory_order_relaxed) != 0;
-    GemmDevice dev{};
-    if (int rc = gemm_device(&dev)) return rc;
-    const int units_max = pair ? dev.pairs[bn_index(bn)] : dev.nsm; // CTAs or CTA pairs resident at once
-    if (units_max < 1) return fail(OLG_ERR_CUDA, "k_cgh_gemm: no resident CTA (pair) fits");
-    CUtensorMap mAh, mAl, mBh, mBl;
-    if (int rc = make_map(&mAh, G.a_hi, 2 * (uint64_t)ny, kp, GB_M)) return rc;
-    if (int rc = make_map(&mAl, G.a_lo, 2 * (uint64_t)ny, kp, GB_M)) return rc;
-    if (int rc = make_map(&mBh, G.b_hi, nx, kp, pair ? bn / 2 : bn)) return rc;
-    if (int rc = make_map(&mBl, G.b_lo, nx, kp, pair ? bn / 2 : bn)) return rc;
-    GemmParams P{};
-    P.m2 = 2 * ny;
-    P.n = nx;
-    P.kblocks = kp / GB_K;
-    P.tiles_n = (nx + bn - 1) / bn;
-    const int tile_m = pair ? 2 * GB_M : GB_M;
-    const long long tiles = (long long)P.tiles_n * ((2 * ny + tile_m - 1) / tile_m);
-    P.tiles = (int)tiles;
-    P.U = (float2 *)U;
-    P.vec4 = ((uintptr_t)U % 16 == 0 && nx % 2 == 0) ? 1 : 0;
-    P.chunk = g_chunk.load(std::memory_order_relaxed);
-    P.err = err;
-    const double tw = g_tail_weight.load(std::memory_order_relaxed);
-    // Units (CTAs, or CTA pairs) left over after one per tile take the K
-    // tails: with e extra units each holds `per` tails.  A tail K block costs
-    // g_tail_weight tile K blocks (its operands are not shared in L2 with
-    // other units at the time), so split = total per w / (per w + 1) evens
-    // the two kinds of unit; w <= 0 turns the split off.
-    const int total = 3 * P.kblocks;
-    P.split = total;
-    P.extra = 0;
-    if (tiles < units_max && tw > 0.0) {
-        const int e = units_max - (int)tiles;
-        const int per = ((int)tiles + e - 1) / e;
-        const double pw = per * tw;
-        const int split = (int)((double)total * pw / (pw + 1.0));
-        if (split > 0 && split < total) {
-            P.split = split;
-            P.extra = std::min(e, (int)tiles);
-        }
-    }
-    if (!(flags & OLG_ACCUMULATE)) {
-        const cudaError_t e = cudaMemsetAsync(U, 0, sizeof(float2) * (size_t)ny * nx, st);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
-    }
-    const int units = (int)tiles + P.extra;
-    switch (bn) {
-    case 256: launch_gemm<256>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
-    case 240: launch_gemm<240>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
-    case 224: launch_gemm<224>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
-    case 192: launch_gemm<192>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
-    case 160: launch_gemm<160>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
-    default: launch_gemm<128>(pair, units, mAh, mAl, mBh, mBl, P, st); break;
-    }
+    return gemm_run(G.a_hi, G.a_lo, G.b_hi, G.b_lo, 2 * ny, nx, kp, (float2 *)U, (flags & OLG_ACCUMULATE) != 0, err,
+                    st);
+}
+
+extern "C" size_t olg_cgh_adjoint_gemm_workspace_bytes(int n_points, int ny, int nx)
+{
+    if (n_points <= 0 || ny <= 0 || nx <= 0) return 0;
+    size_t off[8];
+    return adjt_layout(n_points, ny, nx, nullptr, nullptr, off);
+}
+
+extern "C" int olg_cgh_fresnel_adjoint_gemm_c64(const float *points, int n_points, const void *G, void *g, int ny,
+                                                int nx, double py, double px, double lambda, int flags, void *work,
+                                                size_t work_bytes, olg_stream_t stream)
+{
+    if (n_points < 0 || ny <= 0 || nx <= 0) return fail(OLG_ERR_INVALID_ARG, "bad sizes");
+    if (nx > 4096 || ny > 4096) return fail(OLG_ERR_UNSUPPORTED_SIZE, "hologram side must be <= 4096");
+    if (n_points > 0 && (!points || !G || !g)) return fail(OLG_ERR_INVALID_ARG, "null pointer");
+    if (((uintptr_t)G & 7) || ((uintptr_t)g & 7)) return fail(OLG_ERR_INVALID_ARG, "G and g must be 8-byte aligned");
+    if (!(px > 0) || !(py > 0) || !(lambda > 0)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    if (n_points == 0) return OLG_OK;
+    int *err = nullptr;
+    if (int rc = device_fault_word(&err)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    int kp = 0, bands = 0;
+    size_t off[8];
+    const size_t need = adjt_layout(n_points, ny, nx, &kp, &bands, off);
+    Scratch sc;
+    if (int rc = sc.acquire(work, work_bytes, need, st)) return rc;
+    char *base = (char *)sc.ptr;
+    GemmOps O{};
+    O.pts = points; O.n = n_points; O.ny = ny; O.nx = nx; O.kp = kp;
+    O.px = px; O.py = py; O.lambda = lambda;
+    O.coef = (PointCoef *)(base + off[0]);
+    O.a_hi = (__half *)(base + off[1]);
+    O.a_lo = (__half *)(base + off[2]);
+    O.b_hi = (__half *)(base + off[3]);
+    O.b_lo = (__half *)(base + off[4]);
+    float2 *T = (float2 *)(base + off[5]);
+    float2 *part = (float2 *)(base + off[6]);
+    unsigned *mx = (unsigned *)(base + off[7]);
+    const float2 *Gf = (const float2 *)G;
+    k_cgh_gemm_prep<<<(n_points + PREP_THREADS - 1) / PREP_THREADS, PREP_THREADS, 0, st>>>(O);
     count_launch();
-    return check_launch(pair ? "k_cgh_gemm2" : "k_cgh_gemm");
+    if (int rc = check_launch("k_cgh_gemm_prep")) return rc;
+    cudaError_t e = cudaMemsetAsync(mx, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    const long long cnt = (long long)ny * nx;
+    const int mb = (int)std::min<long long>((cnt + 255) / 256, 1024); // grid-stride beyond that
+    k_cgh_absmax<<<mb, 256, 0, st>>>(Gf, cnt, mx);
+    count_launch();
+    if (int rc = check_launch("k_cgh_absmax")) return rc;
+    k_cgh_adjt_aops<<<dim3((kp / 2 + 127) / 128, ny), 128, 0, st>>>(Gf, ny, nx, kp, mx, O.a_hi, O.a_lo);
+    count_launch();
+    if (int rc = check_launch("k_cgh_adjt_aops")) return rc;
+    k_cgh_adjt_bops<<<dim3((n_points + 127) / 128, kp / 32), 128, 0, st>>>(O);
+    count_launch();
+    if (int rc = check_launch("k_cgh_adjt_bops")) return rc;
+    if (int rc = gemm_run(O.a_hi, O.a_lo, O.b_hi, O.b_lo, 2 * ny, n_points, kp, T, false, err, st)) return rc;
+    k_cgh_adjt_rows<<<dim3((n_points + 127) / 128, bands), 128, 0, st>>>(O.coef, T, n_points, ny, part);
+    count_launch();
+    if (int rc = check_launch("k_cgh_adjt_rows")) return rc;
+    k_cgh_adjt_sum<<<(n_points + 255) / 256, 256, 0, st>>>(part, bands, n_points, mx, (float2 *)g,
+                                                          (flags & OLG_ACCUMULATE) ? 1 : 0);
+    count_launch();
+    return check_launch("k_cgh_adjt_sum");
 }
 
 extern "C" int olg_cgh_gemm_chunk(int kblocks)

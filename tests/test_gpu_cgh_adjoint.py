@@ -18,9 +18,9 @@ from test_gpu_cgh import config2_points
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-5
-FWD = {"fresnel": og.cgh_fresnel, "exact": og.cgh_exact}
-ADJ = {"fresnel": og.cgh_fresnel_adjoint, "exact": og.cgh_exact_adjoint}
-ORA = {"fresnel": O.cgh_fresnel_adjoint, "exact": O.cgh_exact_adjoint}
+FWD = {"fresnel": og.cgh_fresnel, "exact": og.cgh_exact, "fresnel_gemm": og.cgh_fresnel_gemm}
+ADJ = {"fresnel": og.cgh_fresnel_adjoint, "exact": og.cgh_exact_adjoint, "fresnel_gemm": og.cgh_fresnel_adjoint_gemm}
+ORA = {"fresnel": O.cgh_fresnel_adjoint, "exact": O.cgh_exact_adjoint, "fresnel_gemm": O.cgh_fresnel_adjoint}
 
 
 def small_case(seed, n=700, ny=100, nx=130, p=8e-6):
@@ -32,9 +32,9 @@ def small_case(seed, n=700, ny=100, nx=130, p=8e-6):
     return pts.astype(np.float32), G
 
 
-@pytest.mark.parametrize("form", ["fresnel", "exact"])
+@pytest.mark.parametrize("form", ["fresnel", "exact", "fresnel_gemm"])
 def test_cgh_adjoint_vs_oracle(form):
-    pts, G = small_case(7 if form == "fresnel" else 8)
+    pts, G = small_case({"fresnel": 7, "exact": 8, "fresnel_gemm": 10}[form])
     ny, nx, p, lam = G.shape[0], G.shape[1], 8e-6, 532e-9
     g = ADJ[form](og.gObject(pts), torch.from_numpy(G).cuda(), ny=ny, nx=nx, py=p, px=p, lam=lam)
     torch.cuda.synchronize()
@@ -42,18 +42,35 @@ def test_cgh_adjoint_vs_oracle(form):
     assert rel_l2(g.cpu().numpy(), ref) < TOL
 
 
-def test_cgh_adjoint_accumulates():
+@pytest.mark.parametrize("form", ["fresnel", "fresnel_gemm"])
+def test_cgh_adjoint_accumulates(form):
     pts, G = small_case(9, n=300, ny=48, nx=64)
     obj, Gd = og.gObject(pts), torch.from_numpy(G).cuda()
     kw = dict(ny=48, nx=64, py=8e-6, px=8e-6, lam=532e-9)
-    once = og.cgh_fresnel_adjoint(obj, Gd, **kw)
+    once = ADJ[form](obj, Gd, **kw)
     g = once.clone()
-    og.cgh_fresnel_adjoint(obj, Gd, g, accumulate=True, **kw)
+    ADJ[form](obj, Gd, g, accumulate=True, **kw)
     torch.cuda.synchronize()
     assert rel_l2(g.cpu().numpy(), 2 * once.cpu().numpy()) < 1e-6
 
 
-@pytest.mark.parametrize("form", ["fresnel", "exact"])
+def test_cgh_adjoint_gemm_scale_and_agreement():
+    """The tensor-core adjoint scales G by a power of two to keep its f16
+    operands in range: a field far outside f16's range (1e8) and a tiny one
+    (1e-9) give the same g up to that factor, and the two Fresnel adjoints
+    agree on an uneven shape (n, nx, ny not multiples of the tiles)."""
+    pts, G = small_case(12, n=517, ny=77, nx=133)
+    obj = og.gObject(pts)
+    kw = dict(ny=77, nx=133, py=8e-6, px=8e-6, lam=532e-9)
+    ref = og.cgh_fresnel_adjoint(obj, torch.from_numpy(G).cuda(), **kw).cpu().numpy()
+    for scale in (1.0, 1e8, 1e-9):
+        Gs = torch.from_numpy((G * scale).astype(np.complex64)).cuda()
+        g = og.cgh_fresnel_adjoint_gemm(obj, Gs, **kw)
+        torch.cuda.synchronize()
+        assert rel_l2(g.cpu().numpy() / scale, ref) < TOL, scale
+
+
+@pytest.mark.parametrize("form", ["fresnel", "exact", "fresnel_gemm"])
 def test_cgh_adjoint_dot_product_workload(form):
     """<A x, G> = <x, A^H G> on the CGH workload: 10,000 points with complex
     amplitudes x_j = a_j e^{i phi_j}, 1920 x 1080 hologram, random G."""
