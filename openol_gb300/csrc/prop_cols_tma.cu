@@ -58,7 +58,7 @@ __device__ __noinline__ void cols_tile_tma(const PropParams &P, const CUtensorMa
         for (int r = 4; r < 12; ++r) v[r] = stg[(j + (r - 4) * B) * C + c];
         dft16_in_mid<-1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = v[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[17 * C * j + c + k * C] = v[outpos<16>(k)];
     }
     __syncthreads();
     // the staging buffer is free: fetch the next tile behind this one's transforms
@@ -76,7 +76,7 @@ __device__ __noinline__ void cols_tile_tma(const PropParams &P, const CUtensorMa
     for (int t = 0; t < BPT; ++t) {
         const int b = tid + t * NT, c = b % C, j = b / C;
 #pragma unroll
-        for (int r = 0; r < 16; ++r) vv[t][r] = sm[pidx(j + r * B) * C + c];
+        for (int r = 0; r < 16; ++r) vv[t][r] = sm[pidx(j) * C + c + r * (pstride<B>() * C)];
     }
     __syncthreads();
 #pragma unroll
@@ -89,7 +89,7 @@ __device__ __noinline__ void cols_tile_tma(const PropParams &P, const CUtensorMa
         for (int k = 0; k < 16; ++k) w[k] = kx < NX ? cmul(vv[t][outpos<16>(k)], tf_at(P, j + k * B, kx, N)) : vv[t][outpos<16>(k)];
         dft<16, +1>(w);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = w[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[17 * C * j + c + k * C] = w[outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, +1, NT, true, C>(sm, 0, g_tw, tid);
@@ -99,7 +99,7 @@ __device__ __noinline__ void cols_tile_tma(const PropParams &P, const CUtensorMa
         const int b = tid + t * NT, c = b % C, j = b / C, kx = c0 + c;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j + r * B) * C + c];
+        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j) * C + c + r * (pstride<B>() * C)];
         last_twiddle<N, +1>(v, j, g_tw);
         dft16_out_mid<+1>(v);
         if (kx < NX) {

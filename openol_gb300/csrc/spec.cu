@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(512, 2) k_spec_cols_fwd(SpecArgs A, const floa
             v[r] = kx < NX ? __ldcg(A.in + (size_t)(j + (r - 4) * B) * NX + kx) : make_float2(0.f, 0.f);
         dft16_in_mid<-1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = v[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[17 * C * j + c + k * C] = v[outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, -1, NT, true, C>(sm, 0, tw, tid);
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(512, 2) k_spec_cols_fwd(SpecArgs A, const floa
         const int b = tid + t * NT, c = b % C, j = b / C, kx = c0 + c;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j + r * B) * C + c];
+        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j) * C + c + r * (pstride<B>() * C)];
         last_twiddle<N, -1>(v, j, tw);
         dft<16, -1>(v);
         if (kx >= NX) continue;
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(512, 2) k_spec_cols_inv(SpecArgs A, const floa
         }
         dft<16, +1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = v[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[17 * C * j + c + k * C] = v[outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, +1, NT, true, C>(sm, 0, tw, tid);
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(512, 2) k_spec_cols_inv(SpecArgs A, const floa
         const int b = tid + t * NT, c = b % C, j = b / C, kx = c0 + c;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j + r * B) * C + c];
+        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j) * C + c + r * (pstride<B>() * C)];
         last_twiddle<N, +1>(v, j, tw);
         dft16_out_mid<+1>(v);
         if (kx >= NX) continue;

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(512) k_tilt_cols_fwd2(TiltArgs T, const float2
             v[r] = kx < NX ? T.D[(size_t)(j + (r - 4) * B) * NX + kx] : make_float2(0.f, 0.f);
         dft16_in_mid<-1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = v[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[17 * C * j + c + k * C] = v[outpos<16>(k)];
     }
     __syncthreads();
     mid_stages<N, -1, NT, true, C>(sm, 0, tw, tid);
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(512) k_tilt_cols_fwd2(TiltArgs T, const float2
         const int b = tid + t * NT, c = b % C, j = b / C, kx = c0 + c;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j + r * B) * C + c];
+        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j) * C + c + r * (pstride<B>() * C)];
         last_twiddle<N, -1>(v, j, tw);
         dft<16, -1>(v);
         if (kx >= NX) continue;
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(512) k_tilt_cols_inv2(TiltArgs T, const float2
             v[r] = kx < NX ? T.D[(size_t)(j + r * B) * NX + kx] : make_float2(0.f, 0.f);
         dft<16, +1>(v);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sm[pidx(j * 16 + k) * C + c] = v[outpos<16>(k)];
+        for (int k = 0; k < 16; ++k) sm[17 * C * j + c + k * C] = v[outpos<16>(k)];
     }
     // every column of this tile is now in shared memory: the writes below go
     // back into the same columns of D
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(512) k_tilt_cols_inv2(TiltArgs T, const float2
         const int b = tid + t * NT, c = b % C, j = b / C, kx = c0 + c;
         float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j + r * B) * C + c];
+        for (int r = 0; r < 16; ++r) v[r] = sm[pidx(j) * C + c + r * (pstride<B>() * C)];
         last_twiddle<N, +1>(v, j, tw);
         dft16_out_mid<+1>(v);
         if (kx >= NX) continue;
