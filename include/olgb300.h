@@ -286,6 +286,21 @@ int olg_batch_plan_direct_fields(olg_batch_plan plan);
 long long olg_batch_direct_pixels(long long pixels);
 int olg_batch_plan_destroy(olg_batch_plan plan);
 
+/* Single-field propagation plans (the cached-plan form of olg_asm_prop_c64,
+ * olg_fresnel_prop_c64 and olg_arss_prop_c64): the field described by an
+ * olg_field (its `in` / `out` are ignored; method OLG_BATCH_*, sizes as the
+ * single calls accept, mixed radix included) is checked, its scratch
+ * allocated and, for Fresnel and ARSS, its chirp spectra computed once, at
+ * creation (cudaMalloc and a synchronisation).  Each execution then binds
+ * device fields (16-byte aligned, in == out allowed) and runs the three
+ * passes on `stream`, with the results of the matching single call.  The
+ * executions of one plan share its scratch: order them (one stream, or
+ * synchronised between streams). */
+typedef struct olg_prop_plan_s *olg_prop_plan;
+int olg_prop_plan_create(const olg_field *field, olg_prop_plan *plan);
+int olg_prop_plan_execute(olg_prop_plan plan, const void *in, void *out, olg_stream_t stream);
+int olg_prop_plan_destroy(olg_prop_plan plan);
+
 /* -------------------------------------------------- phase optimisation */
 /* Multi-plane phase-only hologram optimisation (the reference has none; it
  * builds on its ASM, golprop.h:507-534).  phi: ny x nx float (radians);

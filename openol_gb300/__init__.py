@@ -11,7 +11,7 @@ from .cgh import (Cgh, Object2cuda, autotune_cgh_gemm, WRPMethod, WRPMethod_D, W
 from .img import MODE, binarize, complex2img  # noqa: F401
 from .objects import (OBJSET_MODE, ZMIDDLE, ZMIN, bmpread, bmpwrite, objinfo, objread, objset, objsort,  # noqa: F401
                       objwrite_3d)
-from .batch import BatchPlan, config5_fields, direct_pixels as batch_direct_pixels  # noqa: F401
+from .batch import BatchPlan, PropPlan, config5_fields, direct_pixels as batch_direct_pixels  # noqa: F401
 from .optim import PhaseOptimizer, make_targets, phase_loss_grad  # noqa: F401
 from .prop import (ASM, AUTO, FRESNEL, PROPMODE, ARSSFresnelProp, AsmProp, AsmPropCheck, FresnelProp,
                    FresnelPropBandLimit, FresnelPropCheck, PropHost,  # noqa: F401

@@ -66,6 +66,9 @@ SIGNATURES = {
     "olg_batch_execute": (_i, [_p, _p]),
     "olg_batch_execute_serial": (_i, [_p, _p]),
     "olg_batch_execute_host": (_i, [_p, _p, _p, _p]),
+    "olg_prop_plan_create": (_i, [_p, _p]),
+    "olg_prop_plan_execute": (_i, [_p, _p, _p, _p]),
+    "olg_prop_plan_destroy": (_i, [_p]),
     "olg_batch_check": (_i, [_p]),
     "olg_batch_plan_items": (_i, [_p]),
     "olg_batch_plan_destroy": (_i, [_p]),

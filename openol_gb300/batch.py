@@ -83,6 +83,43 @@ class BatchPlan:
             pass
 
 
+class PropPlan:
+    """One propagation set up once (olg_prop_plan_*): method ('asm' | 'fresnel' |
+    'arss' | 'fresnel_bandlimit'), field shape (ny, nx), dy, dx, lam, z and, for
+    ARSS, s (oy, ox optional); flags as the single calls take.  Creation checks
+    the parameters, allocates the scratch and computes the Fresnel / ARSS chirp
+    spectra; ``execute`` binds device fields and runs the three passes.
+    Executions share the plan's scratch: keep them on one stream."""
+
+    def __init__(self, method, ny, nx, *, dy, dx, lam, z, s=0.5, oy=0.0, ox=0.0, flags=0):
+        self.shape = (int(ny), int(nx))
+        desc = OlgField(None, None, int(ny), int(nx), METHODS[method], int(flags), float(dy), float(dx), float(lam),
+                        float(z), float(s), float(oy), float(ox))
+        self._plan = C.c_void_p()
+        call("olg_prop_plan_create", C.byref(desc), C.byref(self._plan))
+
+    def execute(self, u_in, u_out=None, stream=None):
+        """Propagate ``u_in`` into ``u_out`` (in place when omitted): contiguous
+        CUDA complex64 tensors of the plan's shape."""
+        u_out = u_in if u_out is None else u_out
+        for t in (u_in, u_out):
+            if not (t.is_cuda and t.dtype == torch.complex64 and t.is_contiguous()) or tuple(t.shape) != self.shape:
+                raise TypeError("fields must be contiguous CUDA complex64 tensors of the plan's shape")
+        call("olg_prop_plan_execute", self._plan, u_in.data_ptr(), u_out.data_ptr(), _stream(stream))
+        return u_out
+
+    def close(self):
+        if self._plan:
+            lib().olg_prop_plan_destroy(self._plan)
+            self._plan = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def direct_pixels(pixels=None):
     """The size (ny * nx) from which plans created afterwards run a field through
     the single-field passes instead of the persistent kernel; with ``pixels``,

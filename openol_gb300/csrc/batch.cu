@@ -168,6 +168,21 @@ bool batch_size_ok(int n) { return n >= 256 && n <= FFT_MAX / 2 && is_pow2(n); }
 // more than the work.
 std::atomic<long long> g_batch_direct_pixels{2048LL * 2048LL};
 
+// the physical checks of the single-call entry points, per method
+int check_field(const olg_field &F)
+{
+    if (F.method < OLG_BATCH_ASM || F.method > OLG_BATCH_FRESNEL_BANDLIMIT)
+        return fail(OLG_ERR_INVALID_ARG, "unknown propagation method");
+    if (int rc = check_phys(F.dy, F.dx, F.lambda, F.z, F.method != OLG_BATCH_ASM)) return rc;
+    if (F.method == OLG_BATCH_ARSS) {
+        if (!std::isfinite(F.s) || !std::isfinite(F.oy) || !std::isfinite(F.ox))
+            return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+        if (F.s == 0.0 || F.s == 1.0)
+            return fail(OLG_ERR_INVALID_ARG, "ARSS is undefined for s = 0 or s = 1 (window limits divide by s|s-1|)");
+    }
+    return OLG_OK;
+}
+
 int field_setup(const olg_field &F, const Layout &L, PropSetup *S)
 {
     switch (F.method) {
@@ -191,6 +206,7 @@ extern "C" int olg_batch_plan_create(const olg_field *fields, int n_fields, olg_
     for (int i = 0; i < n_fields; ++i) {
         const olg_field &F = fields[i];
         if (int rc = validate(F.in, F.out, F.ny, F.nx)) return rc;
+        if (int rc = check_field(F)) return rc;
         if (!batch_size_ok(F.ny) || !batch_size_ok(F.nx))
             return fail(OLG_ERR_UNSUPPORTED_SIZE, "batched fields must be powers of two in [256, 4096]");
     }
@@ -515,3 +531,78 @@ extern "C" int olg_batch_plan_destroy(olg_batch_plan plan)
     return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaFree (batch plan)");
 }
 
+
+// ------------------------------------------------- single-field plans
+// One propagation's set-up done once: the parameters checked, the scratch
+// (half-padded spectrum and chirp tables) allocated, and the Fresnel / ARSS
+// chirp spectra computed; each execution binds the fields and runs the three
+// passes.  Executions of one plan share its scratch, so they must be ordered
+// (one stream, or synchronised between streams).
+struct olg_prop_plan_s {
+    olg_field F{};
+    char *mem = nullptr;
+    PropSetup S{};
+};
+
+extern "C" int olg_prop_plan_create(const olg_field *field, olg_prop_plan *out)
+{
+    if (!out || !field) return fail(OLG_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    const olg_field &F = *field;
+    if (!axis_ok(F.ny) || !axis_ok(F.nx))
+        return fail(OLG_ERR_UNSUPPORTED_SIZE,
+                    "ny, nx must be powers of two in [16, 4096] or have 2n = 2^a 3^b 5^c <= 7680 (n >= 8)");
+    if (int rc = check_field(F)) return rc;
+    if (int rc = ensure_twiddles()) return rc;
+    auto *plan = new olg_prop_plan_s();
+    plan->F = F;
+    const size_t bytes = layout_bytes(F.ny, F.nx, nullptr, nullptr);
+    cudaError_t e = cudaMalloc(&plan->mem, bytes);
+    if (e != cudaSuccess) {
+        delete plan;
+        return cuda_fail(e, "cudaMalloc (propagation plan)");
+    }
+    Layout L;
+    layout_bytes(F.ny, F.nx, &L, plan->mem);
+    olg_field G = F; // the fields are bound at execution; the scratch stands in
+    G.in = plan->mem;
+    G.out = plan->mem;
+    int rc = field_setup(G, L, &plan->S);
+    if (!rc && plan->S.chirps) {
+        cudaStream_t st = nullptr;
+        e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamCreate (propagation plan)");
+        if (!rc) rc = chirp_axis(plan->S.ax, st);
+        if (!rc) rc = chirp_axis(plan->S.ay, st);
+        if (st) {
+            e = cudaStreamSynchronize(st);
+            if (!rc && e != cudaSuccess) rc = cuda_fail(e, "computing the plan's chirp spectra");
+            cudaStreamDestroy(st);
+        }
+    }
+    if (rc) {
+        cudaFree(plan->mem);
+        delete plan;
+        return rc;
+    }
+    *out = plan;
+    return OLG_OK;
+}
+
+extern "C" int olg_prop_plan_execute(olg_prop_plan plan, const void *in, void *out, olg_stream_t stream)
+{
+    if (!plan) return fail(OLG_ERR_INVALID_ARG, "null plan");
+    if (int rc = validate(in, out, plan->F.ny, plan->F.nx)) return rc;
+    PropParams P = plan->S.P;
+    P.in = (const float2 *)in;
+    P.out = (float2 *)out;
+    return run_passes(P, (cudaStream_t)stream);
+}
+
+extern "C" int olg_prop_plan_destroy(olg_prop_plan plan)
+{
+    if (!plan) return OLG_OK;
+    const cudaError_t e = cudaFree(plan->mem);
+    delete plan;
+    return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaFree (propagation plan)");
+}

@@ -185,6 +185,38 @@ def test_argument_validation_without_gpu():
     assert L.olg_tilted_workspace_bytes(64, 64) >= 2 * 128 * 128 * 8
 
 
+def test_plan_validation_without_gpu():
+    """Propagation and batch plans check the field description (size, method,
+    physical parameters, ARSS s) before any device work."""
+    L = _lib.lib()
+    buf = (C.c_char * 64)()
+    base = (C.addressof(buf) + 15) // 16 * 16
+    F = _lib.OlgField
+
+    def desc(**kw):
+        d = dict(in_=base, out=base, ny=64, nx=64, method=0, flags=0, dy=8e-6, dx=8e-6, lam=532e-9, z=0.05, s=0.5,
+                 oy=0.0, ox=0.0)
+        d.update(kw)
+        return F(**d)
+
+    plan = C.c_void_p()
+    assert L.olg_prop_plan_create(None, C.byref(plan)) == -1
+    assert L.olg_prop_plan_create(C.byref(desc(ny=14)), C.byref(plan)) == -2       # 28 = 4 * 7
+    assert L.olg_prop_plan_create(C.byref(desc(method=9)), C.byref(plan)) == -1
+    assert L.olg_prop_plan_create(C.byref(desc(lam=float("nan"))), C.byref(plan)) == -1
+    assert L.olg_prop_plan_create(C.byref(desc(method=1, z=0.0)), C.byref(plan)) == -1   # Fresnel at z = 0
+    assert L.olg_prop_plan_create(C.byref(desc(method=2, s=1.0)), C.byref(plan)) == -1   # ARSS, s = 1
+    assert L.olg_prop_plan_create(C.byref(desc(method=2, ox=float("inf"))), C.byref(plan)) == -1
+    assert plan.value is None
+    assert L.olg_prop_plan_execute(None, base, base, None) == -1
+    assert L.olg_prop_plan_destroy(None) == 0
+    # the batch plan runs the same checks on every field
+    arr = (F * 2)(desc(ny=256, nx=256), desc(ny=256, nx=256, method=2, s=0.0))
+    bplan = C.c_void_p()
+    assert L.olg_batch_plan_create(arr, 2, C.byref(bplan)) == -1
+    assert b"s = 0" in L.olg_last_error() or b"s|s-1|" in L.olg_last_error()
+
+
 def test_workspace_size():
     L = _lib.lib()
     ws = L.olg_prop_workspace_bytes(1024, 1024)
