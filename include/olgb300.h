@@ -361,7 +361,10 @@ size_t olg_cgh_adjoint_workspace_bytes(int n_points, int ny, int nx, int exact);
  * then g_j = sum_h conj(Y[h, j]) T[h, j] summed over row bands in a fixed
  * order (deterministic).  Same arguments and flags as
  * olg_cgh_fresnel_adjoint_c64; nx, ny <= 4096.  Scratch:
- * olg_cgh_adjoint_gemm_workspace_bytes (work == NULL: stream-ordered pool). */
+ * olg_cgh_adjoint_gemm_workspace_bytes (work == NULL: stream-ordered pool),
+ * about (2 ny + n_points) x 2 nx x 4 + ny x n_points x 8 bytes (275 MB for
+ * 1080 x 1920 and 10^4 points): it holds T, so it grows with ny x n_points,
+ * where the direct adjoint's grows with n_points alone. */
 size_t olg_cgh_adjoint_gemm_workspace_bytes(int n_points, int ny, int nx);
 int olg_cgh_fresnel_adjoint_gemm_c64(const float *points, int n_points, const void *G, void *g, int ny, int nx,
                                      double py, double px, double lambda, int flags, void *work, size_t work_bytes,
