@@ -13,7 +13,7 @@
 // F is private to these kernels and is stored by column tiles: tile
 // t = kx / C holds rows ky = 0..NY-1 of its C columns contiguously
 // (F[t NY C + ky C + kx % C]), so that every CTA reads and writes one
-// contiguous block.  Two 512-thread CTAs per SM (64 registers).
+// contiguous block.
 #include "common.cuh"
 #include "fft.cuh"
 #include "fft2.cuh"
@@ -21,15 +21,21 @@
 
 namespace olg {
 
+// Launch shape: from N = 2048, one 1024-thread CTA per SM over 16384
+// elements (one butterfly per thread; 139 KB of shared memory), which took
+// the 2048^2 phase-gradient step from 2.48 to 2.38 ms against two 512-thread
+// CTAs of 8192 elements; below, the latter.
 template <int N>
 struct SpecCol {
-    static constexpr int NT = 512, C = 8192 / N, B = N / 16, BPT = C * B / NT;
+    static constexpr bool BIG = N >= 2048;
+    static constexpr int NT = BIG ? 1024 : 512, MINB = BIG ? 1 : 2;
+    static constexpr int C = (BIG ? 16384 : 8192) / N, B = N / 16, BPT = C * B / NT;
     static constexpr int SMEM = padded_len(N) * C * (int)sizeof(float2);
     static_assert((C * B) % NT == 0, "threads must divide the butterflies");
 };
 
 template <int N>
-__global__ void __launch_bounds__(512, 2) k_spec_cols_fwd(SpecArgs A, const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(SpecCol<N>::NT, SpecCol<N>::MINB) k_spec_cols_fwd(SpecArgs A, const float2 *__restrict__ tw)
 {
     using S = SpecCol<N>;
     constexpr int B = S::B, C = S::C, NT = S::NT;
@@ -74,7 +80,7 @@ __global__ void __launch_bounds__(512, 2) k_spec_cols_fwd(SpecArgs A, const floa
 }
 
 template <int N>
-__global__ void __launch_bounds__(512, 2) k_spec_cols_inv(SpecArgs A, const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(SpecCol<N>::NT, SpecCol<N>::MINB) k_spec_cols_inv(SpecArgs A, const float2 *__restrict__ tw)
 {
     using S = SpecCol<N>;
     constexpr int B = S::B, C = S::C, NT = S::NT;
