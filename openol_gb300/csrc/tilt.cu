@@ -16,16 +16,18 @@
 
 namespace olg {
 
-// one shape for every length: 512 threads, C = 8192 / N columns per CTA
+// from N = 2048: 1024 threads over C = 16384 / N columns per CTA (one
+// butterfly per thread; one CTA per SM); below: 512 threads, C = 8192 / N
 template <int N>
 struct TiltCol {
-    static constexpr int NT = 512, C = 8192 / N, B = N / 16, BPT = C * B / NT;
+    static constexpr bool BIG = N >= 2048;
+    static constexpr int NT = BIG ? 1024 : 512, C = (BIG ? 16384 : 8192) / N, B = N / 16, BPT = C * B / NT;
     static constexpr int SMEM = padded_len(N) * C * (int)sizeof(float2);
     static_assert((C * B) % NT == 0, "threads must divide the butterflies");
 };
 
 template <int N>
-__global__ void __launch_bounds__(512) k_tilt_cols_fwd2(TiltArgs T, const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(TiltCol<N>::NT) k_tilt_cols_fwd2(TiltArgs T, const float2 *__restrict__ tw)
 {
     using S = TiltCol<N>;
     constexpr int B = S::B, C = S::C, NT = S::NT;
@@ -66,7 +68,7 @@ __global__ void __launch_bounds__(512) k_tilt_cols_fwd2(TiltArgs T, const float2
 }
 
 template <int N>
-__global__ void __launch_bounds__(512) k_tilt_cols_inv2(TiltArgs T, const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(TiltCol<N>::NT) k_tilt_cols_inv2(TiltArgs T, const float2 *__restrict__ tw)
 {
     using S = TiltCol<N>;
     constexpr int B = S::B, C = S::C, NT = S::NT;
