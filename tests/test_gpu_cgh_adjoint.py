@@ -54,20 +54,26 @@ def test_cgh_adjoint_accumulates(form):
     assert rel_l2(g.cpu().numpy(), 2 * once.cpu().numpy()) < 1e-6
 
 
-def test_cgh_adjoint_gemm_scale_and_agreement():
+@pytest.mark.parametrize("pairs", [False, True], ids=["single", "pairs"])
+def test_cgh_adjoint_gemm_scale_and_agreement(pairs):
     """The tensor-core adjoint scales G by a power of two to keep its f16
     operands in range: a field far outside f16's range (1e8) and a tiny one
     (1e-9) give the same g up to that factor, and the two Fresnel adjoints
-    agree on an uneven shape (n, nx, ny not multiples of the tiles)."""
+    agree on an uneven shape (n, nx, ny not multiples of the tiles), in both
+    GEMM tile forms."""
     pts, G = small_case(12, n=517, ny=77, nx=133)
     obj = og.gObject(pts)
     kw = dict(ny=77, nx=133, py=8e-6, px=8e-6, lam=532e-9)
     ref = og.cgh_fresnel_adjoint(obj, torch.from_numpy(G).cuda(), **kw).cpu().numpy()
-    for scale in (1.0, 1e8, 1e-9):
-        Gs = torch.from_numpy((G * scale).astype(np.complex64)).cuda()
-        g = og.cgh_fresnel_adjoint_gemm(obj, Gs, **kw)
-        torch.cuda.synchronize()
-        assert rel_l2(g.cpu().numpy() / scale, ref) < TOL, scale
+    prev = og.cgh_gemm_pairs(pairs)
+    try:
+        for scale in (1.0, 1e8, 1e-9):
+            Gs = torch.from_numpy((G * scale).astype(np.complex64)).cuda()
+            g = og.cgh_fresnel_adjoint_gemm(obj, Gs, **kw)
+            torch.cuda.synchronize()
+            assert rel_l2(g.cpu().numpy() / scale, ref) < TOL, scale
+    finally:
+        og.cgh_gemm_pairs(prev)
 
 
 @pytest.mark.parametrize("form", ["fresnel", "exact", "fresnel_gemm"])
