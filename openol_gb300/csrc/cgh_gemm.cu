@@ -21,12 +21,14 @@
 //                  MUFU sin/cos
 // k_cgh_gemm<BN>   warp-specialised tcgen05 GEMM, one CTA per tile plus CTAs on
 //                  the spare SMs that take the tiles' K tails: warp 0 issues TMA loads into a
-//                  4-stage ring (128 x 64 A and BN x 64 B f16 tiles, 128-byte
-//                  swizzle), warp 1 owns TMEM (two f32 accumulators of BN
-//                  columns) and issues the 128 x BN x 16 MMAs chunk by chunk,
-//                  warps 2-9 add each finished chunk into f32 registers and add
-//                  every finished piece of a tile into the complex64 output.
-//                  BN in {128, ..., 256} is the N tile that pads nx least
+//                  2-stage ring, each stage the four f16 tiles of one 64-wide K
+//                  range (A hi, A lo: 128 x 64; B hi, B lo: BN x 64; 128-byte
+//                  swizzle); warp 1 owns TMEM (two f32 accumulators of BN
+//                  columns) and issues the three split products' 128 x BN x 16
+//                  MMAs from each stage, chunk by chunk; warps 2-9 add each
+//                  finished chunk into f32 registers and add every finished
+//                  piece of a tile into the complex64 output.  BN in
+//                  {128, ..., 256} is the N tile that pads nx least
 //                  (1920 = 8 x 240).
 #include <cuda.h>
 #include <cuda_fp16.h>
@@ -44,16 +46,21 @@
 
 namespace olg {
 
-constexpr int GB_M = 128, GB_K = 64, GB_STAGES = 4;
+constexpr int GB_M = 128, GB_K = 64;
 constexpr int GB_A_BYTES = GB_M * GB_K * 2;
 // N tile widths (multiples of 16 up to 256, the kind::f16 limit at M = 128):
 // the host takes the one whose tiles cover nx with the least padding
 // (1920 = 8 x 240 exactly, where 256 would pad to 2048).
+// Single-SM tiles stage, per 64-wide K range, all four operand tiles (A hi,
+// A lo, B hi, B lo) and issue the three split products from them: 12 MMAs
+// per 92 KB stage at BN = 240 instead of 4 MMAs per 46 KB, two stages deep.
+constexpr int GB_FSTAGES = 2;
 template <int BN>
 struct GemmTile {
     static_assert(BN % 16 == 0 && BN >= 128 && BN <= 256, "N tile");
-    static constexpr int B_BYTES = BN * GB_K * 2;           // a multiple of 1024: SW128 stages stay aligned
-    static constexpr int SMEM = GB_STAGES * (GB_A_BYTES + B_BYTES) + 1024 + 256;
+    static constexpr int B_BYTES = BN * GB_K * 2;           // a multiple of 1024: SW128 tiles stay aligned
+    static constexpr int STAGE = 2 * GB_A_BYTES + 2 * B_BYTES; // A hi, A lo, B hi, B lo
+    static constexpr int SMEM = GB_FSTAGES * STAGE + 1024 + 256;
 };
 constexpr long long GB_WAIT = 4000000000LL; // ~2 s of SM clock per wait
 
@@ -324,8 +331,10 @@ struct GemmParams {
     int m2, n, kblocks; // rows of D (2 ny), columns (nx), K blocks of 64 per segment
     int tiles_n;        // N tiles across D
     int tiles;          // 128 x BN tiles of D
-    int split;          // K blocks (of 3 kblocks) a tile's own CTA does
-    int extra;          // CTAs beyond `tiles` that do the rest [split, 3 kblocks)
+    int total;          // K steps per tile: kblocks (single-SM: all three products per step)
+                        // or 3 kblocks (CTA pairs: one product per step)
+    int split;          // K steps a tile's own unit does
+    int extra;          // units beyond `tiles` that do the rest [split, total)
     int vec4;           // U is 16-byte aligned and n even: two complex values per atomic
     int chunk;          // K blocks per TMEM accumulation before the f32 register add
     float2 *U;          // added to with atomics (zeroed first unless accumulating)
@@ -448,21 +457,23 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
     using T = GemmTile<BN>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem;
-    uint8_t *sB = smem + GB_STAGES * GB_A_BYTES;
-    uint64_t *full = (uint64_t *)(sB + GB_STAGES * T::B_BYTES);
-    uint64_t *empty = full + GB_STAGES;
-    uint64_t *tfull = empty + GB_STAGES; // [2]
-    uint64_t *tfree = tfull + 2;         // [2]
+    // stage s: [A hi | A lo | B hi | B lo]
+    auto stage = [&](int s) { return smem + s * T::STAGE; };
+    uint64_t *full = (uint64_t *)(smem + GB_FSTAGES * T::STAGE);
+    uint64_t *empty = full + GB_FSTAGES;
+    uint64_t *tfull = empty + GB_FSTAGES; // [2]
+    uint64_t *tfree = tfull + 2;          // [2]
     uint32_t *tmem_slot = (uint32_t *)(tfree + 2);
     volatile int *fault = (volatile int *)(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int total = 3 * P.kblocks; // K blocks per tile
+    const int total = P.total; // K steps per tile (kblocks)
     const int np = gemm_pieces(P, blockIdx.x);
+    // K steps per TMEM accumulation: P.chunk counts one-product K blocks
+    const int chunk = max(1, (P.chunk + 2) / 3);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < GB_STAGES; ++s) {
+        for (int s = 0; s < GB_FSTAGES; ++s) {
             mbar_init(smem_u32(full + s), 1);
             mbar_init(smem_u32(empty + s), 1);
         }
@@ -490,24 +501,26 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                 gemm_piece(P, blockIdx.x, p, total, t, k0, k1);
                 const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * BN;
                 for (int kb = k0; kb < k1 && !*fault; ++kb, ++i) {
-                    const int s = i % GB_STAGES;
-                    const uint32_t ph = (uint32_t)(i / GB_STAGES) & 1u;
+                    const int s = i % GB_FSTAGES;
+                    const uint32_t ph = (uint32_t)(i / GB_FSTAGES) & 1u;
                     if (!mbar_wait(smem_u32(empty + s), ph ^ 1u, GB_WAIT)) {
                         *fault = 1;
                         break;
                     }
-                    const int seg = kb / P.kblocks, kk = (kb % P.kblocks) * GB_K;
-                    const CUtensorMap *ma = seg < 2 ? &tAh : &tAl;
-                    const CUtensorMap *mb = seg == 1 ? &tBl : &tBh;
-                    mbar_expect_tx(smem_u32(full + s), GB_A_BYTES + T::B_BYTES);
-                    tma_load_2d(smem_u32(sA + s * GB_A_BYTES), ma, smem_u32(full + s), kk, m0);
-                    tma_load_2d(smem_u32(sB + s * T::B_BYTES), mb, smem_u32(full + s), kk, n0);
+                    const int kk = kb * GB_K;
+                    uint8_t *st = stage(s);
+                    const uint32_t fb = smem_u32(full + s);
+                    mbar_expect_tx(fb, T::STAGE);
+                    tma_load_2d(smem_u32(st), &tAh, fb, kk, m0);
+                    tma_load_2d(smem_u32(st + GB_A_BYTES), &tAl, fb, kk, m0);
+                    tma_load_2d(smem_u32(st + 2 * GB_A_BYTES), &tBh, fb, kk, n0);
+                    tma_load_2d(smem_u32(st + 2 * GB_A_BYTES + T::B_BYTES), &tBl, fb, kk, n0);
                     issued = i + 1;
                 }
             }
             // never leave with copies in flight
-            for (int j = issued > GB_STAGES ? issued - GB_STAGES : 0; j < issued; ++j)
-                mbar_wait(smem_u32(full + j % GB_STAGES), (uint32_t)(j / GB_STAGES) & 1u, GB_WAIT);
+            for (int j = issued > GB_FSTAGES ? issued - GB_FSTAGES : 0; j < issued; ++j)
+                mbar_wait(smem_u32(full + j % GB_FSTAGES), (uint32_t)(j / GB_FSTAGES) & 1u, GB_WAIT);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -524,19 +537,27 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                     }
                     tc_fence_after();
                     const uint32_t d = tmem + (uint32_t)(b * 256);
-                    const int kend = min(k1, kb + P.chunk);
+                    const int kend = min(k1, kb + chunk);
                     for (int kc = kb; kc < kend; ++kc, ++i) {
-                        const int s = i % GB_STAGES;
-                        if (!mbar_wait(smem_u32(full + s), (uint32_t)(i / GB_STAGES) & 1u, GB_WAIT)) {
+                        const int s = i % GB_FSTAGES;
+                        if (!mbar_wait(smem_u32(full + s), (uint32_t)(i / GB_FSTAGES) & 1u, GB_WAIT)) {
                             *fault = 1;
                             break;
                         }
                         tc_fence_after();
-                        const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * T::B_BYTES);
+                        const uint32_t ah = smem_u32(stage(s)), al = ah + GB_A_BYTES;
+                        const uint32_t bh = ah + 2 * GB_A_BYTES, bl = bh + T::B_BYTES;
+                        // hi.hi, hi.lo, lo.hi of this K range into one accumulator
 #pragma unroll
                         for (int k = 0; k < GB_K / 16; ++k)
-                            umma_f16(d, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), idesc,
+                            umma_f16(d, sdesc_sw128(ah + 32 * k), sdesc_sw128(bh + 32 * k), idesc,
                                      (kc > kb || k > 0) ? 1u : 0u);
+#pragma unroll
+                        for (int k = 0; k < GB_K / 16; ++k)
+                            umma_f16(d, sdesc_sw128(ah + 32 * k), sdesc_sw128(bl + 32 * k), idesc, 1u);
+#pragma unroll
+                        for (int k = 0; k < GB_K / 16; ++k)
+                            umma_f16(d, sdesc_sw128(al + 32 * k), sdesc_sw128(bh + 32 * k), idesc, 1u);
                         umma_commit(smem_u32(empty + s));
                     }
                     umma_commit(smem_u32(tfull + b));
@@ -572,7 +593,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
                 __syncwarp();
                 if (lane == 0)
                     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(tfree + b)) : "memory");
-                kb = min(k1, kb + P.chunk);
+                kb = min(k1, kb + chunk);
             }
             const int m0 = (t / P.tiles_n) * GB_M, n0 = (t % P.tiles_n) * BN;
             const int row = m0 + 32 * q + lane; // row of D
@@ -637,7 +658,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_THREADS, 1)
     const bool lead = rank == 0;
     const int pair = blockIdx.x >> 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int total = 3 * P.kblocks;
+    const int total = P.total; // 3 kblocks: one split product per K step
     const int np = gemm_pieces(P, pair);
 
     if (threadIdx.x == 0) {
@@ -949,7 +970,8 @@ int gemm_run(const __half *a_hi, const __half *a_lo, const __half *b_hi, const _
     // g_tail_weight tile K blocks (its operands are not shared in L2 with
     // other units at the time), so split = total per w / (per w + 1) evens
     // the two kinds of unit; w <= 0 turns the split off.
-    const int total = 3 * P.kblocks;
+    const int total = pair ? 3 * P.kblocks : P.kblocks;
+    P.total = total;
     P.split = total;
     P.extra = 0;
     if (tiles < units_max && tw > 0.0) {
