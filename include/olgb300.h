@@ -393,10 +393,11 @@ int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, const float 
  * 1.2; 0 turns the split off).  Sets w when 0 <= w <= 16 and returns the
  * previous value. */
 double olg_cgh_gemm_tail_weight(double w);
-/* Accumulation length of the GEMM (no counterpart in the reference): K
- * blocks of 64 (x 3 split products) summed in the tensor core's f32
- * accumulator before each partial sum is added into f32 registers (default
- * 8).  Longer chunks hand accumulators to the epilogue less often; shorter
+/* Accumulation length of the GEMM (no counterpart in the reference), in K
+ * blocks of 64 of one split product: ceil(kblocks / 3) K steps, each the
+ * three split products over a 64-wide K range, are summed in the tensor
+ * core's f32 accumulator before each partial sum is added into f32 registers
+ * (default 8: 3 steps, 576 products).  Longer chunks hand accumulators to the epilogue less often; shorter
  * ones keep the tensor-core sums shorter.  Sets it for 1 <= kblocks <= 64
  * and returns the previous value; other values only return it. */
 int olg_cgh_gemm_chunk(int kblocks);

@@ -331,8 +331,7 @@ struct GemmParams {
     int m2, n, kblocks; // rows of D (2 ny), columns (nx), K blocks of 64 per segment
     int tiles_n;        // N tiles across D
     int tiles;          // 128 x BN tiles of D
-    int total;          // K steps per tile: kblocks (single-SM: all three products per step)
-                        // or 3 kblocks (CTA pairs: one product per step)
+    int total;          // K steps per tile (kblocks: all three split products per step)
     int split;          // K steps a tile's own unit does
     int extra;          // units beyond `tiles` that do the rest [split, total)
     int vec4;           // U is 16-byte aligned and n even: two complex values per atomic
@@ -369,11 +368,12 @@ __device__ __forceinline__ void gemm_piece(const GemmParams &P, int u, int p, in
     }
 }
 
-// Accumulation within a piece: the MMA warp writes chunks of P.chunk
-// K-blocks alternately into two TMEM accumulators (BN columns each); the 8 epilogue
-// warps add every finished chunk into f32 registers (rounded adds) while the
-// next chunk runs, so the tensor pipe's own accumulation never spans more
-// than P.chunk x 64 x 3 products (default 8: 1536 products).
+// Accumulation within a piece: the MMA warp writes chunks of
+// ceil(P.chunk / 3) K steps (each step: the three split products over a
+// 64-wide K range) alternately into two TMEM accumulators (BN columns each);
+// the 8 epilogue warps add every finished chunk into f32 registers (rounded
+// adds) while the next chunk runs, so the tensor pipe's own accumulation
+// never spans more than 3 x 64 x 3 = 576 products at the default P.chunk = 8.
 constexpr int GB_EPI_WARPS = 8;
 constexpr int GB_THREADS = 64 + 32 * GB_EPI_WARPS;
 constexpr uint32_t GB_TMEM_COLS = 512; // two accumulators, at columns 0 and 256
@@ -625,13 +625,15 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
 // 16 epilogue warps of the pair.  Every wait is bounded, and both CTAs meet
 // at a cluster barrier before TMEM is released and either exits, so no CTA
 // leaves while its peer may still touch its shared memory.
-constexpr int G2_STAGES = 6;
+// As the single-SM form, each stage holds all four operand tiles of one K
+// range (this CTA's halves): 62 KB at BN = 240, three stages.
+constexpr int G2_STAGES = 3;
 template <int BN>
 struct Gemm2Tile {
     static_assert(BN % 16 == 0 && BN >= 128 && BN <= 256, "N tile");
-    static constexpr int BH = BN / 2;                  // B rows per CTA (a multiple of 8)
-    static constexpr int B_BYTES = BH * GB_K * 2;      // a multiple of 1024
-    static constexpr int STAGE = GB_A_BYTES + B_BYTES; // bytes one CTA loads per K block
+    static constexpr int BH = BN / 2;                          // B rows per CTA (a multiple of 8)
+    static constexpr int B_BYTES = BH * GB_K * 2;              // a multiple of 1024
+    static constexpr int STAGE = 2 * GB_A_BYTES + 2 * B_BYTES; // A hi, A lo, B hi, B lo of one CTA
     // + B_BYTES of slack at the end: every B descriptor's reach, even a whole
     // BN-row tile from the last stage, stays inside the allocation
     static constexpr int SMEM = G2_STAGES * STAGE + 1024 + 256 + B_BYTES;
@@ -645,9 +647,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_THREADS, 1)
     using T = Gemm2Tile<BN>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem;
-    uint8_t *sB = smem + G2_STAGES * GB_A_BYTES;
-    uint64_t *full = (uint64_t *)(sB + G2_STAGES * T::B_BYTES);
+    auto stage = [&](int s) { return smem + s * T::STAGE; }; // [A hi | A lo | B hi | B lo]
+    uint64_t *full = (uint64_t *)(smem + G2_STAGES * T::STAGE);
     uint64_t *empty = full + G2_STAGES;
     uint64_t *tfull = empty + G2_STAGES; // [2]
     uint64_t *tfree = tfull + 2;         // [2]
@@ -658,8 +659,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_THREADS, 1)
     const bool lead = rank == 0;
     const int pair = blockIdx.x >> 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int total = P.total; // 3 kblocks: one split product per K step
+    const int total = P.total; // kblocks: all three split products per K step
     const int np = gemm_pieces(P, pair);
+    const int chunk = max(1, (P.chunk + 2) / 3);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < G2_STAGES; ++s) {
@@ -698,12 +700,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_THREADS, 1)
                         *fault = 1;
                         break;
                     }
-                    const int seg = kb / P.kblocks, kk = (kb % P.kblocks) * GB_K;
-                    const CUtensorMap *ma = seg < 2 ? &tAh : &tAl;
-                    const CUtensorMap *mb = seg == 1 ? &tBl : &tBh;
+                    const int kk = kb * GB_K;
+                    uint8_t *st = stage(s);
+                    const uint32_t fb = full_lead + 8u * s;
                     if (lead) mbar_expect_tx(smem_u32(full + s), 2 * T::STAGE);
-                    tma_load_2d_pair(smem_u32(sA + s * GB_A_BYTES), ma, full_lead + 8u * s, kk, m0);
-                    tma_load_2d_pair(smem_u32(sB + s * T::B_BYTES), mb, full_lead + 8u * s, kk, n0);
+                    tma_load_2d_pair(smem_u32(st), &tAh, fb, kk, m0);
+                    tma_load_2d_pair(smem_u32(st + GB_A_BYTES), &tAl, fb, kk, m0);
+                    tma_load_2d_pair(smem_u32(st + 2 * GB_A_BYTES), &tBh, fb, kk, n0);
+                    tma_load_2d_pair(smem_u32(st + 2 * GB_A_BYTES + T::B_BYTES), &tBl, fb, kk, n0);
                     issued = i + 1;
                 }
             }
@@ -728,7 +732,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_THREADS, 1)
                     }
                     tc_fence_after();
                     const uint32_t d = tmem + (uint32_t)(b * 256);
-                    const int kend = min(k1, kb + P.chunk);
+                    const int kend = min(k1, kb + chunk);
                     for (int kc = kb; kc < kend; ++kc, ++i) {
                         const int s = i % G2_STAGES;
                         if (!mbar_wait(smem_u32(full + s), (uint32_t)(i / G2_STAGES) & 1u, GB_WAIT)) {
@@ -736,11 +740,18 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_THREADS, 1)
                             break;
                         }
                         tc_fence_after();
-                        const uint32_t a0 = smem_u32(sA + s * GB_A_BYTES), b0 = smem_u32(sB + s * T::B_BYTES);
+                        const uint32_t ah = smem_u32(stage(s)), al = ah + GB_A_BYTES;
+                        const uint32_t bh = ah + 2 * GB_A_BYTES, bl = bh + T::B_BYTES;
 #pragma unroll
                         for (int k = 0; k < GB_K / 16; ++k)
-                            umma_f16_pair(d, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), idesc,
+                            umma_f16_pair(d, sdesc_sw128(ah + 32 * k), sdesc_sw128(bh + 32 * k), idesc,
                                           (kc > kb || k > 0) ? 1u : 0u);
+#pragma unroll
+                        for (int k = 0; k < GB_K / 16; ++k)
+                            umma_f16_pair(d, sdesc_sw128(ah + 32 * k), sdesc_sw128(bl + 32 * k), idesc, 1u);
+#pragma unroll
+                        for (int k = 0; k < GB_K / 16; ++k)
+                            umma_f16_pair(d, sdesc_sw128(al + 32 * k), sdesc_sw128(bh + 32 * k), idesc, 1u);
                         umma_commit_pair(smem_u32(empty + s), 3);
                     }
                     umma_commit_pair(smem_u32(tfull + b), 3);
@@ -776,7 +787,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_THREADS, 1)
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive_remote(tfree_lead + 8u * b);
-                kb = min(k1, kb + P.chunk);
+                kb = min(k1, kb + chunk);
             }
             const int m0 = (t / P.tiles_n) * (2 * GB_M) + (int)rank * GB_M, n0 = (t % P.tiles_n) * BN;
             const int row = m0 + 32 * q + lane; // row of D
@@ -970,7 +981,7 @@ int gemm_run(const __half *a_hi, const __half *a_lo, const __half *b_hi, const _
     // g_tail_weight tile K blocks (its operands are not shared in L2 with
     // other units at the time), so split = total per w / (per w + 1) evens
     // the two kinds of unit; w <= 0 turns the split off.
-    const int total = pair ? 3 * P.kblocks : P.kblocks;
+    const int total = P.kblocks; // K steps: all three split products per step, both forms
     P.total = total;
     P.split = total;
     P.extra = 0;
