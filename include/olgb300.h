@@ -402,8 +402,8 @@ double olg_cgh_gemm_tail_weight(double w);
  * and returns the previous value; other values only return it. */
 int olg_cgh_gemm_chunk(int kblocks);
 /* Tile form of the GEMM (no counterpart in the reference): 1 = 256 x BN tiles
- * on pairs of SMs (a two-CTA cluster sharing each MMA), 0 = 128 x BN tiles on
- * single SMs (the default).  Sets the form when on is 0 or 1 and returns
+ * on pairs of SMs (a two-CTA cluster sharing each MMA; the default), 0 =
+ * 128 x BN tiles on single SMs.  Sets the form when on is 0 or 1 and returns
  * the previous one; any other value only returns the current one. */
 int olg_cgh_gemm_pairs(int on);
 /* Autotuner of the tile form and that split (project-written; the reference

@@ -611,12 +611,11 @@ __global__ void __launch_bounds__(GB_THREADS, 1)
 // CTA r of the pair loads A rows [128 r, +128) and B rows [BN/2 r, +BN/2) of
 // the tile into its own shared memory; the even CTA issues the M = 256 MMAs,
 // which read both CTAs' halves, and each CTA's TMEM receives its own 128 rows
-// of D.  Each SM then stages 31 KB per K block for the same tensor work that
-// takes 46 KB on a single-SM 128 x 240 tile, so shared memory (TMA writes
-// plus MMA operand reads) is lighter, and the smaller stages fit a 6-deep
-// ring.  Measured on 1920 x 1080 x 10^4: the same issued-flop rate as the
-// single-SM form (~1.5 PFLOP/s), so there the single-SM form's finer M
-// padding (2176 vs 2304 rows of D) wins; the autotuner picks per shape.
+// of D.  With all four operand tiles of a K range staged together, each SM
+// stages 62 KB per 12 MMAs of 128 x BN per SM, against 92 KB on a single-SM
+// tile, and three stages fit instead of two.  Measured on 1920 x 1080 x 10^4:
+// 0.27 ms against 0.31 ms single-SM, despite the coarser M padding (2304 vs
+// 2176 rows of D); the autotuner picks per shape.
 //
 // Barriers: full[s] of the even CTA counts both CTAs' TMA bytes (its
 // producer posts the expected total; the odd CTA's loads complete on it
@@ -805,7 +804,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(GB_THREADS, 1)
 namespace {
 
 std::atomic<double> g_tail_weight{1.2};
-std::atomic<int> g_pairs{0}; // single-SM tiles unless switched (or autotuned) to pairs
+std::atomic<int> g_pairs{1}; // two-SM tiles unless switched (or autotuned) to single-SM
 std::atomic<int> g_chunk{8};
 std::mutex g_encode_mu;
 

@@ -78,10 +78,10 @@ def test_tuning_knobs_without_gpu():
     assert L.olg_cgh_gemm_tail_weight(w) == 2.0
     # GEMM tile form: 0 / 1 set it, anything else only reads it
     f = L.olg_cgh_gemm_pairs(-1)
-    assert f == 0
-    assert L.olg_cgh_gemm_pairs(1) == 0
-    assert L.olg_cgh_gemm_pairs(7) == 1
-    assert L.olg_cgh_gemm_pairs(f) == 1
+    assert f == 1
+    assert L.olg_cgh_gemm_pairs(0) == 1
+    assert L.olg_cgh_gemm_pairs(7) == 0
+    assert L.olg_cgh_gemm_pairs(f) == 0
     # GEMM accumulation chunk: 1..64 K blocks
     ch = L.olg_cgh_gemm_chunk(-1)
     assert ch == 8
