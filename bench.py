@@ -66,7 +66,7 @@ ADAM = dict(n=2048, p=6.4e-6, lam=532e-9, planes=8, z0=0.08, dz=0.01, lr=0.05, s
 # kernels each roofline covers, from ncu captures of this bench's own timed
 # region (--ncu-range); the profile file named beside each holds the command.
 TRAFFIC = {
-    "cgh": (553.6e6 + 15.6e6, "k_cgh_gemm, profiles/cgh_gemm_1920x1080_10k.md"),
+    "cgh": (360.2e6 + 14.6e6, "k_cgh_gemm2 (two-SM tiles), profiles/cgh_gemm_1920x1080_10k.md"),
     "asm": ((8.5 + 16.9 + 16.8) * 1e6, "the three passes, profiles/asm_1024_kernels.md (S stays in L2)"),
     "wrp": ((134.4 + 205.0 + 268.5 + 211.6 + 268.5 + 99.1) * 1e6,
             "the three 8192-point passes of step 2, profiles/asm_4096_to_8192_wrp_step2.md"),
@@ -524,8 +524,9 @@ def wl_cgh(x, K, W, cpu):
         "roofline": {"bound": "tensor", "achieved": ach_tf, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": ach_tf / pk["bf16_tflops"], "traffic": traffic("cgh")[0],
                      "traffic_source": traffic("cgh")[1],
-                     "note": f"k_cgh_gemm alone ({ms_g:.3f} ms): 24 M N K issued f16 flop (3 split products x "
-                             f"4 real GEMMs), useful 8 M N K; peak = {pk_kind} dense bf16 (f16 same rate)"},
+                     "note": f"the GEMM kernel alone ({ms_g:.3f} ms): 24 M N K f16 flop (3 split products x "
+                             f"4 real GEMMs; tile padding not counted), useful 8 M N K; "
+                             f"peak = {pk_kind} dense bf16 (f16 same rate)"},
         "exact_kernel_sfu": {"achieved": sfu_gops, "peak": peak_gops, "unit": "Gop/s (MUFU)",
                              "frac": sfu_gops / peak_gops,
                              "note": f"exact kernel: 2 MUFU (sin, cos) per term; peak {nsm} SM x 16 MUFU/clk x "
