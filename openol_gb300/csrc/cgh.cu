@@ -397,11 +397,10 @@ __global__ void k_cgh_adj_reduce(AdjParams A)
 // bands so that chunks x bands fills about 8 waves of the resident CTAs
 static int adj_bands(bool exact, int chunks, int nsub)
 {
-    int dev = 0, nsm = 152, occ = 4;
+    int dev = 0, occ = 4;
+    const int nsm = sm_count();
     if (cudaGetDevice(&dev) == cudaSuccess) {
         int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0) nsm = v;
-        v = 0;
         const cudaError_t e = exact ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cgh_adj<true>, 256, 0)
                                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_cgh_adj<false>, 256, 0);
         if (e == cudaSuccess && v > 0) occ = v;

@@ -32,6 +32,8 @@ int context_id(unsigned long long *id);
 // Budget of one bounded device-side wait, in SM clock cycles (default 4e9,
 // about 2 s at 2 GHz); olg_wait_budget_cycles sets it.
 long long wait_budget_cycles();
+// SMs of the current device (cached per device; prop.cu)
+int sm_count();
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // against libcuda).

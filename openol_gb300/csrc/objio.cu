@@ -107,7 +107,7 @@ int minmax(const float *p, int n, float out[6], cudaStream_t st)
     if (int rc = sc.acquire(nullptr, 0, 6 * sizeof(int), st)) return rc;
     int *mm = (int *)sc.ptr;
     k_obj_init<<<1, 32, 0, st>>>(mm);
-    const int g = std::min(grid_for(n, 256), 152 * 8);
+    const int g = std::min(grid_for(n, 256), 8 * sm_count());
     k_obj_minmax<<<g, 256, 0, st>>>(p, n, mm);
     count_launch(2);
     if (int rc = check_launch("k_obj_minmax")) return rc;

@@ -58,7 +58,8 @@ __global__ void k_loss_scale(double *loss, double s) { *loss *= s; }
 int elem_grid(long n)
 {
     long g = (n + 255) / 256;
-    return (int)(g > 152 * 8 ? 152 * 8 : (g < 1 ? 1 : g));
+    const long cap = 8L * sm_count(); // grid-stride beyond eight CTAs per SM
+    return (int)(g > cap ? cap : (g < 1 ? 1 : g));
 }
 
 PropParams asm_params(const void *in, void *out, int ny, int nx, double dy, double dx, double lambda, double z, bool conj,

@@ -20,9 +20,6 @@ namespace olg {
 int register_twiddle_uploader(int (*fn)(const float2 *tw, const float4 *tw4));
 int ensure_twiddles();
 
-// SMs of the current device (cached per device; 152 on GB300)
-int sm_count();
-
 // selected launch variant per pass kind (0 rows fwd, 1 cols, 2 rows inv) and
 // log2 of the FFT length; atomic so that a set or an autotune on one host
 // thread races no launch on another (autotune.cu)

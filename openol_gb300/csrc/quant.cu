@@ -78,7 +78,8 @@ __global__ void k_binarize(const float2 *u, uint8_t *img, long n)
 static int grid_for(long n)
 {
     long g = (n + 255) / 256;
-    return (int)(g > 152 * 16 ? 152 * 16 : (g < 1 ? 1 : g));
+    const long cap = 16L * sm_count(); // grid-stride beyond sixteen CTAs per SM
+    return (int)(g > cap ? cap : (g < 1 ? 1 : g));
 }
 
 } // namespace olg
