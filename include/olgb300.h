@@ -299,6 +299,16 @@ int olg_batch_plan_destroy(olg_batch_plan plan);
 typedef struct olg_prop_plan_s *olg_prop_plan;
 int olg_prop_plan_create(const olg_field *field, olg_prop_plan *plan);
 int olg_prop_plan_execute(olg_prop_plan plan, const void *in, void *out, olg_stream_t stream);
+/* A sequence of `count` host fields through one plan (host_out[i] = the
+ * propagation of host_in[i]; page-locked host memory for asynchronous
+ * copies).  Field i is copied into device slot i % 3 on a copy stream owned
+ * by the plan, propagated in place there on `stream` and copied back on a
+ * second copy stream, so field i+1's copy in and field i-1's copy out overlap
+ * field i's passes.  Ordered on `stream` like `count` calls of
+ * olg_prop_plan_execute: synchronise `stream` before reading host_out.  The
+ * slots (3 fields) are allocated on first use and freed with the plan. */
+int olg_prop_plan_execute_host(olg_prop_plan plan, const void *const *host_in, void *const *host_out, int count,
+                               olg_stream_t stream);
 int olg_prop_plan_destroy(olg_prop_plan plan);
 
 /* -------------------------------------------------- phase optimisation */
@@ -386,6 +396,21 @@ size_t olg_cgh_gemm_workspace_bytes(int n_points, int ny, int nx);
 int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, const float *phase0, int n_points, void *U,
                              int ny, int nx, double py, double px, double lambda, int flags, void *work,
                              size_t work_bytes, olg_stream_t stream);
+/* A sequence of `count` holograms from host point clouds (the host-buffer
+ * form of olg_cgh_fresnel_gemm_c64, as ol::Cgh takes host objects,
+ * olcgh.h:351-379): U[i] (ny x nx complex64, host) = the hologram of
+ * points[i] (n_points[i] x 3 floats, host), with amp[i] / phase0[i] (host;
+ * the arrays or their entries may be NULL: unit amplitude, zero phase).
+ * Cloud i goes up into a device slot on a copy stream, its hologram is formed
+ * on `stream` and comes down on a second copy stream, so hologram i-1's copy
+ * out and cloud i+1's copy in overlap hologram i's GEMM (page-locked host
+ * memory for asynchronous copies).  Ordered on `stream` like `count` single
+ * calls: synchronise `stream` before reading U.  Scratch from the
+ * stream-ordered pool: three slots of clouds and holograms plus one GEMM
+ * workspace.  OLG_ACCUMULATE and OLG_REUSE_OPERANDS are rejected. */
+int olg_cgh_fresnel_gemm_host_c64(const float *const *points, const float *const *amp, const float *const *phase0,
+                                  const int *n_points, void *const *U, int count, int ny, int nx, double py,
+                                  double px, double lambda, int flags, olg_stream_t stream);
 /* Tuning hook of the GEMM's work split (no counterpart in the reference):
  * when a hologram has fewer output tiles than the GPU has tile units (SMs, or
  * SM pairs), the spare units take the last part of every tile's K range, and

@@ -7,7 +7,7 @@ with PyTorch CUDA tensors standing in for the reference's device buffers.
 """
 from ._lib import OlgError, launch_count, lib  # noqa: F401
 from .cgh import (Cgh, Object2cuda, autotune_cgh_gemm, WRPMethod, WRPMethod_D, WRPStep1, WRPStep1_D, WRPStep2,  # noqa: F401
-                  cgh_adjoint_gemm_workspace, cgh_exact, cgh_exact_adjoint, cgh_fresnel, cgh_fresnel_adjoint, cgh_fresnel_adjoint_gemm, cgh_fresnel_gemm, cgh_gemm_pairs, cgh_gemm_workspace, device_fault_check, gCgh, gCghReduction, gObject, wrp_plane_z)
+                  cgh_adjoint_gemm_workspace, cgh_exact, cgh_exact_adjoint, cgh_fresnel, cgh_fresnel_adjoint, cgh_fresnel_adjoint_gemm, cgh_fresnel_gemm, cgh_fresnel_gemm_host, cgh_gemm_pairs, cgh_gemm_workspace, device_fault_check, gCgh, gCghReduction, gObject, wrp_plane_z)
 from .img import MODE, binarize, complex2img  # noqa: F401
 from .objects import (OBJSET_MODE, ZMIDDLE, ZMIN, bmpread, bmpwrite, objinfo, objread, objset, objsort,  # noqa: F401
                       objwrite_3d)

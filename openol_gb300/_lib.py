@@ -68,6 +68,7 @@ SIGNATURES = {
     "olg_batch_execute_host": (_i, [_p, _p, _p, _p]),
     "olg_prop_plan_create": (_i, [_p, _p]),
     "olg_prop_plan_execute": (_i, [_p, _p, _p, _p]),
+    "olg_prop_plan_execute_host": (_i, [_p, _p, _p, _i, _p]),
     "olg_prop_plan_destroy": (_i, [_p]),
     "olg_batch_check": (_i, [_p]),
     "olg_batch_plan_items": (_i, [_p]),
@@ -89,6 +90,7 @@ SIGNATURES = {
     "olg_cgh_exact_adjoint_c64": (_i, [_p, _i, _p, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),
     "olg_cgh_gemm_workspace_bytes": (_sz, [_i, _i, _i]),
     "olg_cgh_fresnel_gemm_c64": (_i, [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d, _i, _p, _sz, _p]),
+    "olg_cgh_fresnel_gemm_host_c64": (_i, [_p, _p, _p, _p, _p, _i, _i, _i, _d, _d, _d, _i, _p]),
     "olg_device_fault_check": (_i, [_i]),
     "olg_wrp_plane_z": (_f, [_i, _i, _i, _f, _f, _f, _f, _f]),
     "olg_wrp_step1_c64": (_i, [_p, _i, _p, _i, _i, _f, _f, _f, _f, _i, _p]),

@@ -108,6 +108,24 @@ class PropPlan:
         call("olg_prop_plan_execute", self._plan, u_in.data_ptr(), u_out.data_ptr(), _stream(stream))
         return u_out
 
+    def execute_host(self, host_in, host_out, stream=None):
+        """A sequence of host fields through the plan (olg_prop_plan_execute_host):
+        ``host_out[i]`` = the propagation of ``host_in[i]``, with field i+1's copy
+        in and field i-1's copy out overlapping field i's passes.  Host tensors:
+        contiguous CPU complex64 of the plan's shape, pinned (``pin_memory()``)
+        for the copies to run asynchronously.  Ordered on ``stream``: synchronize
+        it before reading ``host_out``."""
+        if len(host_in) != len(host_out):
+            raise ValueError("one host output per host input")
+        for t in list(host_in) + list(host_out):
+            if t.is_cuda or t.dtype != torch.complex64 or not t.is_contiguous() or tuple(t.shape) != self.shape:
+                raise TypeError("host fields must be contiguous CPU complex64 tensors of the plan's shape")
+        n = len(host_in)
+        hin = (C.c_void_p * max(n, 1))(*[t.data_ptr() for t in host_in])
+        hout = (C.c_void_p * max(n, 1))(*[t.data_ptr() for t in host_out])
+        call("olg_prop_plan_execute_host", self._plan, hin, hout, n, _stream(stream))
+        return host_out
+
     def close(self):
         if self._plan:
             lib().olg_prop_plan_destroy(self._plan)

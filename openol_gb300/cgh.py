@@ -121,6 +121,47 @@ def cgh_fresnel_gemm(gobj, U, *, ny, nx, py, px, lam, amp=None, phase0=None, acc
     return U
 
 
+def cgh_fresnel_gemm_host(points, holograms, *, ny, nx, py, px, lam, amp=None, phase0=None, stream=None):
+    """A sequence of holograms from host point clouds (olg_cgh_fresnel_gemm_host_c64):
+    ``holograms[i]`` (CPU complex64, ny x nx) = the Fresnel-form hologram of
+    ``points[i]`` (CPU float32, n_i x 3), with ``amp[i]`` / ``phase0[i]`` (CPU
+    float32, n_i; lists or entries may be None).  Cloud i+1's copy in and
+    hologram i-1's copy out overlap hologram i's GEMM; pinned tensors
+    (``pin_memory()``) for the copies to run asynchronously.  Ordered on
+    ``stream``: synchronize it before reading the holograms."""
+    n = len(points)
+    if len(holograms) != n:
+        raise ValueError("one hologram per point cloud")
+
+    def host(t, dtype, what):
+        if t is None:
+            return None
+        if not (isinstance(t, torch.Tensor) and not t.is_cuda and t.dtype == dtype and t.is_contiguous()):
+            raise TypeError(f"{what} must be contiguous CPU {dtype} tensors")
+        return t
+
+    amp = list(amp) if amp is not None else [None] * n
+    phase0 = list(phase0) if phase0 is not None else [None] * n
+    if len(amp) != n or len(phase0) != n:
+        raise ValueError("one amplitude / phase entry per point cloud")
+    counts = []
+    for i in range(n):
+        p = host(points[i], torch.float32, "points")
+        if p.dim() != 2 or p.shape[1] != 3:
+            raise ValueError("points must be n x 3")
+        counts.append(int(p.shape[0]))
+        for t, what in ((amp[i], "amp"), (phase0[i], "phase0")):
+            if host(t, torch.float32, what) is not None and t.numel() != counts[-1]:
+                raise ValueError(f"{what}[{i}] must have one entry per point")
+        h = host(holograms[i], torch.complex64, "holograms")
+        if tuple(h.shape) != (ny, nx):
+            raise ValueError("holograms must be ny x nx")
+    arr = lambda ts: (C.c_void_p * max(n, 1))(*[t.data_ptr() if t is not None else None for t in ts])
+    call("olg_cgh_fresnel_gemm_host_c64", arr(points), arr(amp), arr(phase0), (C.c_int * max(n, 1))(*counts),
+         arr(holograms), n, int(ny), int(nx), float(py), float(px), float(lam), 0, _stream(stream))
+    return holograms
+
+
 def autotune_cgh_gemm(n_points, ny, nx, reps=5, stream=None):
     """Time the GEMM's tile form and K-tail split for this hologram shape
     (olg_autotune_cgh_gemm) and keep the fastest; returns (pairs, tail weight)."""

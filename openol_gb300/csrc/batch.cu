@@ -542,6 +542,11 @@ struct olg_prop_plan_s {
     olg_field F{};
     char *mem = nullptr;
     PropSetup S{};
+    // olg_prop_plan_execute_host: three device field slots and the copy
+    // pipeline, made on first use
+    char *slots = nullptr;
+    size_t slot_bytes = 0;
+    HostPipeline pipe;
 };
 
 extern "C" int olg_prop_plan_create(const olg_field *field, olg_prop_plan *out)
@@ -599,10 +604,62 @@ extern "C" int olg_prop_plan_execute(olg_prop_plan plan, const void *in, void *o
     return run_passes(P, (cudaStream_t)stream);
 }
 
+// A sequence of host fields through one plan: field i goes up into device
+// slot i % 3 on the plan's copy-in stream, is propagated in place there on
+// the caller's stream and comes down on the copy-out stream, so field i+1's
+// copy in and field i-1's copy out overlap field i's passes.  Ordered on
+// `stream` like `count` calls of olg_prop_plan_execute (the propagations
+// themselves run one after another: they share the plan's scratch).
+extern "C" int olg_prop_plan_execute_host(olg_prop_plan plan, const void *const *host_in, void *const *host_out,
+                                          int count, olg_stream_t stream)
+{
+    if (!plan) return fail(OLG_ERR_INVALID_ARG, "null plan");
+    if (count < 0) return fail(OLG_ERR_INVALID_ARG, "negative field count");
+    if (count == 0) return OLG_OK;
+    if (!host_in || !host_out) return fail(OLG_ERR_INVALID_ARG, "null host field arrays");
+    for (int i = 0; i < count; ++i)
+        if (!host_in[i] || !host_out[i]) return fail(OLG_ERR_INVALID_ARG, "null host field");
+    const size_t field_bytes = sizeof(float2) * (size_t)plan->F.ny * plan->F.nx;
+    if (!plan->slots) {
+        const size_t sb = align_up(field_bytes, 256);
+        const cudaError_t e = cudaMalloc(&plan->slots, HostPipeline::SLOTS * sb);
+        if (e != cudaSuccess) {
+            plan->slots = nullptr;
+            return cuda_fail(e, "cudaMalloc (plan field slots)");
+        }
+        plan->slot_bytes = sb;
+    }
+    if (int rc = plan->pipe.init()) return rc;
+    HostPipeline &H = plan->pipe;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (int rc = H.begin(st)) return rc;
+    for (int i = 0; i < count; ++i) {
+        char *dev = plan->slots + (size_t)(i % HostPipeline::SLOTS) * plan->slot_bytes;
+        if (int rc = H.copy_in_begin(i)) return rc;
+        cudaError_t e = cudaMemcpyAsync(dev, host_in[i], field_bytes, cudaMemcpyHostToDevice, H.s_in);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (field in)");
+        if (int rc = H.copy_in_end(i, st)) return rc;
+        PropParams P = plan->S.P;
+        P.in = (const float2 *)dev;
+        P.out = (float2 *)dev;
+        if (int rc = run_passes(P, st)) return rc;
+        if (int rc = H.compute_end(i, st)) return rc;
+        e = cudaMemcpyAsync(host_out[i], dev, field_bytes, cudaMemcpyDeviceToHost, H.s_out);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (field out)");
+        if (int rc = H.copy_out_end(i)) return rc;
+    }
+    return H.end(st);
+}
+
 extern "C" int olg_prop_plan_destroy(olg_prop_plan plan)
 {
     if (!plan) return OLG_OK;
-    const cudaError_t e = cudaFree(plan->mem);
+    plan->pipe.release();
+    cudaError_t e = cudaFree(plan->mem);
+    if (plan->slots) {
+        const cudaError_t e2 = cudaFree(plan->slots);
+        if (e == cudaSuccess) e = e2;
+    }
     delete plan;
     return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaFree (propagation plan)");
 }

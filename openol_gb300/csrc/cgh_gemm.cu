@@ -1064,6 +1064,89 @@ extern "C" int olg_cgh_fresnel_gemm_c64(const float *points, const float *amp, c
                     st);
 }
 
+// A sequence of holograms from host point clouds: cloud i goes up into device
+// slot i % 3 on a copy-in stream, its hologram is formed there on the caller's
+// stream (olg_cgh_fresnel_gemm_c64, one workspace for all) and comes down on
+// a copy-out stream, so hologram i-1's copy out and cloud i+1's copy in
+// overlap hologram i's GEMM.  Ordered on `stream` like `count` single calls.
+extern "C" int olg_cgh_fresnel_gemm_host_c64(const float *const *points, const float *const *amp,
+                                             const float *const *phase0, const int *n_points, void *const *U,
+                                             int count, int ny, int nx, double py, double px, double lambda,
+                                             int flags, olg_stream_t stream)
+{
+    if (count < 0) return fail(OLG_ERR_INVALID_ARG, "negative hologram count");
+    if (count == 0) return OLG_OK;
+    if (!points || !n_points || !U) return fail(OLG_ERR_INVALID_ARG, "null host arrays");
+    if (flags & (OLG_ACCUMULATE | OLG_REUSE_OPERANDS))
+        return fail(OLG_ERR_INVALID_ARG, "the host form writes each hologram afresh (no OLG_ACCUMULATE or "
+                                         "OLG_REUSE_OPERANDS)");
+    if (ny <= 0 || nx <= 0) return fail(OLG_ERR_INVALID_ARG, "bad sizes");
+    if (nx > 4096 || ny > 4096) return fail(OLG_ERR_UNSUPPORTED_SIZE, "hologram side must be <= 4096 (exact w^2 in float)");
+    if (!(px > 0) || !(py > 0) || !(lambda > 0)) return fail(OLG_ERR_INVALID_ARG, "bad physical parameters");
+    int n_max = 0;
+    for (int i = 0; i < count; ++i) {
+        if (n_points[i] < 0) return fail(OLG_ERR_INVALID_ARG, "negative point count");
+        if ((!points[i] && n_points[i] > 0) || !U[i]) return fail(OLG_ERR_INVALID_ARG, "null host cloud or hologram");
+        n_max = std::max(n_max, n_points[i]);
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    // per slot: xyz, amplitudes, phases, hologram; then the GEMM workspace
+    const size_t pb = align_up(sizeof(float) * 3 * (size_t)n_max + 16, 256);
+    const size_t ab = align_up(sizeof(float) * (size_t)n_max + 16, 256);
+    const size_t ub = align_up(sizeof(float2) * (size_t)ny * nx, 256);
+    const size_t slot = pb + 2 * ab + ub;
+    const size_t wb = align_up(olg_cgh_gemm_workspace_bytes(n_max, ny, nx), 256);
+    Scratch sc;
+    if (int rc = sc.acquire(nullptr, 0, HostPipeline::SLOTS * slot + wb, st)) return rc;
+    char *work = (char *)sc.ptr + HostPipeline::SLOTS * slot;
+    // on an early return the copy streams may still use the scratch, which
+    // is freed on `stream`: let them finish first
+    struct Pipe : HostPipeline {
+        bool ended = false;
+        ~Pipe()
+        {
+            if (!ended && s_in) {
+                cudaStreamSynchronize(s_in);
+                cudaStreamSynchronize(s_out);
+            }
+            release();
+        }
+    } H;
+    if (int rc = H.init()) return rc;
+    if (int rc = H.begin(st)) return rc;
+    auto up = [&](void *dst, const void *src, size_t bytes) -> int {
+        if (!bytes) return OLG_OK;
+        const cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, H.s_in);
+        return e == cudaSuccess ? OLG_OK : cuda_fail(e, "cudaMemcpyAsync (cloud in)");
+    };
+    for (int i = 0; i < count; ++i) {
+        char *base = (char *)sc.ptr + (size_t)(i % HostPipeline::SLOTS) * slot;
+        float *d_pts = (float *)base, *d_amp = (float *)(base + pb), *d_ph = (float *)(base + pb + ab);
+        void *d_U = base + pb + 2 * ab;
+        const int n = n_points[i];
+        const bool has_amp = amp && amp[i], has_ph = phase0 && phase0[i];
+        if (int rc = H.copy_in_begin(i)) return rc;
+        if (int rc = up(d_pts, points[i], sizeof(float) * 3 * (size_t)n)) return rc;
+        if (has_amp)
+            if (int rc = up(d_amp, amp[i], sizeof(float) * (size_t)n)) return rc;
+        if (has_ph)
+            if (int rc = up(d_ph, phase0[i], sizeof(float) * (size_t)n)) return rc;
+        if (int rc = H.copy_in_end(i, st)) return rc;
+        if (int rc = olg_cgh_fresnel_gemm_c64(d_pts, has_amp ? d_amp : nullptr, has_ph ? d_ph : nullptr, n, d_U, ny,
+                                              nx, py, px, lambda, flags, work, wb, stream))
+            return rc;
+        if (int rc = H.compute_end(i, st)) return rc;
+        const cudaError_t e = cudaMemcpyAsync(U[i], d_U, sizeof(float2) * (size_t)ny * nx, cudaMemcpyDeviceToHost,
+                                              H.s_out);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (hologram out)");
+        if (int rc = H.copy_out_end(i)) return rc;
+    }
+    // the scratch is released on `stream` after this wait, behind every copy
+    const int rc = H.end(st);
+    H.ended = rc == OLG_OK;
+    return rc;
+}
+
 extern "C" size_t olg_cgh_adjoint_gemm_workspace_bytes(int n_points, int ny, int nx)
 {
     if (n_points <= 0 || ny <= 0 || nx <= 0) return 0;

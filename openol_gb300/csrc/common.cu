@@ -217,6 +217,93 @@ extern "C" long long olg_wait_budget_cycles(long long cycles)
     return olg::g_wait_budget.load();
 }
 
+namespace olg {
+
+int HostPipeline::init()
+{
+    if (s_in) return OLG_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking);
+    cudaEvent_t *all[2 + 3 * SLOTS] = {&entry, &last};
+    for (int k = 0; k < SLOTS; ++k) {
+        all[2 + k] = &in[k];
+        all[2 + SLOTS + k] = &done[k];
+        all[2 + 2 * SLOTS + k] = &out[k];
+    }
+    for (cudaEvent_t *v : all)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(v, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        release();
+        return cuda_fail(e, "creating the host copy pipeline");
+    }
+    return OLG_OK;
+}
+
+// Streams and events are released once the work queued on them has
+// completed, so this is safe right after the last enqueue.
+void HostPipeline::release()
+{
+    cudaEvent_t *all[2 + 3 * SLOTS] = {&entry, &last};
+    for (int k = 0; k < SLOTS; ++k) {
+        all[2 + k] = &in[k];
+        all[2 + SLOTS + k] = &done[k];
+        all[2 + 2 * SLOTS + k] = &out[k];
+    }
+    for (cudaEvent_t *v : all)
+        if (*v) {
+            cudaEventDestroy(*v);
+            *v = nullptr;
+        }
+    if (s_in) cudaStreamDestroy(s_in);
+    if (s_out) cudaStreamDestroy(s_out);
+    s_in = s_out = nullptr;
+}
+
+namespace {
+int ck(cudaError_t e, const char *what) { return e == cudaSuccess ? OLG_OK : cuda_fail(e, what); }
+} // namespace
+
+int HostPipeline::begin(cudaStream_t st)
+{
+    if (int rc = ck(cudaEventRecord(entry, st), "cudaEventRecord (pipeline entry)")) return rc;
+    if (int rc = ck(cudaStreamWaitEvent(s_in, entry, 0), "cudaStreamWaitEvent")) return rc;
+    return ck(cudaStreamWaitEvent(s_out, entry, 0), "cudaStreamWaitEvent");
+}
+
+// slot i % 3 is free once item i - 3 has been copied out of it
+int HostPipeline::copy_in_begin(int i)
+{
+    if (i < SLOTS) return OLG_OK;
+    return ck(cudaStreamWaitEvent(s_in, out[i % SLOTS], 0), "cudaStreamWaitEvent (slot free)");
+}
+
+int HostPipeline::copy_in_end(int i, cudaStream_t st)
+{
+    if (int rc = ck(cudaEventRecord(in[i % SLOTS], s_in), "cudaEventRecord (copied in)")) return rc;
+    return ck(cudaStreamWaitEvent(st, in[i % SLOTS], 0), "cudaStreamWaitEvent (copied in)");
+}
+
+int HostPipeline::compute_end(int i, cudaStream_t st)
+{
+    if (int rc = ck(cudaEventRecord(done[i % SLOTS], st), "cudaEventRecord (computed)")) return rc;
+    return ck(cudaStreamWaitEvent(s_out, done[i % SLOTS], 0), "cudaStreamWaitEvent (computed)");
+}
+
+int HostPipeline::copy_out_end(int i)
+{
+    return ck(cudaEventRecord(out[i % SLOTS], s_out), "cudaEventRecord (copied out)");
+}
+
+// The caller's stream waited for every copy in before the computation that
+// used it, so waiting for the last copy out orders everything.
+int HostPipeline::end(cudaStream_t st)
+{
+    if (int rc = ck(cudaEventRecord(last, s_out), "cudaEventRecord (pipeline end)")) return rc;
+    return ck(cudaStreamWaitEvent(st, last, 0), "cudaStreamWaitEvent (pipeline end)");
+}
+
+} // namespace olg
+
 extern "C" int olg_inject_alloc_failures(int n)
 {
     return olg::g_fail_allocs.exchange(n > 0 ? n : 0);

@@ -35,6 +35,31 @@ long long wait_budget_cycles();
 // SMs of the current device (cached per device; prop.cu)
 int sm_count();
 
+// Copies of a sequence of host items pipelined against their computation:
+// item i's inputs go up on the copy-in stream, its computation runs on the
+// caller's stream and its result comes down on the copy-out stream, and
+// device slot i % 3 holds item i.  So item i+1's copy in and item i-1's copy
+// out overlap item i's computation.  Both copy streams first wait for the
+// caller's stream, and the caller's stream ends waiting for the last copy
+// out, so the whole sequence is ordered on the caller's stream like one call.
+// Per item: copy_in_begin (then the copies in on s_in), copy_in_end (then
+// the computation on the caller's stream), compute_end (then the copies out
+// on s_out), copy_out_end.
+struct HostPipeline {
+    static constexpr int SLOTS = 3;
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    cudaEvent_t entry = nullptr, last = nullptr;
+    cudaEvent_t in[SLOTS]{}, done[SLOTS]{}, out[SLOTS]{};
+    int init(); // idempotent
+    void release();
+    int begin(cudaStream_t st);
+    int copy_in_begin(int i);
+    int copy_in_end(int i, cudaStream_t st);
+    int compute_end(int i, cudaStream_t st);
+    int copy_out_end(int i);
+    int end(cudaStream_t st);
+};
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // against libcuda).
 int tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000 *out);

@@ -209,12 +209,33 @@ def test_plan_validation_without_gpu():
     assert L.olg_prop_plan_create(C.byref(desc(method=2, ox=float("inf"))), C.byref(plan)) == -1
     assert plan.value is None
     assert L.olg_prop_plan_execute(None, base, base, None) == -1
+    ptrs = (C.c_void_p * 1)(base)
+    assert L.olg_prop_plan_execute_host(None, ptrs, ptrs, 1, None) == -1
     assert L.olg_prop_plan_destroy(None) == 0
     # the batch plan runs the same checks on every field
     arr = (F * 2)(desc(ny=256, nx=256), desc(ny=256, nx=256, method=2, s=0.0))
     bplan = C.c_void_p()
     assert L.olg_batch_plan_create(arr, 2, C.byref(bplan)) == -1
     assert b"s = 0" in L.olg_last_error() or b"s|s-1|" in L.olg_last_error()
+
+
+def test_cgh_host_sequence_validation_without_gpu():
+    """The host-cloud CGH sequence checks its arguments before any device work."""
+    L = _lib.lib()
+    buf = (C.c_float * 16)()
+    p = (C.c_void_p * 1)(C.addressof(buf))
+    n = (C.c_int * 1)(1)
+    args = (6, 8, 8e-6, 8e-6, 532e-9)
+    assert L.olg_cgh_fresnel_gemm_host_c64(p, None, None, n, p, 0, *args, 0, None) == 0      # nothing to do
+    assert L.olg_cgh_fresnel_gemm_host_c64(p, None, None, n, p, -1, *args, 0, None) == -1
+    assert L.olg_cgh_fresnel_gemm_host_c64(None, None, None, n, p, 1, *args, 0, None) == -1
+    assert L.olg_cgh_fresnel_gemm_host_c64(p, None, None, n, p, 1, *args, _lib.OLG_ACCUMULATE, None) == -1
+    assert L.olg_cgh_fresnel_gemm_host_c64(p, None, None, n, p, 1, 6, 5000, 8e-6, 8e-6, 532e-9, 0, None) == -2
+    assert L.olg_cgh_fresnel_gemm_host_c64(p, None, None, n, p, 1, 6, 8, 8e-6, 8e-6, -1.0, 0, None) == -1
+    bad = (C.c_int * 1)(-3)
+    assert L.olg_cgh_fresnel_gemm_host_c64(p, None, None, bad, p, 1, *args, 0, None) == -1
+    nullh = (C.c_void_p * 1)(None)
+    assert L.olg_cgh_fresnel_gemm_host_c64(p, None, None, n, nullh, 1, *args, 0, None) == -1
 
 
 def test_workspace_size():

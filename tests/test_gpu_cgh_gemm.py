@@ -96,3 +96,34 @@ def test_gemm_workload_vs_direct_and_oracle():
     og.cgh_fresnel_gemm(obj, G, accumulate=True, work=ws, **kw)
     og.device_fault_check()
     assert rel_l2(host(G), 2 * host(D)) < TOL
+
+
+def test_gemm_host_sequence_matches_device_calls():
+    """olg_cgh_fresnel_gemm_host_c64: five pinned host clouds of different sizes
+    (one empty, one without amplitudes or phases) through the three-slot copy
+    pipeline give the device calls' holograms (the same kernels; float-atomic
+    accumulation order may differ in the last bits)."""
+    ny, nx, p, lam = 72, 200, 8e-6, 532e-9
+    rng = np.random.default_rng(5)
+    clouds, amps, phs = [], [], []
+    for n in (300, 0, 1000, 64, 513):
+        pts = np.stack([rng.random(n) * nx * p, rng.random(n) * ny * p, 0.02 + rng.random(n) * 0.01], 1)
+        clouds.append(torch.from_numpy(pts.astype(np.float32).reshape(-1, 3)).pin_memory())
+        amps.append(torch.from_numpy((0.5 + 0.5 * rng.random(n)).astype(np.float32)).pin_memory())
+        phs.append(torch.from_numpy((2 * np.pi * rng.random(n)).astype(np.float32)).pin_memory())
+    amps[3] = phs[3] = None
+    holo = [torch.full((ny, nx), complex(np.nan, np.nan), dtype=torch.complex64).pin_memory() for _ in clouds]
+    og.cgh_fresnel_gemm_host(clouds, holo, ny=ny, nx=nx, py=p, px=p, lam=lam, amp=amps, phase0=phs)
+    torch.cuda.synchronize()
+    og.device_fault_check()
+    for k in range(len(clouds)):
+        U = torch.zeros((ny, nx), dtype=torch.complex64, device="cuda")
+        og.cgh_fresnel_gemm(og.gObject(clouds[k].numpy()), U, ny=ny, nx=nx, py=p, px=p, lam=lam,
+                            amp=None if amps[k] is None else amps[k].cuda(),
+                            phase0=None if phs[k] is None else phs[k].cuda())
+        want = host(U)
+        got = holo[k].numpy().astype(np.complex128)
+        if clouds[k].shape[0] == 0:
+            assert np.abs(got).max() == 0
+        else:
+            assert rel_l2(got, want) < 1e-6, k
