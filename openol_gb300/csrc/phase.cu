@@ -78,6 +78,7 @@ PropParams asm_params(const void *in, void *out, int ny, int nx, double dy, doub
     P.tx = (float)(lambda * lambda * du * du);
     P.ty = (float)(lambda * lambda * dv * dv);
     P.zl = (float)zl;
+    P.tf_series = asm_series_ok(NY, NX, dv, du, lambda);
     return P;
 }
 

@@ -216,6 +216,15 @@ int check_phys(double dy, double dx, double lambda, double z, bool nonzero_z)
     return OLG_OK;
 }
 
+// Whether every t = lambda^2 (u^2 + v^2) of an NY x NX frequency grid (steps
+// du, dv; |u| <= NX du / 2, |v| <= NY dv / 2) is <= 1/64, where the ASM
+// transfer function's phase remainder is taken from its series.
+int asm_series_ok(double NY, double NX, double dv, double du, double lambda)
+{
+    const double um = 0.5 * NX * du, vm = 0.5 * NY * dv;
+    return lambda * lambda * (um * um + vm * vm) <= 1.0 / 64.0 ? 1 : 0;
+}
+
 int setup_asm(const void *in, void *out, int ny, int nx, double dy, double dx, double lambda, double z, int flags,
               const Layout &L, PropSetup *S)
 {
@@ -234,6 +243,7 @@ int setup_asm(const void *in, void *out, int ny, int nx, double dy, double dx, d
     P.tx = (float)(lambda * lambda * du * du);
     P.ty = (float)(lambda * lambda * dv * dv);
     P.zl = (float)zl;
+    P.tf_series = asm_series_ok(NY, NX, dv, du, lambda);
     S->P = P;
     S->chirps = false;
     return OLG_OK;

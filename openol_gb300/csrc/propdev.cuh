@@ -41,6 +41,8 @@ struct PropParams {
     float ay_hi, ay_lo;     // z lambda dv^2 / 2
     float tx, ty;           // lambda^2 du^2, lambda^2 dv^2
     float zl;               // z / lambda
+    // every t = lambda^2 (u^2 + v^2) of the grid is <= 1/64: g by its series
+    int tf_series;
     // chirp spectra (M_CHIRP)
     const float2 *Hx, *Hy;
     // pass-1 and pass-3 elementwise operations
@@ -111,10 +113,20 @@ __device__ __forceinline__ float2 asm_tf(const PropParams &P, int fx, int fy)
     // 1 ulp) moves the phase by < 1e-6 cycles at z / lambda ~ 3e5, where the
     // correctly rounded sqrtf costs a multi-instruction sequence per element.
     // A negative argument (evanescent t > 1) still gives NaN.
-    float s;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(s) : "f"(1.0f - t));
-    const float q = __fdividef(t, 1.0f + s); // 1 + s in [1, 2]: the fast divide is within 2 ulp
-    const float g = 0.5f * q * q;
+    float g;
+    if (P.tf_series) {
+        // g = (1 - sqrt(1 - t))^2 / 2 by the binomial series of sqrt(1 - t):
+        // g = t^2/8 + t^3/16 + 5 t^4/128 + 7 t^5/256 + 21 t^6/1024 + ...;
+        // for t <= 1/64 the first omitted term is < 2e-8 of g, below the
+        // float rounding of the sum.
+        const float t2 = t * t;
+        g = t2 * fmaf(t, fmaf(t, fmaf(t, 0.02734375f, 0.0390625f), 0.0625f), 0.125f);
+    } else {
+        float s;
+        asm("sqrt.approx.f32 %0, %1;" : "=f"(s) : "f"(1.0f - t));
+        const float q = __fdividef(t, 1.0f + s); // 1 + s in [1, 2]: the fast divide is within 2 ulp
+        g = 0.5f * q * q;
+    }
     float cyc = P.c0 - frac_mul(P.ax_hi, P.ax_lo, fx2) - frac_mul(P.ay_hi, P.ay_lo, fy2) - P.zl * g;
     if (P.shift) {
         if (P.band && (fx < P.fx_lo || fx > P.fx_hi || fy < P.fy_lo || fy > P.fy_hi)) return make_float2(0.f, 0.f);

@@ -53,6 +53,8 @@ bool axis_ok(int n);
 int validate(const void *a, const void *b, int ny, int nx);
 PropParams base_params(const void *in, void *out, int ny, int nx, const Layout &L);
 int run_passes(const PropParams &P, cudaStream_t st);
+// 1 when every t of the NY x NX ASM frequency grid is <= 1/64 (PropParams::tf_series)
+int asm_series_ok(double NY, double NX, double dv, double du, double lambda);
 long floor_lim(double v);
 void set_quad(float &hi, float &lo, double v);
 // frac(v) in [-0.5, 0.5]

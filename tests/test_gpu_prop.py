@@ -79,6 +79,19 @@ def test_asm_workload_1024():
     assert rel_l2(np.abs(g) ** 2, np.abs(ref) ** 2) < TOL
 
 
+# t = lambda^2 (u^2 + v^2) at the grid's corner: 0.0147 (just under the 1/64
+# above which the phase remainder is evaluated in closed form instead of by
+# its series; z / lambda = 3.8e5) and 0.089 (the closed form)
+@pytest.mark.parametrize("p,lam,z", [(3.1e-6, 532e-9, 0.2), (1.5e-6, 633e-9, 0.01)])
+@pytest.mark.parametrize("shape", [(256, 256), (128, 512)])
+def test_asm_phase_remainder_forms_vs_oracle(p, lam, z, shape):
+    rng = np.random.default_rng(int(p * 1e9) + shape[1])
+    u0 = field(rng, shape).astype(np.complex64)
+    u = dev(u0)
+    og.asm_prop(u, dy=p, dx=p, lam=lam, z=z)
+    assert rel_l2(host(u), O.asm_prop(c64(u0), p, p, lam, z)) < TOL
+
+
 @pytest.mark.parametrize("shape", [(32, 32), (64, 256), (512, 128), (256, 256)])
 @pytest.mark.parametrize("z", [0.02, -0.035])
 def test_all_methods_vs_oracle(shape, z):
