@@ -70,6 +70,8 @@ TRAFFIC = {
     "asm": ((8.5 + 16.9 + 16.8) * 1e6, "the three passes, profiles/asm_1024_kernels.md (S stays in L2)"),
     "wrp": ((134.4 + 205.0 + 268.5 + 211.6 + 268.5 + 99.1) * 1e6,
             "the three 8192-point passes of step 2, profiles/asm_4096_to_8192_wrp_step2.md"),
+    "adam": (4656.1e6, "every kernel of one step, the bench's L2 flush excluded (S and the spectra partly stay in "
+                       "L2), profiles/phase_grad_2048_8planes.md"),
 }
 
 
@@ -864,7 +866,8 @@ def wl_adam(x, K, W, cpu):
                 "d2h_bytes_per_step": phi0.nbytes},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach / pk["hbm_gbs"], "traffic": None,
+                     "frac": ach / pk["hbm_gbs"], "traffic": traffic("adam")[0],
+                     "traffic_source": traffic("adam")[1],
                      "note": f"{b_alg // (n * n)} n bytes per step (one shared forward spectrum, per plane an "
                              f"inverse column pass, the fused seed row pass and a forward column pass into the "
                              f"summed adjoint spectrum; Adam), n = 2048^2; peak {pk_kind}"},
