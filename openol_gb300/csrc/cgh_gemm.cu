@@ -1280,15 +1280,21 @@ extern "C" int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg
     } ev;
     if ((e = cudaEventCreate(&ev.a)) != cudaSuccess || (e = cudaEventCreate(&ev.b)) != cudaSuccess)
         return cuda_fail(e, "cudaEventCreate");
+    // Every (tile form, weight) candidate is timed `reps` times in each of two
+    // rounds, the second in reverse order, and keeps its fastest run: the
+    // choice then rests on each candidate's best case rather than on when in
+    // the sweep it ran.
     const double cand[] = {0.0, 1.0, 1.1, 1.2, 1.3, 1.45, 1.6};
-    double best_w = keep;
-    int best_p = keep_pairs;
-    float best = 1e30f;
-    for (int pr = 1; pr >= 0; --pr) {
-        g_pairs.store(pr);
-        for (double w : cand) {
-            g_tail_weight.store(w);
-            float tot = 0.f;
+    constexpr int NW = (int)(sizeof(cand) / sizeof(cand[0]));
+    float fastest[2][NW];
+    for (auto &row : fastest)
+        for (float &f : row) f = 1e30f;
+    for (int round = 0; round < 2; ++round) {
+        for (int k = 0; k < 2 * NW; ++k) {
+            const int idx = round == 0 ? k : 2 * NW - 1 - k;
+            const int pr = 1 - idx / NW, wi = idx % NW;
+            g_pairs.store(pr);
+            g_tail_weight.store(cand[wi]);
             for (int r = 0; r < reps; ++r) {
                 if ((e = cudaMemsetAsync(flush.ptr, r & 0xff, flush_bytes, st)) != cudaSuccess ||
                     (e = cudaEventRecord(ev.a, st)) != cudaSuccess) {
@@ -1305,15 +1311,20 @@ extern "C" int olg_autotune_cgh_gemm(int n_points, int ny, int nx, int reps, olg
                     restore();
                     return cuda_fail(e, "autotune timing");
                 }
-                tot += t;
-            }
-            if (tot < best) {
-                best = tot;
-                best_w = w;
-                best_p = pr;
+                fastest[pr][wi] = std::min(fastest[pr][wi], t);
             }
         }
     }
+    double best_w = keep;
+    int best_p = keep_pairs;
+    float best = 1e30f;
+    for (int pr = 1; pr >= 0; --pr)
+        for (int wi = 0; wi < NW; ++wi)
+            if (fastest[pr][wi] < best) {
+                best = fastest[pr][wi];
+                best_w = cand[wi];
+                best_p = pr;
+            }
     g_tail_weight.store(best_w);
     g_pairs.store(best_p);
     return OLG_OK;
