@@ -70,16 +70,19 @@ def test_plan_equals_single_call(case):
     plan.close()
 
 
+@pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
 @pytest.mark.parametrize("case", [CASES[0], CASES[3], CASES[4]], ids=["asm", "arss", "asm-mixed-radix"])
-def test_plan_host_sequence_equals_device_executions(case):
-    """olg_prop_plan_execute_host: seven pinned host fields (more than the three
+def test_plan_host_sequence_equals_device_executions(case, pinned):
+    """olg_prop_plan_execute_host: seven host fields (more than the three
     device slots, so slots are reused) give the device executions' results bit
-    for bit, and the caller's stream is ordered after the last copy out."""
+    for bit, and the caller's stream is ordered after the last copy out.
+    Pageable host memory gives the same results (its copies do not overlap)."""
     method, ny, nx, dy, dx, lam, z, s = case
     plan = og.PropPlan(method, ny, nx, dy=dy, dx=dx, lam=lam, z=z, s=s if s is not None else 0.5)
     hs = [field(7 * k + ny, ny, nx) for k in range(7)]
-    hin = [torch.from_numpy(h).pin_memory() for h in hs]
-    hout = [torch.full((ny, nx), complex(np.nan, np.nan), dtype=torch.complex64).pin_memory() for _ in hs]
+    pin = (lambda t: t.pin_memory()) if pinned else (lambda t: t)
+    hin = [pin(torch.from_numpy(h)) for h in hs]
+    hout = [pin(torch.full((ny, nx), complex(np.nan, np.nan), dtype=torch.complex64)) for _ in hs]
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
         plan.execute_host(hin, hout, stream=stream)
