@@ -632,23 +632,30 @@ extern "C" int olg_prop_plan_execute_host(olg_prop_plan plan, const void *const 
     if (int rc = plan->pipe.init()) return rc;
     HostPipeline &H = plan->pipe;
     cudaStream_t st = (cudaStream_t)stream;
-    if (int rc = H.begin(st)) return rc;
-    for (int i = 0; i < count; ++i) {
-        char *dev = plan->slots + (size_t)(i % HostPipeline::SLOTS) * plan->slot_bytes;
-        if (int rc = H.copy_in_begin(i)) return rc;
-        cudaError_t e = cudaMemcpyAsync(dev, host_in[i], field_bytes, cudaMemcpyHostToDevice, H.s_in);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (field in)");
-        if (int rc = H.copy_in_end(i, st)) return rc;
-        PropParams P = plan->S.P;
-        P.in = (const float2 *)dev;
-        P.out = (float2 *)dev;
-        if (int rc = run_passes(P, st)) return rc;
-        if (int rc = H.compute_end(i, st)) return rc;
-        e = cudaMemcpyAsync(host_out[i], dev, field_bytes, cudaMemcpyDeviceToHost, H.s_out);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (field out)");
-        if (int rc = H.copy_out_end(i)) return rc;
-    }
-    return H.end(st);
+    auto enqueue = [&]() -> int {
+        if (int rc = H.begin(st)) return rc;
+        for (int i = 0; i < count; ++i) {
+            char *dev = plan->slots + (size_t)(i % HostPipeline::SLOTS) * plan->slot_bytes;
+            if (int rc = H.copy_in_begin(i)) return rc;
+            cudaError_t e = cudaMemcpyAsync(dev, host_in[i], field_bytes, cudaMemcpyHostToDevice, H.s_in);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (field in)");
+            if (int rc = H.copy_in_end(i, st)) return rc;
+            PropParams P = plan->S.P;
+            P.in = (const float2 *)dev;
+            P.out = (float2 *)dev;
+            if (int rc = run_passes(P, st)) return rc;
+            if (int rc = H.compute_end(i, st)) return rc;
+            e = cudaMemcpyAsync(host_out[i], dev, field_bytes, cudaMemcpyDeviceToHost, H.s_out);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (field out)");
+            if (int rc = H.copy_out_end(i)) return rc;
+        }
+        return H.end(st);
+    };
+    const int rc = enqueue();
+    // on a failure part way, the copies already queued finish before the
+    // caller can reuse or free its host buffers
+    if (rc) H.drain();
+    return rc;
 }
 
 extern "C" int olg_prop_plan_destroy(olg_prop_plan plan)

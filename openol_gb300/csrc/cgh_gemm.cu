@@ -1105,10 +1105,7 @@ extern "C" int olg_cgh_fresnel_gemm_host_c64(const float *const *points, const f
         bool ended = false;
         ~Pipe()
         {
-            if (!ended && s_in) {
-                cudaStreamSynchronize(s_in);
-                cudaStreamSynchronize(s_out);
-            }
+            if (!ended) drain();
             release();
         }
     } H;

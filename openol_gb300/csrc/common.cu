@@ -294,6 +294,12 @@ int HostPipeline::copy_out_end(int i)
     return ck(cudaEventRecord(out[i % SLOTS], s_out), "cudaEventRecord (copied out)");
 }
 
+void HostPipeline::drain()
+{
+    if (s_in) cudaStreamSynchronize(s_in);
+    if (s_out) cudaStreamSynchronize(s_out);
+}
+
 // The caller's stream waited for every copy in before the computation that
 // used it, so waiting for the last copy out orders everything.
 int HostPipeline::end(cudaStream_t st)

@@ -58,6 +58,7 @@ struct HostPipeline {
     int compute_end(int i, cudaStream_t st);
     int copy_out_end(int i);
     int end(cudaStream_t st);
+    void drain(); // waits on the host for both copy streams (error paths)
 };
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
