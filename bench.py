@@ -50,6 +50,10 @@ WRP_DESC = "wrp 200000 points 1-5mm behind a 4096x4096 WRP, p=4um, lambda=532nm,
 ADAM_DESC = "adam 2048x2048 phase, 8 planes z=80..150mm, p=6.4um, lambda=532nm, 5% sparse targets"
 CGH = dict(ny=1080, nx=1920, p=8e-6, lam=532e-9, n=10000, zc=0.1, box=5e-3, seed=20261203 + 2)
 ASM = dict(n=1024, p=8e-6, lam=532e-9, z=0.05, seed=20261203 + 1)
+# the reference's default test field (tests/para.h: 1920*2 x 1080*2, p = 3.74 um,
+# 532 nm, d = -0.1 m), padded to 7680 x 4320: mixed-radix passes
+UHD = dict(ny=2160, nx=3840, p=3.74e-6, lam=532e-9, z=-0.1, seed=20261203 + 7)
+UHD_DESC = "asm 3840x2160 padded 7680x4320 (mixed radix), p=3.74um, lambda=532nm, z=-100mm"
 WRP = dict(N=4096, p=4e-6, lam=532e-9, n=200000, zw=0.15, ext=10e-3, seed=20261203 + 3)
 # tilted planes (the row beside the path): the ASM workload's field, rotated 0.1 rad (source form)
 # or 2 mrad (reference form: its frequency shift a13 / (lambda du) is ~30 samples per mrad here)
@@ -199,6 +203,20 @@ def cpu_asm_sample():
     u = asm_input().astype(np.complex128)
     t0 = time.perf_counter()
     r = O.asm_prop(u, ASM["p"], ASM["p"], ASM["lam"], ASM["z"])
+    return 1.0 / (time.perf_counter() - t0), r
+
+
+def uhd_input():
+    rng = np.random.default_rng(UHD["seed"])
+    shape = (UHD["ny"], UHD["nx"])
+    return ((rng.random(shape) < 0.5) * np.exp(2j * np.pi * rng.random(shape))).astype(np.complex64)
+
+
+def cpu_uhd_sample():
+    import oracle as O
+    u = uhd_input().astype(np.complex128)
+    t0 = time.perf_counter()
+    r = O.asm_prop(u, UHD["p"], UHD["p"], UHD["lam"], UHD["z"])
     return 1.0 / (time.perf_counter() - t0), r
 
 
@@ -369,6 +387,14 @@ def run_reference(args):
         sample = ("one field per size class (512^2 .. 4096^2) of the 96-field batch, FP64, each class costed "
                   "for all its fields, per step")
         config = {"workload": BATCH_DESC}
+    elif wl == "uhd":
+        for k in range(1 + min(args.steps, 2)):
+            v, _ = cpu_uhd_sample()
+            if k >= 1:
+                vals.append(v)
+        metric, unit = "mixed-radix ASM props/s", "props/s"
+        sample = "one full 3840x2160 -> 7680x4320 FP64 ASM propagation per step"
+        config = {"workload": UHD_DESC}
     elif wl == "tilt":
         for k in range(1 + min(args.steps, 3)):
             v, _ = cpu_tilt_sample()
@@ -1103,6 +1129,84 @@ def wl_tilt(x, K, W, cpu):
     return out
 
 
+def wl_uhd(x, K, W, cpu):
+    """ASM of the reference's default 3840 x 2160 test field: padded lengths
+    7680 = 2^9 3 5 and 4320 = 2^5 3^3 5 through the mixed-radix passes."""
+    torch, og, pk, pk_kind = x.torch, x.og, x.pk, x.pk_kind
+    stream, flush, barrier, max_over_ranks = x.stream, x.flush, x.barrier, x.max_over_ranks
+    ws, rank, local, args = x.ws, x.rank, x.local, x.args
+    c = UHD
+    ny, nx = c["ny"], c["nx"]
+    u0 = uhd_input()
+    src = torch.from_numpy(u0).cuda()
+    dst = torch.empty_like(src)
+    ws_buf = og.workspace(ny, nx)
+    kw = dict(dy=c["p"], dx=c["p"], lam=c["lam"], z=c["z"])
+
+    def step():
+        og.asm_prop(src, dst, work=ws_buf, **kw)
+
+    from openol_gb300.plain import plain_asm_prop
+
+    with ClockSampler(local) as clk:
+        l0 = og.launch_count()
+        ms = timed(torch, step, K, W, flush, stream, barrier)
+        launches = (og.launch_count() - l0) // (K + W) * K
+        ms_plain = timed(torch, lambda: plain_asm_prop(src, dst, **kw), K, W, flush, stream, barrier)
+    clocks = clk.summary()
+    t_step = max_over_ranks(statistics.mean(ms))
+    hsrc = torch.from_numpy(u0).pin_memory()
+    hdst = torch.empty_like(hsrc).pin_memory()
+
+    def step_e2e():
+        src.copy_(hsrc, non_blocking=True)
+        step()
+        hdst.copy_(dst, non_blocking=True)
+
+    ms_e = timed(torch, step_e2e, K, W, flush, stream, barrier)
+    plan = og.PropPlan("asm", ny, nx, **kw)
+    houts = [torch.empty_like(hsrc).pin_memory() for _ in range(max(K, W, 3))]
+    ms_seq = timed_sequence(torch, lambda k: plan.execute_host([hsrc] * k, houts[:k], stream=stream), K, W, flush,
+                            stream, barrier)
+    step()
+    torch.cuda.synchronize()
+    seq_equal = bool(torch.equal(houts[K - 1], dst.cpu()))
+    plan.close()
+    forms_e2e = {"per_step_copies": statistics.mean(ms_e)}
+    if seq_equal:
+        forms_e2e["pipelined_sequence"] = ms_seq
+    e2e_form = min(forms_e2e, key=forms_e2e.get)
+    t_e2e = max_over_ranks(forms_e2e[e2e_form])
+    n = ny * nx
+    b_alg = 80 * n
+    ach = b_alg / (statistics.mean(ms) * 1e-3) / 1e9
+    out = {
+        "metric": "mixed-radix ASM props/s", "value": ws / (t_step * 1e-3), "unit": "props/s", "ms_per_step": t_step,
+        "dtype": "f32",
+        "config": {"workload": UHD_DESC, "l2": "inputs larger than L2 (S: %.0f MB), flushed between steps"
+                   % (ny * 2 * nx * 8 / 1e6)},
+        "e2e": {"value": ws / (t_e2e * 1e-3), "unit": "props/s", "h2d_bytes_per_step": u0.nbytes,
+                "d2h_bytes_per_step": u0.nbytes, "form": e2e_form},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": ach / pk["hbm_gbs"], "traffic": None,
+                     "note": f"80 n bytes per propagation (n = 3840 x 2160) over the 3-pass propagation time; "
+                             f"peak {pk_kind}"},
+        "forms": {"fused_mixed_radix": {"props/s": 1e3 / statistics.mean(ms), "ms": statistics.mean(ms)},
+                  "plain_cufft": {"props/s": 1e3 / statistics.mean(ms_plain), "ms": statistics.mean(ms_plain)},
+                  "e2e_per_step_copies": {"props/s": 1e3 / statistics.mean(ms_e), "ms": statistics.mean(ms_e)},
+                  "e2e_pipelined_sequence": {"props/s": 1e3 / ms_seq, "ms": ms_seq, "steps": K,
+                                             "equal_to_device_run": seq_equal}},
+        "clocks": clocks,
+    }
+    v, ref = cpu_uhd_sample()
+    out["accuracy"] = dict(accuracy(dst.cpu().numpy(), ref), against="FP64 oracle, the whole 3840 x 2160 field")
+    if rank == 0 and ws == 1 and cpu:
+        out["cpu_baseline"] = {"value": v, "unit": "props/s", "cores": cpu_threads(), "kind": "port",
+                               "sample": "one full 3840x2160 -> 7680x4320 FP64 ASM propagation"}
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -1167,7 +1271,8 @@ def run_ours(args):
     return 0
 
 
-WORKLOADS = {"cgh": wl_cgh, "asm": wl_asm, "wrp": wl_wrp, "adam": wl_adam, "batch": wl_batch, "tilt": wl_tilt}
+WORKLOADS = {"cgh": wl_cgh, "asm": wl_asm, "wrp": wl_wrp, "adam": wl_adam, "batch": wl_batch, "tilt": wl_tilt,
+             "uhd": wl_uhd}
 
 
 def main():
@@ -1176,7 +1281,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cgh", choices=["cgh", "asm", "wrp", "adam", "batch", "tilt"])
+    ap.add_argument("--workload", default="cgh", choices=["cgh", "asm", "wrp", "adam", "batch", "tilt", "uhd"])
     ap.add_argument("--cpu-rows", type=int, default=48)
     ap.add_argument("--ref-rows", type=int, default=24)
     ap.add_argument("--no-cpu", action="store_true")

@@ -136,4 +136,90 @@ __device__ __forceinline__ void mr_fft(float2 *s, int ss, int nseq, const MrPlan
     }
 }
 
+// ------------------------------------------------- compile-time stage plans
+// The same transform for a few lengths with the plan, the sequence count and
+// the thread count known at compile time: the reference's default field
+// (3840 x 2160, padded 7680 x 4320) and its half (1920 x 1080, padded 3840 x
+// 2160).  The index arithmetic (divisions by B, NS and the sequence count)
+// then folds into multiplications and shifts, and each thread's values stay
+// in registers; the stages, their order and their arithmetic are those of
+// mr_stage, so the results are the run-time plan's bit for bit.
+template <int... Rs>
+struct MrRadices {};
+template <int N>
+struct MrFixedPlan {
+    static constexpr bool ok = false;
+};
+// in mr_plan's order: 16s, then 8, 4, 2, then 5s, then 3s
+template <> struct MrFixedPlan<7680> { static constexpr bool ok = true; using type = MrRadices<16, 16, 2, 5, 3>; };
+template <> struct MrFixedPlan<4320> { static constexpr bool ok = true; using type = MrRadices<16, 2, 5, 3, 3, 3>; };
+template <> struct MrFixedPlan<3840> { static constexpr bool ok = true; using type = MrRadices<16, 16, 5, 3>; };
+template <> struct MrFixedPlan<2160> { static constexpr bool ok = true; using type = MrRadices<16, 5, 3, 3, 3>; };
+
+template <int N, int R, int NS, int DIR, int NT, bool COLS, int NSEQ>
+__device__ __forceinline__ void mrc_stage(float2 *s, int ss, const float2 *__restrict__ tw, int tid)
+{
+    constexpr int B = N / R, BT = NSEQ * B, L = NS * R, step = N / L;
+    constexpr int BPT = (BT + NT - 1) / NT;
+    float2 v[BPT][R];
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT;
+        if (BT % NT != 0 && b >= BT) continue;
+        const int q = COLS ? b % NSEQ : b / B;
+        const int j = COLS ? b / NSEQ : b % B;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int i = j + r * B;
+            v[t][r] = s[COLS ? pidx(i) * NSEQ + q : q * ss + pidx(i)];
+        }
+        if constexpr (NS > 1) {
+            const int k = j % NS;
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[t][r] = cmul(v[t][r], mr_twid<DIR>(tw, r * k * step));
+        }
+        mr_dft<R, DIR>(v[t]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT;
+        if (BT % NT != 0 && b >= BT) continue;
+        const int q = COLS ? b % NSEQ : b / B;
+        const int j = COLS ? b / NSEQ : b % B;
+        const int k = j % NS, base = (j / NS) * L + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int i = base + r * NS;
+            s[COLS ? pidx(i) * NSEQ + q : q * ss + pidx(i)] = v[t][outpos<R>(r)];
+        }
+    }
+    __syncthreads();
+}
+
+template <int N, int NS, int DIR, int NT, bool COLS, int NSEQ, int... Rs>
+struct MrcRun {
+    static __device__ __forceinline__ void run(float2 *, int, const float2 *__restrict__, int) {}
+};
+template <int N, int NS, int DIR, int NT, bool COLS, int NSEQ, int R, int... Rest>
+struct MrcRun<N, NS, DIR, NT, COLS, NSEQ, R, Rest...> {
+    static __device__ __forceinline__ void run(float2 *s, int ss, const float2 *__restrict__ tw, int tid)
+    {
+        mrc_stage<N, R, NS, DIR, NT, COLS, NSEQ>(s, ss, tw, tid);
+        MrcRun<N, NS * R, DIR, NT, COLS, NSEQ, Rest...>::run(s, ss, tw, tid);
+    }
+};
+template <int N, int DIR, int NT, bool COLS, int NSEQ, int... Rs>
+__device__ __forceinline__ void mrc_fft_plan(MrRadices<Rs...>, float2 *s, int ss, const float2 *__restrict__ tw,
+                                             int tid)
+{
+    MrcRun<N, 1, DIR, NT, COLS, NSEQ, Rs...>::run(s, ss, tw, tid);
+}
+// The whole transform of NSEQ sequences of length N in place (unnormalised).
+template <int N, int DIR, int NT, bool COLS, int NSEQ>
+__device__ __forceinline__ void mrc_fft(float2 *s, int ss, const float2 *__restrict__ tw, int tid)
+{
+    mrc_fft_plan<N, DIR, NT, COLS, NSEQ>(typename MrFixedPlan<N>::type{}, s, ss, tw, tid);
+}
+
 } // namespace olg

@@ -91,6 +91,81 @@ __global__ void __launch_bounds__(MR_NT, 1) k_rows_inv_mr(PropParams P)
     if (P.post_mode == OP_SEED) loss_reduce(lsum, P.loss, tid, MR_NT);
 }
 
+// The three passes again for the lengths with a compile-time plan (fftmr.cuh
+// MrFixedPlan): NSEQ rows or columns per CTA of NT threads, as many as keep
+// every thread within 16 values per stage (64 registers at 1024 threads).
+template <int N, int NT, int NSEQ>
+__global__ void __launch_bounds__(NT, 1) k_rows_fwd_mrc(PropParams P)
+{
+    pdl_enter();
+    extern __shared__ float2 sm[];
+    constexpr int SS = padded_len(N);
+    const int tid = threadIdx.x, r0 = blockIdx.x * NSEQ, off = (N - P.nx) / 2;
+    for (int e = tid; e < NSEQ * N; e += NT) {
+        const int q = e / N, i = e % N, h = r0 + q, w = i - off;
+        float2 v = make_float2(0.f, 0.f);
+        if (h < P.ny && w >= 0 && w < P.nx) v = load_in(P, h, w);
+        sm[q * SS + pidx(i)] = v;
+    }
+    __syncthreads();
+    mrc_fft<N, -1, NT, false, NSEQ>(sm, SS, P.twx, tid);
+    for (int e = tid; e < NSEQ * N; e += NT) {
+        const int q = e / N, i = e % N, h = r0 + q;
+        if (h < P.ny) __stcg(P.S + (size_t)h * N + i, sm[q * SS + pidx(i)]);
+    }
+}
+
+template <int N, int NT, int C>
+__global__ void __launch_bounds__(NT, 1) k_cols_mrc(PropParams P)
+{
+    pdl_enter();
+    extern __shared__ float2 sm[];
+    const int NX = P.NX, tid = threadIdx.x;
+    const int c0 = blockIdx.x * C, off = (N - P.ny) / 2;
+    for (int e = tid; e < N * C; e += NT) {
+        const int i = e / C, c = e % C, kx = c0 + c, h = i - off;
+        float2 v = make_float2(0.f, 0.f);
+        if (kx < NX && h >= 0 && h < P.ny) v = __ldcg(P.S + (size_t)h * NX + kx);
+        sm[pidx(i) * C + c] = v;
+    }
+    __syncthreads();
+    mrc_fft<N, -1, NT, true, C>(sm, 0, P.twy, tid);
+    for (int e = tid; e < N * C; e += NT) {
+        const int ky = e / C, c = e % C, kx = c0 + c;
+        if (kx < NX) {
+            float2 &x = sm[pidx(ky) * C + c];
+            x = cmul(x, tf_at(P, ky, kx, N));
+        }
+    }
+    __syncthreads();
+    mrc_fft<N, +1, NT, true, C>(sm, 0, P.twy, tid);
+    for (int e = tid; e < P.ny * C; e += NT) {
+        const int h = e / C, c = e % C, kx = c0 + c;
+        if (kx < NX) __stcg(P.S + (size_t)h * NX + kx, sm[pidx(h + off) * C + c]);
+    }
+}
+
+template <int N, int NT, int NSEQ>
+__global__ void __launch_bounds__(NT, 1) k_rows_inv_mrc(PropParams P)
+{
+    pdl_enter();
+    extern __shared__ float2 sm[];
+    constexpr int SS = padded_len(N);
+    const int tid = threadIdx.x, r0 = blockIdx.x * NSEQ, off = (N - P.nx) / 2;
+    for (int e = tid; e < NSEQ * N; e += NT) {
+        const int q = e / N, i = e % N, h = r0 + q;
+        sm[q * SS + pidx(i)] = h < P.ny ? __ldcg(P.S + (size_t)h * N + i) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    mrc_fft<N, +1, NT, false, NSEQ>(sm, SS, P.twx, tid);
+    float lsum = 0.f;
+    for (int e = tid; e < NSEQ * P.nx; e += NT) {
+        const int q = e / P.nx, w = e % P.nx, h = r0 + q;
+        if (h < P.ny) store_out(P, h, w, sm[q * SS + pidx(w + off)], lsum);
+    }
+    if (P.post_mode == OP_SEED) loss_reduce(lsum, P.loss, tid, NT);
+}
+
 // Chirp spectrum of one axis (blockIdx.x == 0) and its elementwise tables
 // (blockIdx.x == 1); as the power-of-two chirp kernel in prop.cu.
 __global__ void __launch_bounds__(MR_NT, 1) k_chirp_mr(ChirpAxis A, MrPlan pl, const float2 *tw)
@@ -411,8 +486,51 @@ int mr_prepare(PropParams &P)
     return OLG_OK;
 }
 
+// Launch shapes of the compile-time plans: {N, threads, rows or columns per CTA}.
+template <int N, int NT, int NSEQ, typename K>
+int mrc_launch(K kern, int count, cudaStream_t st, const PropParams &P, const char *what)
+{
+    const int smem = NSEQ * padded_len(N) * (int)sizeof(float2);
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((count + NSEQ - 1) / NSEQ);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, P);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    count_launch();
+    return check_launch(what);
+}
+
+template <int N, int NT, int NSEQ>
+int mrc_rows(const PropParams &P, bool inverse, cudaStream_t st)
+{
+    return inverse ? mrc_launch<N, NT, NSEQ>(k_rows_inv_mrc<N, NT, NSEQ>, P.ny, st, P, "k_rows_inv_mrc")
+                   : mrc_launch<N, NT, NSEQ>(k_rows_fwd_mrc<N, NT, NSEQ>, P.ny, st, P, "k_rows_fwd_mrc");
+}
+
+template <int N, int NT, int C>
+int mrc_cols(const PropParams &P, cudaStream_t st)
+{
+    return mrc_launch<N, NT, C>(k_cols_mrc<N, NT, C>, P.NX, st, P, "k_cols_mrc");
+}
+
 int mr_rows_pass(const PropParams &P, bool inverse, cudaStream_t st)
 {
+    switch (P.NX) {
+    case 7680: return mrc_rows<7680, 1024, 2>(P, inverse, st);
+    case 3840: return mrc_rows<3840, 1024, 4>(P, inverse, st);
+    default: break;
+    }
     const int grid = (P.ny + P.mr_rows - 1) / P.mr_rows;
     const int smem = P.mr_rows * padded_len(P.NX) * (int)sizeof(float2);
     return inverse ? mr_launch(k_rows_inv_mr, grid, smem, st, P, "k_rows_inv_mr")
@@ -421,6 +539,11 @@ int mr_rows_pass(const PropParams &P, bool inverse, cudaStream_t st)
 
 int mr_cols_pass(const PropParams &P, cudaStream_t st)
 {
+    switch (P.NY) {
+    case 4320: return mrc_cols<4320, 1024, 2>(P, st);
+    case 2160: return mrc_cols<2160, 1024, 4>(P, st);
+    default: break;
+    }
     const int grid = (P.NX + P.mr_cols - 1) / P.mr_cols;
     const int smem = P.mr_cols * padded_len(P.NY) * (int)sizeof(float2);
     return mr_launch(k_cols_mr, grid, smem, st, P, "k_cols_mr");

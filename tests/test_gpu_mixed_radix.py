@@ -50,6 +50,32 @@ def test_asm_mixed_sizes(shape):
     assert rel_l2(host(out), ref) < TOL
 
 
+def test_asm_reference_default_field():
+    """The reference's default test field (tests/para.h: 3840 x 2160, p = 3.74 um,
+    532 nm, d = -0.1 m): padded 7680 x 4320, the compile-time mixed-radix plans."""
+    shape = (2160, 3840)
+    u = field(np.random.default_rng(7), shape)
+    ref = O.asm_prop(u.astype(np.complex128), 3.74e-6, 3.74e-6, 532e-9, -0.1)
+    out = og.asm_prop(dev(u), torch.empty(shape, dtype=torch.complex64, device="cuda"), dy=3.74e-6, dx=3.74e-6,
+                      lam=532e-9, z=-0.1)
+    assert rel_l2(host(out), ref) < TOL
+
+
+@pytest.mark.parametrize("kind", ["fresnel", "arss"])
+def test_chirp_methods_at_1920x1080(kind):
+    """Fresnel and ARSS (chirp spectra in the column pass) at 1920 x 1080."""
+    shape = (1080, 1920)
+    u = field(np.random.default_rng(11), shape)
+    uc = u.astype(np.complex128)
+    if kind == "fresnel":
+        ref = O.fresnel_prop(uc, 8e-6, 8e-6, 532e-9, 0.2)
+        out = og.fresnel_prop(dev(u), dy=8e-6, dx=8e-6, lam=532e-9, z=0.2)
+    else:
+        ref = O.arss_prop(uc, 8e-6, 8e-6, 532e-9, 0.2, 0.5, 1e-4, -2e-4)
+        out = og.arss_prop(dev(u), dy=8e-6, dx=8e-6, lam=532e-9, z=0.2, s=0.5, oy=1e-4, ox=-2e-4)
+    assert rel_l2(host(out), ref) < TOL
+
+
 @pytest.mark.parametrize("shape", [(240, 320), (200, 256)])
 def test_fresnel_and_arss_mixed_sizes(shape):
     u = field(np.random.default_rng(3), shape)
