@@ -10,6 +10,7 @@
 // (q * ss + pidx(i)) or column tiles (pidx(i) * nseq + q).
 #pragma once
 #include "fft.cuh"
+#include "fft2.cuh"
 #include "propdev.cuh"
 
 namespace olg {
@@ -146,18 +147,45 @@ __device__ __forceinline__ void mr_fft(float2 *s, int ss, int nseq, const MrPlan
 // mr_stage, so the results are the run-time plan's bit for bit.
 template <int... Rs>
 struct MrRadices {};
+// `full`: the whole plan, in mr_plan's order.  Forward: radix 16 first
+// (zero-pruned, from global memory), then `fwd`.  Inverse, row form: `inv`
+// (the same radices in reverse order), then radix 16 last (crop-pruned, to
+// global memory).  Listed here for the lengths it serves.
 template <int N>
 struct MrFixedPlan {
     static constexpr bool ok = false;
 };
-// in mr_plan's order: 16s, then 8, 4, 2, then 5s, then 3s
-template <> struct MrFixedPlan<7680> { static constexpr bool ok = true; using type = MrRadices<16, 16, 2, 5, 3>; };
-template <> struct MrFixedPlan<4320> { static constexpr bool ok = true; using type = MrRadices<16, 2, 5, 3, 3, 3>; };
-template <> struct MrFixedPlan<3840> { static constexpr bool ok = true; using type = MrRadices<16, 16, 5, 3>; };
-template <> struct MrFixedPlan<2160> { static constexpr bool ok = true; using type = MrRadices<16, 5, 3, 3, 3>; };
+template <> struct MrFixedPlan<7680> {
+    static constexpr bool ok = true;
+    using full = MrRadices<16, 16, 2, 5, 3>;
+    using fwd = MrRadices<16, 2, 5, 3>;
+    using inv = MrRadices<3, 5, 2, 16>;
+};
+template <> struct MrFixedPlan<4320> {
+    static constexpr bool ok = true;
+    using full = MrRadices<16, 2, 5, 3, 3, 3>;
+    using fwd = MrRadices<2, 5, 3, 3, 3>;
+    using inv = MrRadices<3, 3, 3, 5, 2>;
+};
+template <> struct MrFixedPlan<3840> {
+    static constexpr bool ok = true;
+    using full = MrRadices<16, 16, 5, 3>;
+    using fwd = MrRadices<16, 5, 3>;
+    using inv = MrRadices<3, 5, 16>;
+};
+template <> struct MrFixedPlan<2160> {
+    static constexpr bool ok = true;
+    using full = MrRadices<16, 5, 3, 3, 3>;
+    using fwd = MrRadices<5, 3, 3, 3>;
+    using inv = MrRadices<3, 3, 3, 5>;
+};
 
-template <int N, int R, int NS, int DIR, int NT, bool COLS, int NSEQ>
-__device__ __forceinline__ void mrc_stage(float2 *s, int ss, const float2 *__restrict__ tw, int tid)
+// One in-place Stockham stage (as mr_stage) with compile-time sizes.  TFE:
+// the stage is the forward transform's last and multiplies each output, a
+// final frequency ky, by the transfer function of its column as it stores.
+template <int N, int R, int NS, int DIR, int NT, bool COLS, int NSEQ, bool TFE>
+__device__ __forceinline__ void mrc_stage(float2 *s, int ss, const float2 *__restrict__ tw, int tid,
+                                          const PropParams *P, int c0)
 {
     constexpr int B = N / R, BT = NSEQ * B, L = NS * R, step = N / L;
     constexpr int BPT = (BT + NT - 1) / NT;
@@ -175,8 +203,12 @@ __device__ __forceinline__ void mrc_stage(float2 *s, int ss, const float2 *__res
         }
         if constexpr (NS > 1) {
             const int k = j % NS;
+            if constexpr (R == 2 || R == 4 || R == 8 || R == 16) {
+                twiddle_powers<R, DIR>(v[t], tw, k * step); // w^r from log2(R) table loads
+            } else {
 #pragma unroll
-            for (int r = 1; r < R; ++r) v[t][r] = cmul(v[t][r], mr_twid<DIR>(tw, r * k * step));
+                for (int r = 1; r < R; ++r) v[t][r] = cmul(v[t][r], mr_twid<DIR>(tw, r * k * step));
+            }
         }
         mr_dft<R, DIR>(v[t]);
     }
@@ -191,35 +223,39 @@ __device__ __forceinline__ void mrc_stage(float2 *s, int ss, const float2 *__res
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int i = base + r * NS;
-            s[COLS ? pidx(i) * NSEQ + q : q * ss + pidx(i)] = v[t][outpos<R>(r)];
+            float2 x = v[t][outpos<R>(r)];
+            if constexpr (TFE) {
+                const int kx = c0 + q;
+                if (kx < P->NX) x = cmul(x, tf_at(*P, i, kx, N));
+            }
+            s[COLS ? pidx(i) * NSEQ + q : q * ss + pidx(i)] = x;
         }
     }
     __syncthreads();
 }
 
-template <int N, int NS, int DIR, int NT, bool COLS, int NSEQ, int... Rs>
+template <int N, int NS, int DIR, int NT, bool COLS, int NSEQ, bool TFE, int... Rs>
 struct MrcRun {
-    static __device__ __forceinline__ void run(float2 *, int, const float2 *__restrict__, int) {}
-};
-template <int N, int NS, int DIR, int NT, bool COLS, int NSEQ, int R, int... Rest>
-struct MrcRun<N, NS, DIR, NT, COLS, NSEQ, R, Rest...> {
-    static __device__ __forceinline__ void run(float2 *s, int ss, const float2 *__restrict__ tw, int tid)
+    static __device__ __forceinline__ void run(float2 *, int, const float2 *__restrict__, int, const PropParams *,
+                                               int)
     {
-        mrc_stage<N, R, NS, DIR, NT, COLS, NSEQ>(s, ss, tw, tid);
-        MrcRun<N, NS * R, DIR, NT, COLS, NSEQ, Rest...>::run(s, ss, tw, tid);
     }
 };
-template <int N, int DIR, int NT, bool COLS, int NSEQ, int... Rs>
-__device__ __forceinline__ void mrc_fft_plan(MrRadices<Rs...>, float2 *s, int ss, const float2 *__restrict__ tw,
-                                             int tid)
+template <int N, int NS, int DIR, int NT, bool COLS, int NSEQ, bool TFE, int R, int... Rest>
+struct MrcRun<N, NS, DIR, NT, COLS, NSEQ, TFE, R, Rest...> {
+    static __device__ __forceinline__ void run(float2 *s, int ss, const float2 *__restrict__ tw, int tid,
+                                               const PropParams *P, int c0)
+    {
+        mrc_stage<N, R, NS, DIR, NT, COLS, NSEQ, TFE && sizeof...(Rest) == 0>(s, ss, tw, tid, P, c0);
+        MrcRun<N, NS * R, DIR, NT, COLS, NSEQ, TFE, Rest...>::run(s, ss, tw, tid, P, c0);
+    }
+};
+// Stages Rs... from NS0 on (all NT threads, after a barrier).
+template <int N, int NS0, int DIR, int NT, bool COLS, int NSEQ, bool TFE, int... Rs>
+__device__ __forceinline__ void mrc_stages(MrRadices<Rs...>, float2 *s, int ss, const float2 *__restrict__ tw,
+                                           int tid, const PropParams *P = nullptr, int c0 = 0)
 {
-    MrcRun<N, 1, DIR, NT, COLS, NSEQ, Rs...>::run(s, ss, tw, tid);
-}
-// The whole transform of NSEQ sequences of length N in place (unnormalised).
-template <int N, int DIR, int NT, bool COLS, int NSEQ>
-__device__ __forceinline__ void mrc_fft(float2 *s, int ss, const float2 *__restrict__ tw, int tid)
-{
-    mrc_fft_plan<N, DIR, NT, COLS, NSEQ>(typename MrFixedPlan<N>::type{}, s, ss, tw, tid);
+    MrcRun<N, NS0, DIR, NT, COLS, NSEQ, TFE, Rs...>::run(s, ss, tw, tid, P, c0);
 }
 
 } // namespace olg

@@ -92,23 +92,34 @@ __global__ void __launch_bounds__(MR_NT, 1) k_rows_inv_mr(PropParams P)
 }
 
 // The three passes again for the lengths with a compile-time plan (fftmr.cuh
-// MrFixedPlan): NSEQ rows or columns per CTA of NT threads, as many as keep
-// every thread within 16 values per stage (64 registers at 1024 threads).
+// MrFixedPlan), NSEQ rows or columns per CTA of NT threads.  As in the tuned
+// power-of-two passes, the forward transforms start with a radix-16 stage
+// that reads the stored half of the padded input straight from global memory
+// (the padding is never formed), the column pass multiplies by the transfer
+// function as its last forward stage stores, and the inverse transforms end
+// with a radix-16 stage that forms only the central outputs and writes them
+// straight to global memory.
 template <int N, int NT, int NSEQ>
 __global__ void __launch_bounds__(NT, 1) k_rows_fwd_mrc(PropParams P)
 {
     pdl_enter();
     extern __shared__ float2 sm[];
-    constexpr int SS = padded_len(N);
-    const int tid = threadIdx.x, r0 = blockIdx.x * NSEQ, off = (N - P.nx) / 2;
-    for (int e = tid; e < NSEQ * N; e += NT) {
-        const int q = e / N, i = e % N, h = r0 + q, w = i - off;
-        float2 v = make_float2(0.f, 0.f);
-        if (h < P.ny && w >= 0 && w < P.nx) v = load_in(P, h, w);
-        sm[q * SS + pidx(i)] = v;
+    constexpr int SS = padded_len(N), B = N / 16, BT = NSEQ * B, BPT = (BT + NT - 1) / NT;
+    const int tid = threadIdx.x, r0 = blockIdx.x * NSEQ;
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT;
+        if (BT % NT != 0 && b >= BT) continue;
+        const int q = b / B, j = b % B, h = r0 + q;
+        float2 v[16];
+#pragma unroll
+        for (int r = 4; r < 12; ++r) v[r] = h < P.ny ? load_in(P, h, j + (r - 4) * B) : make_float2(0.f, 0.f);
+        dft16_in_mid<-1>(v);
+#pragma unroll
+        for (int r = 0; r < 16; ++r) sm[q * SS + pidx(16 * j + r)] = v[outpos<16>(r)];
     }
     __syncthreads();
-    mrc_fft<N, -1, NT, false, NSEQ>(sm, SS, P.twx, tid);
+    mrc_stages<N, 16, -1, NT, false, NSEQ, false>(typename MrFixedPlan<N>::fwd{}, sm, SS, P.twx, tid);
     for (int e = tid; e < NSEQ * N; e += NT) {
         const int q = e / N, i = e % N, h = r0 + q;
         if (h < P.ny) __stcg(P.S + (size_t)h * N + i, sm[q * SS + pidx(i)]);
@@ -120,28 +131,30 @@ __global__ void __launch_bounds__(NT, 1) k_cols_mrc(PropParams P)
 {
     pdl_enter();
     extern __shared__ float2 sm[];
-    const int NX = P.NX, tid = threadIdx.x;
-    const int c0 = blockIdx.x * C, off = (N - P.ny) / 2;
-    for (int e = tid; e < N * C; e += NT) {
-        const int i = e / C, c = e % C, kx = c0 + c, h = i - off;
-        float2 v = make_float2(0.f, 0.f);
-        if (kx < NX && h >= 0 && h < P.ny) v = __ldcg(P.S + (size_t)h * NX + kx);
-        sm[pidx(i) * C + c] = v;
+    constexpr int B = N / 16, BT = C * B, BPT = (BT + NT - 1) / NT;
+    const int NX = P.NX, tid = threadIdx.x, c0 = blockIdx.x * C;
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT;
+        if (BT % NT != 0 && b >= BT) continue;
+        const int c = b % C, j = b / C, kx = c0 + c;
+        float2 v[16];
+#pragma unroll
+        for (int r = 4; r < 12; ++r)
+            v[r] = kx < NX ? __ldcg(P.S + (size_t)(j + (r - 4) * B) * NX + kx) : make_float2(0.f, 0.f);
+        dft16_in_mid<-1>(v);
+#pragma unroll
+        for (int r = 0; r < 16; ++r) sm[pidx(16 * j + r) * C + c] = v[outpos<16>(r)];
     }
     __syncthreads();
-    mrc_fft<N, -1, NT, true, C>(sm, 0, P.twy, tid);
-    for (int e = tid; e < N * C; e += NT) {
-        const int ky = e / C, c = e % C, kx = c0 + c;
-        if (kx < NX) {
-            float2 &x = sm[pidx(ky) * C + c];
-            x = cmul(x, tf_at(P, ky, kx, N));
-        }
-    }
-    __syncthreads();
-    mrc_fft<N, +1, NT, true, C>(sm, 0, P.twy, tid);
-    for (int e = tid; e < P.ny * C; e += NT) {
+    mrc_stages<N, 16, -1, NT, true, C, true>(typename MrFixedPlan<N>::fwd{}, sm, 0, P.twy, tid, &P, c0);
+    // inverse: the whole plan in shared memory (its radix-16 stage first, with
+    // no twiddles), then the central rows back to S
+    mrc_stages<N, 1, +1, NT, true, C, false>(typename MrFixedPlan<N>::full{}, sm, 0, P.twy, tid);
+    constexpr int OFF = N / 4;
+    for (int e = tid; e < (N / 2) * C; e += NT) {
         const int h = e / C, c = e % C, kx = c0 + c;
-        if (kx < NX) __stcg(P.S + (size_t)h * NX + kx, sm[pidx(h + off) * C + c]);
+        if (kx < NX) __stcg(P.S + (size_t)h * NX + kx, sm[pidx(h + OFF) * C + c]);
     }
 }
 
@@ -150,18 +163,30 @@ __global__ void __launch_bounds__(NT, 1) k_rows_inv_mrc(PropParams P)
 {
     pdl_enter();
     extern __shared__ float2 sm[];
-    constexpr int SS = padded_len(N);
-    const int tid = threadIdx.x, r0 = blockIdx.x * NSEQ, off = (N - P.nx) / 2;
+    constexpr int SS = padded_len(N), B = N / 16, BT = NSEQ * B, BPT = (BT + NT - 1) / NT;
+    const int tid = threadIdx.x, r0 = blockIdx.x * NSEQ;
     for (int e = tid; e < NSEQ * N; e += NT) {
         const int q = e / N, i = e % N, h = r0 + q;
         sm[q * SS + pidx(i)] = h < P.ny ? __ldcg(P.S + (size_t)h * N + i) : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    mrc_fft<N, +1, NT, false, NSEQ>(sm, SS, P.twx, tid);
+    mrc_stages<N, 1, +1, NT, false, NSEQ, false>(typename MrFixedPlan<N>::inv{}, sm, SS, P.twx, tid);
     float lsum = 0.f;
-    for (int e = tid; e < NSEQ * P.nx; e += NT) {
-        const int q = e / P.nx, w = e % P.nx, h = r0 + q;
-        if (h < P.ny) store_out(P, h, w, sm[q * SS + pidx(w + off)], lsum);
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT;
+        if (BT % NT != 0 && b >= BT) continue;
+        const int q = b / B, j = b % B, h = r0 + q;
+        float2 v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = sm[q * SS + pidx(j + r * B)];
+#pragma unroll
+        twiddle_powers<16, +1>(v, P.twx, j);
+        dft16_out_mid<+1>(v);
+        if (h < P.ny) {
+#pragma unroll
+            for (int k = 4; k < 12; ++k) store_out(P, h, j + (k - 4) * B, v[outpos<16>(k)], lsum);
+        }
     }
     if (P.post_mode == OP_SEED) loss_reduce(lsum, P.loss, tid, NT);
 }
