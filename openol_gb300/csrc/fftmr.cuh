@@ -147,10 +147,10 @@ __device__ __forceinline__ void mr_fft(float2 *s, int ss, int nseq, const MrPlan
 // mr_stage, so the results are the run-time plan's bit for bit.
 template <int... Rs>
 struct MrRadices {};
-// `full`: the whole plan, in mr_plan's order.  Forward: radix 16 first
-// (zero-pruned, from global memory), then `fwd`.  Inverse, row form: `inv`
-// (the same radices in reverse order), then radix 16 last (crop-pruned, to
-// global memory).  Listed here for the lengths it serves.
+// `full`: the whole plan, in mr_plan's order (the inverse transforms run it
+// in shared memory).  `fwd`: the plan after its leading radix 16, which the
+// forward transforms apply zero-pruned, straight from global memory.  Listed
+// for the lengths it serves.
 template <int N>
 struct MrFixedPlan {
     static constexpr bool ok = false;
@@ -159,25 +159,21 @@ template <> struct MrFixedPlan<7680> {
     static constexpr bool ok = true;
     using full = MrRadices<16, 16, 2, 5, 3>;
     using fwd = MrRadices<16, 2, 5, 3>;
-    using inv = MrRadices<3, 5, 2, 16>;
 };
 template <> struct MrFixedPlan<4320> {
     static constexpr bool ok = true;
     using full = MrRadices<16, 2, 5, 3, 3, 3>;
     using fwd = MrRadices<2, 5, 3, 3, 3>;
-    using inv = MrRadices<3, 3, 3, 5, 2>;
 };
 template <> struct MrFixedPlan<3840> {
     static constexpr bool ok = true;
     using full = MrRadices<16, 16, 5, 3>;
     using fwd = MrRadices<16, 5, 3>;
-    using inv = MrRadices<3, 5, 16>;
 };
 template <> struct MrFixedPlan<2160> {
     static constexpr bool ok = true;
     using full = MrRadices<16, 5, 3, 3, 3>;
     using fwd = MrRadices<5, 3, 3, 3>;
-    using inv = MrRadices<3, 3, 3, 5>;
 };
 
 // One in-place Stockham stage (as mr_stage) with compile-time sizes.  TFE:
