@@ -74,6 +74,8 @@ TRAFFIC = {
     "asm": ((8.5 + 16.9 + 16.8) * 1e6, "the three passes, profiles/asm_1024_kernels.md (S stays in L2)"),
     "wrp": ((134.4 + 205.0 + 268.5 + 211.6 + 268.5 + 99.1) * 1e6,
             "the three 8192-point passes of step 2, profiles/asm_4096_to_8192_wrp_step2.md"),
+    "uhd": ((66.5 + 70.8 + 132.8 + 84.4 + 132.8 + 33.4) * 1e6,
+            "the three mixed-radix passes, profiles/asm_3840x2160_mixed_radix.md"),
     "adam": (4656.1e6, "every kernel of one step, the bench's L2 flush excluded (S and the spectra partly stay in "
                        "L2), profiles/phase_grad_2048_8planes.md"),
 }
@@ -1189,7 +1191,7 @@ def wl_uhd(x, K, W, cpu):
                 "d2h_bytes_per_step": u0.nbytes, "form": e2e_form},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": ach / pk["hbm_gbs"], "traffic": None,
+                     "frac": ach / pk["hbm_gbs"], "traffic": traffic("uhd")[0], "traffic_source": traffic("uhd")[1],
                      "note": f"80 n bytes per propagation (n = 3840 x 2160) over the 3-pass propagation time; "
                              f"peak {pk_kind}"},
         "forms": {"fused_mixed_radix": {"props/s": 1e3 / statistics.mean(ms), "ms": statistics.mean(ms)},
