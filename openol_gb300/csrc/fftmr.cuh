@@ -51,11 +51,103 @@ __device__ __forceinline__ void dft5(float2 (&v)[5])
     v[3] = csub(r2, i2);
 }
 
+// exp(DIR 2 pi i p / n) from (cos, sin) of 2 pi p / n
+template <int DIR>
+__device__ __forceinline__ float2 mr_w(float c, float s)
+{
+    return make_float2(c, DIR < 0 ? -s : s);
+}
+
+// Composite radices of the compile-time plans, Cooley-Tukey over a radix-3 or
+// radix-2 outer split with the inner DFTs in registers; natural output order.
+// DFT6: n = 2m + e, X[k] = A[k mod 3] + w6^k B[k mod 3] (A, B the DFT3s of the
+// even and odd samples; w6^(k+3) = -w6^k).
+template <int DIR>
+__device__ __forceinline__ void dft6(float2 (&v)[6])
+{
+    float2 a[3] = {v[0], v[2], v[4]}, b[3] = {v[1], v[3], v[5]};
+    dft3<DIR>(a);
+    dft3<DIR>(b);
+    const float2 b1 = cmul(b[1], mr_w<DIR>(0.5f, 0.86602540378443865f));
+    const float2 b2 = cmul(b[2], mr_w<DIR>(-0.5f, 0.86602540378443865f));
+    v[0] = cadd(a[0], b[0]);
+    v[3] = csub(a[0], b[0]);
+    v[1] = cadd(a[1], b1);
+    v[4] = csub(a[1], b1);
+    v[2] = cadd(a[2], b2);
+    v[5] = csub(a[2], b2);
+}
+
+// DFT9: n = 3m + e, X[k + 3j] = DFT3 over e of w9^(e k) Y_e[k], Y_e the DFT3
+// of samples e, e + 3, e + 6.
+template <int DIR>
+__device__ __forceinline__ void dft9(float2 (&v)[9])
+{
+    float2 y[3][3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        float2 t[3] = {v[e], v[e + 3], v[e + 6]};
+        dft3<DIR>(t);
+        y[e][0] = t[0];
+        y[e][1] = t[1];
+        y[e][2] = t[2];
+    }
+    const float2 w1 = mr_w<DIR>(0.76604444311897804f, 0.64278760968653933f);  // w9
+    const float2 w2 = mr_w<DIR>(0.17364817766693035f, 0.98480775301220806f);  // w9^2
+    const float2 w4 = mr_w<DIR>(-0.93969262078590838f, 0.34202014332566873f); // w9^4
+    y[1][1] = cmul(y[1][1], w1);
+    y[1][2] = cmul(y[1][2], w2);
+    y[2][1] = cmul(y[2][1], w2);
+    y[2][2] = cmul(y[2][2], w4);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float2 z[3] = {y[0][k], y[1][k], y[2][k]};
+        dft3<DIR>(z);
+        v[k] = z[0];
+        v[k + 3] = z[1];
+        v[k + 6] = z[2];
+    }
+}
+
+// DFT15: n = 3m + e, X[k + 5j] = DFT3 over e of w15^(e k) Y_e[k], Y_e the DFT5
+// of samples e, e + 3, ..., e + 12.
+template <int DIR>
+__device__ __forceinline__ void dft15(float2 (&v)[15])
+{
+    float2 y[3][5];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        float2 t[5] = {v[e], v[e + 3], v[e + 6], v[e + 9], v[e + 12]};
+        dft5<DIR>(t);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) y[e][k] = t[k];
+    }
+    y[1][1] = cmul(y[1][1], mr_w<DIR>(0.91354545764260087f, 0.40673664307580021f));  // w15
+    y[1][2] = cmul(y[1][2], mr_w<DIR>(0.66913060635885824f, 0.74314482547739424f));  // w15^2
+    y[1][3] = cmul(y[1][3], mr_w<DIR>(0.30901699437494742f, 0.95105651629515357f));  // w15^3
+    y[1][4] = cmul(y[1][4], mr_w<DIR>(-0.10452846326765347f, 0.99452189536827329f)); // w15^4
+    y[2][1] = cmul(y[2][1], mr_w<DIR>(0.66913060635885824f, 0.74314482547739424f));  // w15^2
+    y[2][2] = cmul(y[2][2], mr_w<DIR>(-0.10452846326765347f, 0.99452189536827329f)); // w15^4
+    y[2][3] = cmul(y[2][3], mr_w<DIR>(-0.80901699437494742f, 0.58778525229247313f)); // w15^6
+    y[2][4] = cmul(y[2][4], mr_w<DIR>(-0.97814760073380569f, -0.20791169081775934f)); // w15^8
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        float2 z[3] = {y[0][k], y[1][k], y[2][k]};
+        dft3<DIR>(z);
+        v[k] = z[0];
+        v[k + 5] = z[1];
+        v[k + 10] = z[2];
+    }
+}
+
 template <int R, int DIR>
 __device__ __forceinline__ void mr_dft(float2 (&v)[R])
 {
     if constexpr (R == 3) dft3<DIR>(v);
     else if constexpr (R == 5) dft5<DIR>(v);
+    else if constexpr (R == 6) dft6<DIR>(v);
+    else if constexpr (R == 9) dft9<DIR>(v);
+    else if constexpr (R == 15) dft15<DIR>(v);
     else dft<R, DIR>(v);
 }
 
@@ -147,33 +239,35 @@ __device__ __forceinline__ void mr_fft(float2 *s, int ss, int nseq, const MrPlan
 // mr_stage, so the results are the run-time plan's bit for bit.
 template <int... Rs>
 struct MrRadices {};
-// `full`: the whole plan, in mr_plan's order (the inverse transforms run it
-// in shared memory).  `fwd`: the plan after its leading radix 16, which the
-// forward transforms apply zero-pruned, straight from global memory.  Listed
-// for the lengths it serves.
+// `full`: the whole plan (the inverse transforms run it in shared memory),
+// radix 16 first and the composite radices 6, 9 and 15 in place of pairs of
+// 2, 3 and 5, so that 7680 takes four stages and 4320 four instead of six.
+// `fwd`: the plan after its leading radix 16, which the forward transforms
+// apply zero-pruned, straight from global memory.  Listed for the lengths it
+// serves; every stage keeps each thread within 16 values.
 template <int N>
 struct MrFixedPlan {
     static constexpr bool ok = false;
 };
 template <> struct MrFixedPlan<7680> {
     static constexpr bool ok = true;
-    using full = MrRadices<16, 16, 2, 5, 3>;
-    using fwd = MrRadices<16, 2, 5, 3>;
+    using full = MrRadices<16, 16, 15, 2>;
+    using fwd = MrRadices<16, 15, 2>;
 };
 template <> struct MrFixedPlan<4320> {
     static constexpr bool ok = true;
-    using full = MrRadices<16, 2, 5, 3, 3, 3>;
-    using fwd = MrRadices<2, 5, 3, 3, 3>;
+    using full = MrRadices<16, 6, 5, 9>;
+    using fwd = MrRadices<6, 5, 9>;
 };
 template <> struct MrFixedPlan<3840> {
     static constexpr bool ok = true;
-    using full = MrRadices<16, 16, 5, 3>;
-    using fwd = MrRadices<16, 5, 3>;
+    using full = MrRadices<16, 16, 15>;
+    using fwd = MrRadices<16, 15>;
 };
 template <> struct MrFixedPlan<2160> {
     static constexpr bool ok = true;
-    using full = MrRadices<16, 5, 3, 3, 3>;
-    using fwd = MrRadices<5, 3, 3, 3>;
+    using full = MrRadices<16, 15, 9>;
+    using fwd = MrRadices<15, 9>;
 };
 
 // One in-place Stockham stage (as mr_stage) with compile-time sizes.  TFE:
