@@ -74,7 +74,7 @@ TRAFFIC = {
     "asm": ((8.5 + 16.9 + 16.8) * 1e6, "the three passes, profiles/asm_1024_kernels.md (S stays in L2)"),
     "wrp": ((134.4 + 205.0 + 268.5 + 211.6 + 268.5 + 99.1) * 1e6,
             "the three 8192-point passes of step 2, profiles/asm_4096_to_8192_wrp_step2.md"),
-    "uhd": ((66.5 + 70.8 + 132.8 + 84.4 + 132.8 + 33.4) * 1e6,
+    "uhd": ((66.5 + 70.8 + 132.8 + 76.0 + 132.8 + 33.3) * 1e6,
             "the three mixed-radix passes, profiles/asm_3840x2160_mixed_radix.md"),
     "adam": (4656.1e6, "every kernel of one step, the bench's L2 flush excluded (S and the spectra partly stay in "
                        "L2), profiles/phase_grad_2048_8planes.md"),
