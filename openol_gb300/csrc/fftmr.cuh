@@ -340,6 +340,81 @@ struct MrcRun<N, NS, DIR, NT, COLS, NSEQ, TFE, R, Rest...> {
         MrcRun<N, NS * R, DIR, NT, COLS, NSEQ, TFE, Rest...>::run(s, ss, tw, tid, P, c0);
     }
 };
+// The same stage out of place, from `src` to `dst` (a second shared buffer):
+// each butterfly is read, transformed and written at once, and one barrier
+// ends the stage instead of two.
+template <int N, int R, int NS, int DIR, int NT, bool COLS, int NSEQ, bool TFE>
+__device__ __forceinline__ void mrc_stage_pp(const float2 *src, float2 *dst, int ss, const float2 *__restrict__ tw,
+                                             int tid, const PropParams *P, int c0)
+{
+    constexpr int B = N / R, BT = NSEQ * B, L = NS * R, step = N / L;
+    constexpr int BPT = (BT + NT - 1) / NT;
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int b = tid + t * NT;
+        if (BT % NT != 0 && b >= BT) continue;
+        const int q = COLS ? b % NSEQ : b / B;
+        const int j = COLS ? b / NSEQ : b % B;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int i = j + r * B;
+            v[r] = src[COLS ? pidx(i) * NSEQ + q : q * ss + pidx(i)];
+        }
+        const int k = j % NS;
+        if constexpr (NS > 1) {
+            if constexpr (R == 2 || R == 4 || R == 8 || R == 16) {
+                twiddle_powers<R, DIR>(v, tw, k * step);
+            } else {
+#pragma unroll
+                for (int r = 1; r < R; ++r) v[r] = cmul(v[r], mr_twid<DIR>(tw, r * k * step));
+            }
+        }
+        mr_dft<R, DIR>(v);
+        const int base = (j / NS) * L + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int i = base + r * NS;
+            float2 x = v[outpos<R>(r)];
+            if constexpr (TFE) {
+                const int kx = c0 + q;
+                if (kx < P->NX) x = cmul(x, tf_at(*P, i, kx, N));
+            }
+            dst[COLS ? pidx(i) * NSEQ + q : q * ss + pidx(i)] = x;
+        }
+    }
+    __syncthreads();
+}
+
+template <int N, int NS, int DIR, int NT, bool COLS, int NSEQ, bool TFE, bool SRC_B, int... Rs>
+struct MrcRunPP {
+    static __device__ __forceinline__ void run(float2 *, float2 *, int, const float2 *__restrict__, int,
+                                               const PropParams *, int)
+    {
+    }
+};
+template <int N, int NS, int DIR, int NT, bool COLS, int NSEQ, bool TFE, bool SRC_B, int R, int... Rest>
+struct MrcRunPP<N, NS, DIR, NT, COLS, NSEQ, TFE, SRC_B, R, Rest...> {
+    static __device__ __forceinline__ void run(float2 *a, float2 *b, int ss, const float2 *__restrict__ tw, int tid,
+                                               const PropParams *P, int c0)
+    {
+        mrc_stage_pp<N, R, NS, DIR, NT, COLS, NSEQ, TFE && sizeof...(Rest) == 0>(SRC_B ? b : a, SRC_B ? a : b, ss, tw,
+                                                                                 tid, P, c0);
+        MrcRunPP<N, NS * R, DIR, NT, COLS, NSEQ, TFE, !SRC_B, Rest...>::run(a, b, ss, tw, tid, P, c0);
+    }
+};
+// Stages Rs... from NS0 on, alternating between buffers a and b, starting
+// from a (SRC_B false) or b; the result is in b after an odd count.
+template <int N, int NS0, int DIR, int NT, bool COLS, int NSEQ, bool TFE, bool SRC_B, int... Rs>
+__device__ __forceinline__ void mrc_stages_pp(MrRadices<Rs...>, float2 *a, float2 *b, int ss,
+                                              const float2 *__restrict__ tw, int tid, const PropParams *P = nullptr,
+                                              int c0 = 0)
+{
+    MrcRunPP<N, NS0, DIR, NT, COLS, NSEQ, TFE, SRC_B, Rs...>::run(a, b, ss, tw, tid, P, c0);
+}
+template <int... Rs>
+__host__ __device__ constexpr int mr_count(MrRadices<Rs...>) { return (int)sizeof...(Rs); }
+
 // Stages Rs... from NS0 on (all NT threads, after a barrier).
 template <int N, int NS0, int DIR, int NT, bool COLS, int NSEQ, bool TFE, int... Rs>
 __device__ __forceinline__ void mrc_stages(MrRadices<Rs...>, float2 *s, int ss, const float2 *__restrict__ tw,

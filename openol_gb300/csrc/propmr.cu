@@ -129,12 +129,16 @@ __global__ void __launch_bounds__(NT, 1) k_rows_fwd_mrc(PropParams P)
     }
 }
 
+// Two shared buffers of the column tile (2 C padded_len(N) complex values):
+// the stages alternate between them with one barrier each.
 template <int N, int NT, int C>
 __global__ void __launch_bounds__(NT, 1) k_cols_mrc(PropParams P)
 {
     pdl_enter();
     extern __shared__ float2 sm[];
+    using Plan = MrFixedPlan<N>;
     constexpr int B = N / 16, BT = C * B, BPT = (BT + NT - 1) / NT;
+    float2 *sa = sm, *sb = sm + C * padded_len(N);
     const int NX = P.NX, tid = threadIdx.x, c0 = blockIdx.x * C;
 #pragma unroll
     for (int t = 0; t < BPT; ++t) {
@@ -147,17 +151,20 @@ __global__ void __launch_bounds__(NT, 1) k_cols_mrc(PropParams P)
             v[r] = kx < NX ? __ldcg(P.S + (size_t)(j + (r - 4) * B) * NX + kx) : make_float2(0.f, 0.f);
         dft16_in_mid<-1>(v);
 #pragma unroll
-        for (int r = 0; r < 16; ++r) sm[pidx(16 * j + r) * C + c] = v[outpos<16>(r)];
+        for (int r = 0; r < 16; ++r) sa[pidx(16 * j + r) * C + c] = v[outpos<16>(r)];
     }
     __syncthreads();
-    mrc_stages<N, 16, -1, NT, true, C, true>(typename MrFixedPlan<N>::fwd{}, sm, 0, P.twy, tid, &P, c0);
-    // inverse: the whole plan in shared memory (its radix-16 stage first, with
-    // no twiddles), then the central rows back to S
-    mrc_stages<N, 1, +1, NT, true, C, false>(typename MrFixedPlan<N>::full{}, sm, 0, P.twy, tid);
+    // forward: a -> b -> ... (the transfer function in the last stage)
+    mrc_stages_pp<N, 16, -1, NT, true, C, true, false>(typename Plan::fwd{}, sa, sb, 0, P.twy, tid, &P, c0);
+    // the spectrum is in b after an odd count of forward stages
+    constexpr bool FWD_IN_B = mr_count(typename Plan::fwd{}) % 2 == 1;
+    mrc_stages_pp<N, 1, +1, NT, true, C, false, FWD_IN_B>(typename Plan::full{}, sa, sb, 0, P.twy, tid);
+    constexpr bool INV_IN_B = FWD_IN_B != (mr_count(typename Plan::full{}) % 2 == 1);
+    const float2 *res = INV_IN_B ? sb : sa;
     constexpr int OFF = N / 4;
     for (int e = tid; e < (N / 2) * C; e += NT) {
         const int h = e / C, c = e % C, kx = c0 + c;
-        if (kx < NX) __stcg(P.S + (size_t)h * NX + kx, sm[pidx(h + OFF) * C + c]);
+        if (kx < NX) __stcg(P.S + (size_t)h * NX + kx, res[pidx(h + OFF) * C + c]);
     }
 }
 
@@ -505,9 +512,9 @@ int mr_prepare(PropParams &P)
 
 // Launch shapes of the compile-time plans: {N, threads, rows or columns per CTA}.
 template <int N, int NT, int NSEQ, typename K>
-int mrc_launch(K kern, int count, cudaStream_t st, const PropParams &P, const char *what)
+int mrc_launch(K kern, int count, cudaStream_t st, const PropParams &P, const char *what, int buffers = 1)
 {
-    const int smem = NSEQ * padded_len(N) * (int)sizeof(float2);
+    const int smem = buffers * NSEQ * padded_len(N) * (int)sizeof(float2);
     if (smem > 48 * 1024) {
         const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
@@ -538,7 +545,7 @@ int mrc_rows(const PropParams &P, bool inverse, cudaStream_t st)
 template <int N, int NT, int C>
 int mrc_cols(const PropParams &P, cudaStream_t st)
 {
-    return mrc_launch<N, NT, C>(k_cols_mrc<N, NT, C>, P.NX, st, P, "k_cols_mrc");
+    return mrc_launch<N, NT, C>(k_cols_mrc<N, NT, C>, P.NX, st, P, "k_cols_mrc", 2);
 }
 
 int mr_rows_pass(const PropParams &P, bool inverse, cudaStream_t st)
