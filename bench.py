@@ -1241,13 +1241,13 @@ def run_ours(args):
     x.stream, x.flush, x.barrier, x.max_over_ranks = stream, flush, barrier, max_over_ranks
     x.ws, x.rank, x.local, x.args = ws, rank, local, args
     out = WORKLOADS[args.workload](x, K, W, not args.no_cpu)
-    # The default (CGH) line also carries the other configurations of the
-    # spec set, each run briefly (at most 5 timed steps) with its
-    # accuracy against the FP64 oracle; their CPU baselines are left to their
-    # own --workload runs.
+    # The default (CGH) line also carries the other benchmark configurations
+    # and the reference's default 3840 x 2160 field, each run briefly (at most
+    # 5 timed steps) with its accuracy against the FP64 oracle; their CPU
+    # baselines are left to their own --workload runs.
     configs = {}
     if args.workload == "cgh" and not args.no_configs:
-        for name in ("asm", "wrp", "adam", "batch"):
+        for name in ("asm", "wrp", "adam", "batch", "uhd"):
             o = WORKLOADS[name](x, min(K, 5), 3, False)
             configs[name] = {"metric": o["metric"], "value": o["value"], "unit": o["unit"],
                              "ms_per_step": o["ms_per_step"], "workload": o["config"]["workload"],
