@@ -242,6 +242,8 @@ struct MrRadices {};
 // `full`: the whole plan (the inverse transforms run it in shared memory),
 // radix 16 first and the composite radices 6, 9 and 15 in place of pairs of
 // 2, 3 and 5, so that 7680 takes four stages and 4320 four instead of six.
+// The lengths are those of 3840 x 2160, 1920 x 1080, 2560 x 1440 and
+// 1280 x 720 fields.
 // `fwd`: the plan after its leading radix 16, which the forward transforms
 // apply zero-pruned, straight from global memory.  Listed for the lengths it
 // serves; every stage keeps each thread within 16 values.
@@ -263,6 +265,26 @@ template <> struct MrFixedPlan<3840> {
     static constexpr bool ok = true;
     using full = MrRadices<16, 16, 15>;
     using fwd = MrRadices<16, 15>;
+};
+template <> struct MrFixedPlan<5120> {
+    static constexpr bool ok = true;
+    using full = MrRadices<16, 16, 4, 5>;
+    using fwd = MrRadices<16, 4, 5>;
+};
+template <> struct MrFixedPlan<2880> {
+    static constexpr bool ok = true;
+    using full = MrRadices<16, 4, 5, 9>;
+    using fwd = MrRadices<4, 5, 9>;
+};
+template <> struct MrFixedPlan<2560> {
+    static constexpr bool ok = true;
+    using full = MrRadices<16, 16, 2, 5>;
+    using fwd = MrRadices<16, 2, 5>;
+};
+template <> struct MrFixedPlan<1440> {
+    static constexpr bool ok = true;
+    using full = MrRadices<16, 6, 15>;
+    using fwd = MrRadices<6, 15>;
 };
 template <> struct MrFixedPlan<2160> {
     static constexpr bool ok = true;

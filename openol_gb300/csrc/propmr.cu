@@ -92,7 +92,8 @@ __global__ void __launch_bounds__(MR_NT, 1) k_rows_inv_mr(PropParams P)
 }
 
 // The three passes again for the lengths with a compile-time plan (fftmr.cuh
-// MrFixedPlan), NSEQ rows or columns per CTA of NT threads.  As in the tuned
+// MrFixedPlan: 3840 x 2160, 2560 x 1440, 1920 x 1080 and 1280 x 720 fields),
+// NSEQ rows or columns per CTA of NT threads.  As in the tuned
 // power-of-two passes, the forward transforms start with a radix-16 stage
 // that reads the stored half of the padded input straight from global memory
 // (the padding is never formed), and the column pass multiplies by the
@@ -552,7 +553,9 @@ int mr_rows_pass(const PropParams &P, bool inverse, cudaStream_t st)
 {
     switch (P.NX) {
     case 7680: return mrc_rows<7680, 1024, 2>(P, inverse, st);
+    case 5120: return mrc_rows<5120, 1024, 3>(P, inverse, st);
     case 3840: return mrc_rows<3840, 1024, 4>(P, inverse, st);
+    case 2560: return mrc_rows<2560, 1024, 6>(P, inverse, st);
     default: break;
     }
     const int grid = (P.ny + P.mr_rows - 1) / P.mr_rows;
@@ -565,7 +568,9 @@ int mr_cols_pass(const PropParams &P, cudaStream_t st)
 {
     switch (P.NY) {
     case 4320: return mrc_cols<4320, 1024, 2>(P, st);
+    case 2880: return mrc_cols<2880, 1024, 4>(P, st);
     case 2160: return mrc_cols<2160, 1024, 4>(P, st);
+    case 1440: return mrc_cols<1440, 1024, 8>(P, st);
     default: break;
     }
     const int grid = (P.NX + P.mr_cols - 1) / P.mr_cols;

@@ -61,6 +61,19 @@ def test_asm_reference_default_field():
     assert rel_l2(host(out), ref) < TOL
 
 
+@pytest.mark.parametrize("shape", [(720, 1280), (1440, 2560)])
+def test_asm_hd_and_qhd_fields(shape):
+    """1280 x 720 and 2560 x 1440 fields (padded lengths 2560, 1440 and 5120,
+    2880: compile-time plans)."""
+    u = field(np.random.default_rng(shape[1]), shape)
+    ref = O.asm_prop(u.astype(np.complex128), 5e-6, 5e-6, 532e-9, 0.08)
+    out = og.asm_prop(dev(u), torch.empty(shape, dtype=torch.complex64, device="cuda"), dy=5e-6, dx=5e-6,
+                      lam=532e-9, z=0.08)
+    assert rel_l2(host(out), ref) < TOL
+    f = og.fresnel_prop(dev(u), dy=5e-6, dx=5e-6, lam=532e-9, z=0.3)
+    assert rel_l2(host(f), O.fresnel_prop(u.astype(np.complex128), 5e-6, 5e-6, 532e-9, 0.3)) < TOL
+
+
 @pytest.mark.parametrize("kind", ["fresnel", "arss"])
 def test_chirp_methods_at_1920x1080(kind):
     """Fresnel and ARSS (chirp spectra in the column pass) at 1920 x 1080."""
