@@ -230,13 +230,14 @@ __device__ __forceinline__ void mr_fft(float2 *s, int ss, int nseq, const MrPlan
 }
 
 // ------------------------------------------------- compile-time stage plans
-// The same transform for a few lengths with the plan, the sequence count and
-// the thread count known at compile time: the reference's default field
-// (3840 x 2160, padded 7680 x 4320) and its half (1920 x 1080, padded 3840 x
-// 2160).  The index arithmetic (divisions by B, NS and the sequence count)
-// then folds into multiplications and shifts, and each thread's values stay
-// in registers; the stages, their order and their arithmetic are those of
-// mr_stage, so the results are the run-time plan's bit for bit.
+// The same Stockham transform for a few lengths with the plan, the sequence
+// count and the thread count known at compile time: those of the reference's
+// default field (3840 x 2160, padded 7680 x 4320) and of 1920 x 1080,
+// 2560 x 1440 and 1280 x 720 fields.  The index arithmetic (divisions by B,
+// NS and the sequence count) then folds into multiplications and shifts and
+// each thread's values stay in registers; the plans use the composite radices
+// 6, 9 and 15 as well, and radix-2^k stages form their twiddles as powers.
+// Results agree with the run-time plan's to float rounding, not bit for bit.
 template <int... Rs>
 struct MrRadices {};
 // `full`: the whole plan (the inverse transforms run it in shared memory),
