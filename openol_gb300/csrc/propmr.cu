@@ -191,6 +191,30 @@ __global__ void __launch_bounds__(NT, 1) k_rows_inv_mrc(PropParams P)
     if (P.post_mode == OP_SEED) loss_reduce(lsum, P.loss, tid, NT);
 }
 
+// The chirp spectrum of one axis with a compile-time plan (blockIdx.x == 0),
+// and its elementwise tables (blockIdx.x == 1), as k_chirp_mr.
+template <int N>
+__global__ void __launch_bounds__(1024, 1) k_chirp_mrc(ChirpAxis A, const float2 *tw)
+{
+    pdl_enter();
+    extern __shared__ float2 sm[];
+    const int tid = threadIdx.x;
+    if (blockIdx.x == 0) {
+        for (int j = tid; j < N; j += 1024) {
+            const int m = j < N / 2 ? j : j - N;
+            sm[pidx(j)] = chirp_sample(A, m);
+        }
+        __syncthreads();
+        mrc_stages<N, 1, -1, 1024, false, 1, false>(typename MrFixedPlan<N>::full{}, sm, padded_len(N), tw, tid);
+        for (int j = tid; j < N; j += 1024) {
+            const float2 v = cscale(sm[pidx(j)], A.scale);
+            A.H[j] = A.conj_spec ? cconj(v) : v;
+        }
+    } else {
+        chirp_tables(A, tid, 1024);
+    }
+}
+
 // Chirp spectrum of one axis (blockIdx.x == 0) and its elementwise tables
 // (blockIdx.x == 1); as the power-of-two chirp kernel in prop.cu.
 __global__ void __launch_bounds__(MR_NT, 1) k_chirp_mr(ChirpAxis A, MrPlan pl, const float2 *tw)
@@ -586,8 +610,26 @@ int mr_chirp_axis(const ChirpAxis &A, cudaStream_t st)
     const float2 *tw = nullptr;
     if (int rc = mr_table(A.L, &tw)) return rc;
     const int smem = padded_len(A.L) * (int)sizeof(float2);
+    const int grid = (A.ta || A.tb) ? 2 : 1;
+    auto fixed = [&](auto kern) -> int {
+        if (int rc = mr_smem(kern, smem)) return rc;
+        kern<<<grid, 1024, smem, st>>>(A, tw);
+        count_launch();
+        return check_launch("k_chirp_mrc");
+    };
+    switch (A.L) {
+    case 7680: return fixed(k_chirp_mrc<7680>);
+    case 5120: return fixed(k_chirp_mrc<5120>);
+    case 4320: return fixed(k_chirp_mrc<4320>);
+    case 3840: return fixed(k_chirp_mrc<3840>);
+    case 2880: return fixed(k_chirp_mrc<2880>);
+    case 2560: return fixed(k_chirp_mrc<2560>);
+    case 2160: return fixed(k_chirp_mrc<2160>);
+    case 1440: return fixed(k_chirp_mrc<1440>);
+    default: break;
+    }
     if (int rc = mr_smem(k_chirp_mr, smem)) return rc;
-    k_chirp_mr<<<(A.ta || A.tb) ? 2 : 1, MR_NT, smem, st>>>(A, pl, tw);
+    k_chirp_mr<<<grid, MR_NT, smem, st>>>(A, pl, tw);
     count_launch();
     return check_launch("k_chirp_mr");
 }
