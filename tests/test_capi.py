@@ -243,3 +243,29 @@ def test_workspace_size():
     ws = L.olg_prop_workspace_bytes(1024, 1024)
     assert ws >= 1024 * 2048 * 8
     assert ws < 1024 * 2048 * 8 * 1.1
+
+
+def test_cgh_host_sequence_python_checks_without_gpu():
+    """openol_gb300.cgh_fresnel_gemm_host checks its host tensors before any
+    device work: one hologram per cloud, n x 3 float32 clouds, ny x nx
+    complex64 holograms, per-point amplitudes of the cloud's length."""
+    import pytest
+    import torch
+
+    import openol_gb300 as og
+
+    pts = [torch.zeros((4, 3), dtype=torch.float32)]
+    holo = [torch.zeros((6, 8), dtype=torch.complex64)]
+    kw = dict(ny=6, nx=8, py=8e-6, px=8e-6, lam=532e-9)
+    with pytest.raises(ValueError):
+        og.cgh_fresnel_gemm_host(pts, holo * 2, **kw)
+    with pytest.raises(TypeError):
+        og.cgh_fresnel_gemm_host([torch.zeros((4, 3), dtype=torch.float64)], holo, **kw)
+    with pytest.raises(ValueError):
+        og.cgh_fresnel_gemm_host([torch.zeros((4, 2), dtype=torch.float32)], holo, **kw)
+    with pytest.raises(ValueError):
+        og.cgh_fresnel_gemm_host(pts, [torch.zeros((5, 8), dtype=torch.complex64)], **kw)
+    with pytest.raises(ValueError):
+        og.cgh_fresnel_gemm_host(pts, holo, amp=[torch.zeros(3, dtype=torch.float32)], **kw)
+    with pytest.raises(TypeError):
+        og.cgh_fresnel_gemm_host(pts, [torch.zeros((6, 8), dtype=torch.complex128)], **kw)
